@@ -1,0 +1,331 @@
+/*
+ * raycer_gb300 — C ABI of the GB300 (sm_103a) path-tracing / ray-casting hot path.
+ *
+ * This is the drop-in boundary for raycer's GPU tracer. Every entry point
+ * replaces one piece of the reference's OpenCL tracer host side
+ * (src/OpenCL/CLTracer.{h,cpp}, src/OpenCL/CLScene.cpp) or of the CPU
+ * Tracer API (src/Raytracing/Tracers/Tracer.h), as cited beside it.
+ *
+ * Conventions
+ *   - Plain C: pointers + sizes, no C++ or torch types. Nothing throws.
+ *   - Every function returns an rc_status (0 = RC_OK). On failure the
+ *     handle's message is available from rc_last_error(). The C++ wrapper
+ *     (raycer_gb300/cpp/CudaTracer.hpp) turns status + message into
+ *     std::runtime_error, which is how CLManager::checkError reports errors
+ *     (src/OpenCL/CLManager.cpp:73-101).
+ *   - A handle owns all device memory it allocates (like CLTracer owns its
+ *     cl_mem objects, CLTracer.cpp:38-43, 165-170, 240-260). Caller-owned
+ *     host arrays are only read during the call; no pointer is retained.
+ *   - One handle per host thread / stream. Calls on one handle are serialised
+ *     by the caller, as the reference's render thread does
+ *     (src/Runners/ConsoleRunner.cpp:94-142).
+ *   - Pixel (0,0) is the bottom-left pixel and y grows upwards
+ *     (src/Rendering/Image.h:10-14); images are row-major RGBA float32.
+ */
+#ifndef RAYCER_GB300_H
+#define RAYCER_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------------ */
+/* Status codes                                                              */
+
+typedef enum rc_status
+{
+    RC_OK = 0,
+    RC_INVALID_ARG = 1,  /* bad pointer, size or record field              */
+    RC_OOM = 2,          /* device or host allocation refused              */
+    RC_CUDA = 3,         /* a CUDA runtime call failed (message has it)    */
+    RC_CANCELLED = 4,    /* the caller's cancel flag was raised            */
+    RC_TIMEOUT = 5,      /* a kernel's iteration budget ran out            */
+    RC_NOT_READY = 6,    /* call order: e.g. render before upload/resize   */
+    RC_UNSUPPORTED = 7,  /* valid in the reference, not in this build      */
+    RC_DEVICE_ERROR = 8  /* a kernel reported an error status (e.g. stack) */
+} rc_status;
+
+typedef struct rc_tracer rc_tracer; /* opaque handle: one tracer on one GPU */
+
+/* ------------------------------------------------------------------------ */
+/* Plain records (host side)                                                 */
+
+/* Material fields the hot path reads: src/Raytracing/Material.h:23-44,
+ * flattened like OpenCL::Material (src/OpenCL/CLStructs.h, CLScene.cpp:110-147).
+ * Textures are not supported (texture indices of the reference = -1). */
+typedef struct rc_material
+{
+    float diffuse[3];     /* diffuseReflectance                          */
+    float emittance[3];   /* emittance                                   */
+    int32_t is_emissive;  /* isEmissive                                  */
+    int32_t non_shadowing;/* nonShadowing: skipped by shadow rays        */
+    int32_t invert_normal;/* invertNormal                                */
+    int32_t reserved;     /* must be 0                                   */
+} rc_material;
+
+/* Float32 camera record, the fields CLScene::readSceneCamera copies
+ * (src/OpenCL/CLScene.cpp:242-262) for a perspective camera. Fill it with
+ * rc_camera_from_euler() or from the reference's Camera::cameraState. */
+typedef struct rc_camera
+{
+    float position[3];
+    float forward[3];
+    float right[3];
+    float up[3];
+    float image_plane_center[3];
+    float aspect_ratio;        /* height / width        (Camera.cpp:33) */
+    float image_plane_width;   /* width - 1             (Camera.cpp:31) */
+    float image_plane_height;  /* height - 1            (Camera.cpp:32) */
+} rc_camera;
+
+typedef enum rc_tracer_type { RC_TRACER_RAY = 0, RC_TRACER_PATH = 1 } rc_tracer_type;
+/* Values follow the reference's enums (Rendering/Samplers/Sampler.h:24,
+ * Rendering/Filters/Filter.h:10, Rendering/ToneMappers/ToneMapper.h:15). */
+typedef enum rc_sampler_type { RC_SAMPLER_CENTER = 0, RC_SAMPLER_RANDOM = 1, RC_SAMPLER_CMJ = 4 } rc_sampler_type;
+typedef enum rc_filter_type { RC_FILTER_BOX = 0 } rc_filter_type;
+typedef enum rc_tonemapper_type { RC_TONEMAP_PASSTHROUGH = 0, RC_TONEMAP_REINHARD = 3 } rc_tonemapper_type;
+
+/* Scene::General fields on the hot path (src/Raytracing/Scene.h:89-131)
+ * plus the GPU-only knobs. */
+typedef struct rc_general
+{
+    int32_t tracer_type;             /* rc_tracer_type (tracerType)                 */
+    int32_t max_path_length;         /* maxPathLength: segments per path            */
+    int32_t path_sample_count;       /* pathSampleCount: paths per camera ray       */
+    int32_t multi_sample_count_sqrt; /* multiSampleCountSqrt: n x n film samples    */
+    int32_t multi_sampler_type;      /* rc_sampler_type (multiSamplerType)          */
+    int32_t filter_type;             /* rc_filter_type (multiSamplerFilterType)     */
+    float filter_radius[2];          /* BoxFilter radius (BoxFilter.h:16: 0.5, 0.5) */
+    float ray_start_offset;          /* rayStartOffset (Scene.h:95: 1e-5)           */
+    float background[3];             /* backgroundColor (RAY tracer, miss)          */
+    int32_t russian_roulette_depth;  /* 0 = off (reference); else first RR segment  */
+    int32_t reserved;                /* must be 0                                   */
+    uint64_t seed;                   /* random stream seed (paths, CMJ permutation) */
+} rc_general;
+
+/* Scene::ToneMapper fields (src/Raytracing/Scene.h:135-159). */
+typedef struct rc_tonemapper
+{
+    int32_t type;          /* rc_tonemapper_type */
+    int32_t apply_gamma;
+    int32_t should_clamp;
+    int32_t reserved;      /* must be 0 */
+    double gamma;
+    double key;
+} rc_tonemapper;
+
+/* DirectionalLight (src/Raytracing/Lights.h:47-57): direction the light
+ * travels; shadow rays go toward -direction (Raytracer.cpp:499). */
+typedef struct rc_directional_light
+{
+    float direction[3];
+    float color[3];
+    float intensity;
+} rc_directional_light;
+
+/* One node of the reference's flat BVH (FlatBVHNode, FlatBVH.h:38-53):
+ * preorder array; left child = i + 1, right child = i + right_offset,
+ * leaf <=> right_offset == 0. */
+typedef struct rc_bvh_node
+{
+    double aabb_min[3];
+    double aabb_max[3];
+    int64_t right_offset;
+    uint64_t start_offset;
+    uint64_t primitive_count;
+} rc_bvh_node;
+
+/* Ray for the generic cast entry points: origin, direction (need not be
+ * normalised), and the [t_min, t_max] window of Ray::minDistance /
+ * maxDistance (src/Raytracing/Ray.h:16-17). */
+typedef struct rc_ray
+{
+    float origin[3];
+    float t_min;
+    float direction[3];
+    float t_max;
+} rc_ray;
+
+/* Hit record: prim = caller's triangle index (the reference's primitive id
+ * minus the first id) or -1 for a miss; t = hit distance; u, v =
+ * barycentrics of the reported hit. */
+typedef struct rc_hit
+{
+    int32_t prim;
+    float t;
+    float u;
+    float v;
+} rc_hit;
+
+/* Per-pixel ray-cast result (RAY tracer): primary hit and the directional
+ * light's shadow query (Raytracer::calculateShadowAmount, Raytracer.cpp:497). */
+typedef struct rc_cast_pixel
+{
+    int32_t prim;      /* primary hit triangle (caller index) or -1          */
+    float t;           /* primary hit distance                               */
+    int32_t occluder;  /* first triangle the shadow ray found, -1 = lit       */
+    int32_t flags;     /* bit0: primary hit; bit1: shadow ray cast; bit2: occluded */
+} rc_cast_pixel;
+
+/* Traversal order of the closest-hit query.
+ * RC_ORDER_REFERENCE: the reference's preorder DFS (left subtree first, no
+ *   distance culling; FlatBVH::intersect FlatBVH.cpp:22-75).
+ * RC_ORDER_NEAREST: nearer child first + distance culling; reports the same
+ *   hit (minimum t, ties to the later triangle in BVH order, Triangle.cpp:93). */
+typedef enum rc_traversal_order { RC_ORDER_REFERENCE = 0, RC_ORDER_NEAREST = 1 } rc_traversal_order;
+
+typedef struct rc_stats
+{
+    uint64_t rays_traced;      /* BVH queries in the last render / cast call   */
+    uint64_t node_visits;      /* inner-node pair tests (when counting is on)  */
+    uint64_t tri_tests;        /* triangle tests (when counting is on)         */
+    double last_ms;            /* device time of the last render / cast call   */
+    uint64_t bvh_inner_nodes;  /* inner nodes of the device BVH                */
+    uint64_t bvh_depth;        /* depth of the uploaded BVH                    */
+    uint64_t device_bytes;     /* device memory held by the handle             */
+} rc_stats;
+
+/* ------------------------------------------------------------------------ */
+/* Lifetime — CLTracer::CLTracer / ~CLTracer (CLTracer.cpp:32-43) and
+ * CLTracer::initializeKernels / releaseKernels (CLTracer.cpp:45-98).        */
+
+rc_status rc_create(rc_tracer** out, int device);
+void rc_destroy(rc_tracer* h);
+const char* rc_last_error(const rc_tracer* h);
+const char* rc_version(void);
+
+/* ------------------------------------------------------------------------ */
+/* Scene — CLTracer::initializeBuffers + CLScene::readSceneFull
+ * (CLTracer.cpp:173-238, CLScene.cpp:72-240).                               */
+
+/* Upload triangles (vertices: n*9 doubles, v0 v1 v2, caller order) with a
+ * material index per triangle into `materials`, and build the SAH flat BVH
+ * on the host exactly as FlatBVH::build does (FlatBVH.cpp:89-343: SAH over
+ * {AABB centre, centroid median} per axis, in-place partition, half split
+ * fallback) with BVHBuildInfo.maxLeafSize = max_leaf_size (1..15). */
+rc_status rc_upload_scene(rc_tracer* h, const double* vertices, const uint32_t* material_index, int64_t n,
+                          const rc_material* materials, int32_t material_count, uint32_t max_leaf_size);
+
+/* Same, but with a BVH the caller already built (the reference's
+ * scene.rootBVH.bvh.flatNodes and the order of its orderedPrimitives, as
+ * caller triangle indices) — the verbatim node copy of
+ * CLScene.cpp:224-237. The node array is validated before use. */
+rc_status rc_upload_scene_prebuilt(rc_tracer* h, const double* vertices, const uint32_t* material_index, int64_t n,
+                                   const rc_material* materials, int32_t material_count,
+                                   const rc_bvh_node* nodes, int64_t node_count, const uint64_t* ordered_index);
+
+/* The flat BVH of the last upload in the reference's FlatBVHNode form (for
+ * checks and for caching; nodes: node_count entries, ordered_index: n). */
+rc_status rc_get_bvh(const rc_tracer* h, rc_bvh_node* nodes, int64_t node_capacity, int64_t* node_count,
+                     uint64_t* ordered_index, int64_t index_capacity);
+
+/* Host-only SAH build (no device memory, no GPU needed): the BVH
+ * rc_upload_scene would build, returned in the reference's FlatBVHNode form
+ * (FlatBVH::build, FlatBVH.cpp:89-204). Call with nodes == NULL to get the
+ * node count. ordered_index receives n entries. */
+rc_status rc_build_bvh(const double* vertices, int64_t n, uint32_t max_leaf_size, rc_bvh_node* nodes,
+                       int64_t node_capacity, int64_t* node_count, uint64_t* ordered_index, uint32_t* depth);
+
+/* Release the scene buffers — CLTracer::releaseBuffers (CLTracer.cpp:240). */
+rc_status rc_release_scene(rc_tracer* h);
+
+/* Per-frame records — CLTracer::uploadMinimalData (CLTracer.cpp:441-451)
+ * and the General / ToneMapper / light uploads of uploadFullData (:389). */
+rc_status rc_set_camera(rc_tracer* h, const rc_camera* camera);
+rc_status rc_set_general(rc_tracer* h, const rc_general* general);
+rc_status rc_set_tonemapper(rc_tracer* h, const rc_tonemapper* tonemapper);
+rc_status rc_set_directional_lights(rc_tracer* h, const rc_directional_light* lights, int32_t count);
+
+/* Camera::update's perspective basis (Camera.cpp:157-160, 277-283:
+ * ONB::fromNormal(EulerAngle::getDirection()), imagePlaneDistance =
+ * 0.5 / tan(fov / 2), fov horizontal, degrees) in float64, cast to the
+ * float32 record, for a width x height film (Camera::setImagePlaneSize). */
+rc_status rc_camera_from_euler(const double position[3], double pitch, double yaw, double roll, double fov,
+                               uint64_t width, uint64_t height, rc_camera* out);
+
+/* Default General / ToneMapper records (the reference's defaults,
+ * Scene.h:89-159, with box filter and the given tracer type). */
+void rc_general_defaults(rc_general* out, int32_t tracer_type);
+void rc_tonemapper_defaults(rc_tonemapper* out);
+
+/* ------------------------------------------------------------------------ */
+/* Film — CLTracer::initializeImageBuffers / releaseImageBuffers / clear
+ * (CLTracer.cpp:100-171, 325-333).                                          */
+
+rc_status rc_resize(rc_tracer* h, uint64_t width, uint64_t height);
+rc_status rc_clear(rc_tracer* h);
+
+/* ------------------------------------------------------------------------ */
+/* Render — Tracer::run / CLTracer::run (Tracer.cpp:58-113, CLTracer.cpp:262).
+ * Renders pixel_count pixels starting at pixel_start of a film_width x
+ * film_height image into film pixels [0, pixel_count) — the TracerState
+ * contract (TracerState.h:13-26) the network runner uses
+ * (NetworkRunner.cpp:398-417). PATH: adds filter-weighted samples to the
+ * film. RAY: casts the primary ray of every pixel and, for each hit, one
+ * shadow ray per directional light, into the cast buffer (rc_read_cast).
+ * cancel: optional host flag polled between launches; when it is non-zero
+ * the call returns RC_CANCELLED with the film holding whole passes only.
+ * pixels_processed: optional; set to pixel_count on success
+ * (Tracer.cpp:111-112, CLTracer.cpp:304). Blocks until the device is done. */
+rc_status rc_render(rc_tracer* h, uint64_t pixel_start, uint64_t pixel_count,
+                    const volatile int32_t* cancel, uint64_t* pixels_processed);
+
+/* Film::generateToneMappedImage (Film.cpp:61-69) with the handle's tone
+ * mapper (ReinhardToneMapper::apply, ReinhardToneMapper.cpp:18-86), and the
+ * download of CLTracer::downloadImage (CLTracer.cpp:307): out_rgba =
+ * film pixels x 4 floats on the host. */
+rc_status rc_resolve(rc_tracer* h, float* out_rgba);
+
+/* Linear film resolve (cumulativeColor / filterWeightSum) to the host, and
+ * the raw accumulators (r, g, b, weight per pixel). */
+rc_status rc_read_linear(rc_tracer* h, float* out_rgba);
+rc_status rc_read_film(rc_tracer* h, float* out_rgbw);
+
+/* Tone-map a caller film (pixels x {r, g, b, weight sum}, host floats) with
+ * the handle's tone mapper: Film::generateToneMappedImage on any film
+ * (Film.cpp:61-69), e.g. one the CPU-compatible adapter accumulated.
+ * Copies in and out are included. */
+rc_status rc_tonemap_film(rc_tracer* h, const float* film_rgbw, uint64_t pixels, float* out_rgba);
+
+/* Per-pixel results of the last RAY render (film pixels entries). */
+rc_status rc_read_cast(rc_tracer* h, rc_cast_pixel* out);
+
+/* ------------------------------------------------------------------------ */
+/* Ray queries through the root BVH — the intersect calls of
+ * PathTracer::traceRecursive (PathTracer.cpp:36-40) and
+ * Raytracer::calculateShadowAmount (Raytracer.cpp:497-522), batched.
+ * any_hit != 0: shadow-ray semantics (isShadowRay + fastOcclusion:
+ * nonShadowing triangles skipped, first hit found is reported).           */
+
+/* Host buffers: rays -> hits, copies included. */
+rc_status rc_cast(rc_tracer* h, const rc_ray* rays, int64_t n, int32_t any_hit, int32_t order, rc_hit* hits);
+
+/* Device buffers (device pointers, on the handle's stream); no copies. */
+rc_status rc_cast_device(rc_tracer* h, const rc_ray* d_rays, int64_t n, int32_t any_hit, int32_t order,
+                         rc_hit* d_hits);
+
+/* Primary + shadow cast of whole frames from host-side primary rays: the
+ * RAY render's ray set fed from the host (n rays in, n rc_cast_pixel out,
+ * host buffers, copies included). Uses the first directional light. */
+rc_status rc_cast_with_shadow(rc_tracer* h, const rc_ray* rays, int64_t n, int32_t order, rc_cast_pixel* out);
+
+/* ------------------------------------------------------------------------ */
+/* Options, statistics, synchronisation.                                     */
+
+/* Closest-hit traversal order for renders (rc_traversal_order). */
+rc_status rc_set_traversal_order(rc_tracer* h, int32_t order);
+/* Count node / triangle tests in kernels (slower; off by default). */
+rc_status rc_set_counting(rc_tracer* h, int32_t enable);
+rc_status rc_get_stats(const rc_tracer* h, rc_stats* out);
+/* The handle's CUDA stream (cudaStream_t) as an opaque pointer. */
+void* rc_stream(rc_tracer* h);
+rc_status rc_sync(rc_tracer* h);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RAYCER_GB300_H */

@@ -1,0 +1,97 @@
+// Device data layout of the scene and of the per-frame records (HBM).
+//
+// Scene (uploaded once, read by every traversal):
+//   DevNode  64 B per INNER node of the flat BVH, both child boxes inline
+//            (the 2-wide node of Aila & Laine 2009). One 64-B fetch tests two
+//            children; leaves are not stored as nodes — a child link < 0 is
+//            ~((start << 4) | count) into the triangle arrays.
+//            1M triangles, leaf <= 4: ~264k inner nodes = 17 MB.
+//   DevTri   48 B per triangle in BVH order (the order of the reference's
+//            FlatBVH::orderedPrimitives): v0, e1 = v1 - v0, e2 = v2 - v0 in
+//            float32 (the same float subtraction intersectTriangle performs,
+//            intersections.cl:37-38), material index + nonShadowing bit, and
+//            the caller's triangle index. 1M triangles = 48 MB.
+//   DevShade 48 B per triangle in BVH order: geometric normal, tangent,
+//            bitangent (Triangle::initialize, Triangle.cpp:18-47, float64 on
+//            the host, cast like CLScene.cpp:214-216); read once per hit.
+//   DevMat   32 B per material.
+// Everything is 16-B aligned and fetched with 128-bit loads.
+#pragma once
+
+#include <stdint.h>
+
+#if defined(__CUDACC__)
+#include <cuda_runtime.h>
+#else
+#include <vector_types.h>
+#endif
+
+namespace rcx
+{
+
+struct __align__(16) DevNode
+{
+    float4 xy0;  // child 0: lo.x, hi.x, lo.y, hi.y
+    float4 xy1;  // child 1: lo.x, hi.x, lo.y, hi.y
+    float4 z01;  // child 0 lo.z, hi.z; child 1 lo.z, hi.z
+    int4 link;   // child 0 (left), child 1 (right), depth-first subtree end, reserved
+};
+
+struct __align__(16) DevTri
+{
+    float4 a;  // v0.x v0.y v0.z e1.x
+    float4 b;  // e1.y e1.z e2.x e2.y
+    float4 c;  // e2.z, meta (as bits), caller index (as bits), 0
+};
+
+struct __align__(16) DevShade
+{
+    float4 n;   // normal xyz, unused
+    float4 t;   // tangent xyz, unused
+    float4 bt;  // bitangent xyz, unused
+};
+
+struct __align__(16) DevMat
+{
+    float4 diffuse;    // rgb, unused
+    float4 emittance;  // rgb, flags as bits (bit0 emissive, bit1 nonShadowing, bit2 invertNormal)
+};
+
+// meta word of DevTri.c.y
+constexpr uint32_t kMetaMaterialMask = 0x00ffffffu;
+constexpr uint32_t kMetaNonShadowing = 0x80000000u;
+
+constexpr uint32_t kMatEmissive = 1u;
+constexpr uint32_t kMatNonShadowing = 2u;
+constexpr uint32_t kMatInvertNormal = 4u;
+
+constexpr int kLeafCountBits = 4;
+constexpr int kMaxStack = 64;
+
+// Device scene handed to every kernel by value.
+struct DevScene
+{
+    const DevNode* nodes;
+    const DevTri* tris;
+    const DevShade* shade;
+    const DevMat* mats;
+    int rootLink;  // >= 0: inner node 0; < 0: the root is a leaf (~leaf code)
+    int numTris;
+    int numMats;
+    int pad;
+};
+
+// Float32 camera record used by the kernels (same fields as rc_camera).
+struct DevCamera
+{
+    float pos[3];
+    float fwd[3];
+    float right[3];
+    float up[3];
+    float center[3];
+    float aspect;
+    float ipw;
+    float iph;
+};
+
+}  // namespace rcx

@@ -1,0 +1,91 @@
+// Internal definition of the rc_tracer handle and the render helpers shared
+// by the host translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/raycer_gb300.h"
+#include "bvh_build.h"
+#include "device_types.h"
+#include "kernels.h"
+
+struct rc_tracer
+{
+    int device = 0;
+    int numSMs = 1;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr;
+    cudaEvent_t ev1 = nullptr;
+    std::string err;
+
+    // Scene (device layout of device_types.h) and its host flat-BVH copy.
+    rcx::DevNode* dNodes = nullptr;
+    rcx::DevTri* dTris = nullptr;
+    rcx::DevShade* dShade = nullptr;
+    rcx::DevMat* dMats = nullptr;
+    size_t innerCount = 0;
+    int64_t nTris = 0;
+    int32_t nMats = 0;
+    int32_t rootLink = 0;
+    uint64_t bvhInner = 0;
+    uint64_t bvhDepth = 0;
+    bool sceneReady = false;
+    std::vector<rcx::BuildNode> hostNodes;
+    std::vector<uint32_t> hostOrder;
+
+    // Per-frame records.
+    rc_camera camera{};
+    bool cameraSet = false;
+    rc_general general{};
+    rc_tonemapper tonemapper{};
+    std::vector<rc_directional_light> lights;
+    int order = RC_ORDER_NEAREST;
+    int counting = 0;
+    uint32_t frameIndex = 0;  // advances per PATH render, reset by rc_clear
+
+    // Film: r, g, b, filter-weight sum per pixel (float32), and the RAY
+    // tracer's per-pixel cast records.
+    uint64_t width = 0;
+    uint64_t height = 0;
+    uint64_t filmPixels = 0;
+    float4* dFilm = nullptr;
+    rc_cast_pixel* dCast = nullptr;
+    int* dQueue = nullptr;
+
+    // Path-tracer wavefront state (grow-only; see pathtrace.cu).
+    void* dPath = nullptr;
+    size_t capPath = 0;
+    uint64_t pathSlots = 0;
+    unsigned* dCounts = nullptr;
+    size_t capCounts = 0;
+
+    // Tone-mapping scratch (partial sums) and output staging.
+    void* dTone = nullptr;
+    size_t capTone = 0;
+    void* dImage = nullptr;
+    size_t capImage = 0;
+
+    // Scratch for the host-buffer entry points.
+    void* dTmpA = nullptr;
+    size_t capTmpA = 0;
+    void* dTmpB = nullptr;
+    size_t capTmpB = 0;
+
+    rcx::DevControl* dCtl = nullptr;
+    rc_stats stats{};
+    size_t deviceBytes = 0;
+};
+
+namespace rcx
+{
+
+rc_status raycast_into(rc_tracer* h, const rc_ray* dRays, uint64_t pixelStart, uint64_t count, int order,
+                       rc_cast_pixel* dOut, int* dQueue);
+rc_status render_raycast(rc_tracer* h, uint64_t pixelStart, uint64_t count, const rc_ray* dRays);
+rc_status render_path(rc_tracer* h, uint64_t pixelStart, uint64_t count, const volatile int32_t* cancel);
+void release_render_buffers(rc_tracer* h);
+
+}  // namespace rcx

@@ -1,0 +1,43 @@
+// Host-callable launchers of the device kernels (defined in the .cu files).
+// All launches go to the given stream; none synchronises.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/raycer_gb300.h"
+#include "device_types.h"
+
+namespace rcx
+{
+
+// Small device-side control block shared by the kernels of one handle.
+struct DevControl
+{
+    unsigned int head[8];          // work-queue heads / queue counts
+    unsigned long long stats[4];   // rays, node fetches, triangle tests, spare
+    int error;                     // bit0: traversal stack overflow
+    int pad[3];
+};
+
+struct LaunchInfo
+{
+    cudaStream_t stream;
+    int numSMs;
+    int counting;  // count node / triangle tests
+};
+
+// Generic ray queries (rc_ray -> rc_hit).
+cudaError_t launch_cast(const LaunchInfo& li, const DevScene& sc, const rc_ray* rays, int64_t n, int anyHit,
+                        int order, rc_hit* hits, DevControl* ctl);
+
+// Ray-cast frame: primary closest hit per pixel + shadow any-hit per hit.
+// Primary rays come from the camera (rays == nullptr) or from `rays`
+// (one per pixel, caller order). Writes out[0..count); shadowQueue needs
+// `count` entries. ctl->head[0], head[1], head[2] must be zero on entry.
+cudaError_t launch_raycast(const LaunchInfo& li, const DevScene& sc, const DevCamera& cam, const rc_ray* rays,
+                           uint64_t pixelStart, int64_t count, int64_t width, int order, int castShadow,
+                           float3 dirToLight, float rayStartOffset, rc_cast_pixel* out, int* shadowQueue,
+                           DevControl* ctl);
+
+}  // namespace rcx

@@ -1,0 +1,290 @@
+// Host orchestration of the PATH tracer and of the film read-back / tone
+// mapping entry points (rc_render for PATH, rc_resolve, rc_read_linear,
+// rc_read_film).
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <string>
+
+#include "host_internal.h"
+#include "pathtrace.h"
+
+using namespace rcx;
+
+namespace
+{
+
+// Target slots per pass: 4M paths x 88 B of state = 352 MB.
+constexpr uint64_t kTargetSlots = uint64_t(1) << 22;
+
+rc_status fail(rc_tracer* h, rc_status s, const std::string& msg)
+{
+    h->err = msg;
+    return s;
+}
+
+rc_status cuda_fail(rc_tracer* h, cudaError_t e, const char* what)
+{
+    std::string msg = std::string(what) + ": " + cudaGetErrorString(e);
+    return fail(h, e == cudaErrorMemoryAllocation ? RC_OOM : RC_CUDA, msg);
+}
+
+#define RC_CUDA_TRY(h, expr, what)             \
+    do                                         \
+    {                                          \
+        cudaError_t e_ = (expr);               \
+        if (e_ != cudaSuccess)                 \
+            return cuda_fail((h), e_, (what)); \
+    } while (0)
+
+rc_status grow(rc_tracer* h, void** ptr, size_t* cap, size_t bytes, const char* what)
+{
+    if (*ptr && *cap >= bytes)
+        return RC_OK;
+    if (*ptr)
+    {
+        cudaFree(*ptr);
+        h->deviceBytes -= *cap;
+        *ptr = nullptr;
+        *cap = 0;
+    }
+    cudaError_t e = cudaMalloc(ptr, bytes);
+    if (e != cudaSuccess)
+    {
+        cudaGetLastError();
+        return cuda_fail(h, e, what);
+    }
+    *cap = bytes;
+    h->deviceBytes += bytes;
+    return RC_OK;
+}
+
+}  // namespace
+
+namespace rcx
+{
+
+void release_render_buffers(rc_tracer* h)
+{
+    void** ptrs[] = { &h->dPath, reinterpret_cast<void**>(&h->dCounts), &h->dTone, &h->dImage };
+    size_t* caps[] = { &h->capPath, &h->capCounts, &h->capTone, &h->capImage };
+    for (int i = 0; i < 4; ++i)
+    {
+        if (*ptrs[i])
+        {
+            cudaFree(*ptrs[i]);
+            h->deviceBytes -= *caps[i];
+            *ptrs[i] = nullptr;
+            *caps[i] = 0;
+        }
+    }
+    h->pathSlots = 0;
+}
+
+rc_status render_path(rc_tracer* h, uint64_t pixelStart, uint64_t count, const volatile int32_t* cancel)
+{
+    const rc_general& g = h->general;
+    const int n = g.multi_sample_count_sqrt;
+    const int P = g.path_sample_count;
+    const uint64_t spp = uint64_t(n) * uint64_t(n) * uint64_t(P);
+    if (spp > kTargetSlots)
+        return fail(h, RC_UNSUPPORTED, "render: samples per pixel exceed one pass");
+    const uint64_t pixelsPerPass = std::max<uint64_t>(1, kTargetSlots / spp);
+    const uint64_t slots = std::min<uint64_t>(pixelsPerPass, count) * spp;
+
+    if (h->pathSlots < slots)
+    {
+        void* p = h->dPath;
+        size_t cap = h->capPath;
+        rc_status s = grow(h, &p, &cap, size_t(slots) * kPathBytesPerSlot, "allocate path state");
+        h->dPath = p;
+        h->capPath = cap;
+        if (s != RC_OK)
+            return s;
+        h->pathSlots = slots;
+    }
+    size_t countsBytes = size_t(g.max_path_length + 1) * 4 * sizeof(unsigned);
+    {
+        void* p = h->dCounts;
+        size_t cap = h->capCounts;
+        rc_status s = grow(h, &p, &cap, countsBytes, "allocate queue counters");
+        h->dCounts = static_cast<unsigned*>(p);
+        h->capCounts = cap;
+        if (s != RC_OK)
+            return s;
+    }
+
+    const uint64_t S = h->pathSlots;
+    char* base = static_cast<char*>(h->dPath);
+    PathParams p{};
+    p.sc.nodes = h->dNodes;
+    p.sc.tris = h->dTris;
+    p.sc.shade = h->dShade;
+    p.sc.mats = h->dMats;
+    p.sc.rootLink = h->rootLink;
+    p.sc.numTris = int(h->nTris);
+    p.sc.numMats = int(h->nMats);
+    for (int k = 0; k < 3; ++k)
+    {
+        p.cam.pos[k] = h->camera.position[k];
+        p.cam.fwd[k] = h->camera.forward[k];
+        p.cam.right[k] = h->camera.right[k];
+        p.cam.up[k] = h->camera.up[k];
+        p.cam.center[k] = h->camera.image_plane_center[k];
+    }
+    p.cam.aspect = h->camera.aspect_ratio;
+    p.cam.ipw = h->camera.image_plane_width;
+    p.cam.iph = h->camera.image_plane_height;
+    p.o = reinterpret_cast<float4*>(base);
+    p.d = reinterpret_cast<float4*>(base + S * 16);
+    p.thr = reinterpret_cast<float4*>(base + S * 32);
+    p.res = reinterpret_cast<float4*>(base + S * 48);
+    p.hit = reinterpret_cast<int4*>(base + S * 64);
+    p.qa = reinterpret_cast<int*>(base + S * 80);
+    p.qb = reinterpret_cast<int*>(base + S * 84);
+    p.counts = h->dCounts;
+    p.film = h->dFilm;
+    p.ctl = h->dCtl;
+    p.pixelStart = pixelStart;
+    p.width = int64_t(h->width);
+    p.n = n;
+    p.P = P;
+    p.spp = int(spp);
+    p.samplerType = g.multi_sampler_type;
+    p.rx = g.filter_radius[0];
+    p.ry = g.filter_radius[1];
+    // BoxFilter::setRadius (BoxFilter.cpp:15-21): weight = 1 / (2 r).
+    p.wx = 1.0f / (2.0f * g.filter_radius[0]);
+    p.wy = 1.0f / (2.0f * g.filter_radius[1]);
+    p.rayStartOffset = g.ray_start_offset;
+    p.maxPathLength = g.max_path_length;
+    p.rrDepth = g.russian_roulette_depth;
+    p.seed = g.seed;
+    p.frame = h->frameIndex;
+
+    RC_CUDA_TRY(h, cudaMemsetAsync(h->dCtl, 0, sizeof(DevControl), h->stream), "reset control block");
+    RC_CUDA_TRY(h, cudaEventRecord(h->ev0, h->stream), "record start event");
+    for (uint64_t done = 0; done < count; done += pixelsPerPass)
+    {
+        if (done > 0 && cancel && *cancel)
+        {
+            cudaStreamSynchronize(h->stream);
+            h->frameIndex++;
+            return fail(h, RC_CANCELLED, "render: cancelled");
+        }
+        uint64_t np = std::min(pixelsPerPass, count - done);
+        p.passPixel = done;
+        p.nslots = int(np * spp);
+        RC_CUDA_TRY(h, cudaMemsetAsync(h->dCounts, 0, countsBytes, h->stream), "reset queue counters");
+        RC_CUDA_TRY(h, launch_path_pass(p, int(np), h->order, h->counting, h->stream, h->numSMs),
+                    "launch path-tracing pass");
+    }
+    RC_CUDA_TRY(h, cudaEventRecord(h->ev1, h->stream), "record end event");
+    DevControl ctl;
+    RC_CUDA_TRY(h, cudaMemcpyAsync(&ctl, h->dCtl, sizeof(ctl), cudaMemcpyDeviceToHost, h->stream),
+                "read control block");
+    RC_CUDA_TRY(h, cudaStreamSynchronize(h->stream), "path tracing");
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+    h->stats.last_ms = double(ms);
+    h->stats.rays_traced = ctl.stats[0];
+    h->stats.node_visits = ctl.stats[1];
+    h->stats.tri_tests = ctl.stats[2];
+    h->frameIndex++;
+    if (ctl.error & 1)
+        return fail(h, RC_DEVICE_ERROR, "path tracing: traversal stack overflow");
+    return RC_OK;
+}
+
+}  // namespace rcx
+
+extern "C" {
+
+rc_status rc_resolve(rc_tracer* h, float* out_rgba)
+{
+    if (!h)
+        return RC_INVALID_ARG;
+    if (!h->dFilm || !out_rgba)
+        return fail(h, RC_NOT_READY, "resolve: no film or null output");
+    cudaSetDevice(h->device);
+    rc_status s = grow(h, &h->dTone, &h->capTone, tone_partials_bytes(h->filmPixels), "allocate tone scratch");
+    if (s != RC_OK)
+        return s;
+    if ((s = grow(h, &h->dImage, &h->capImage, size_t(h->filmPixels) * sizeof(float4), "allocate image")) != RC_OK)
+        return s;
+    const rc_tonemapper& t = h->tonemapper;
+    RC_CUDA_TRY(h,
+                launch_tonemap(h->dFilm, h->filmPixels, t.type, t.apply_gamma, t.should_clamp, t.gamma, t.key,
+                               h->dTone, static_cast<float4*>(h->dImage), h->stream, h->numSMs),
+                "launch tone mapping");
+    RC_CUDA_TRY(h,
+                cudaMemcpyAsync(out_rgba, h->dImage, size_t(h->filmPixels) * sizeof(float4), cudaMemcpyDeviceToHost,
+                                h->stream),
+                "download image");
+    RC_CUDA_TRY(h, cudaStreamSynchronize(h->stream), "resolve");
+    return RC_OK;
+}
+
+rc_status rc_tonemap_film(rc_tracer* h, const float* film_rgbw, uint64_t pixels, float* out_rgba)
+{
+    if (!h)
+        return RC_INVALID_ARG;
+    if (!film_rgbw || !out_rgba || pixels == 0 || pixels > (uint64_t(1) << 31))
+        return fail(h, RC_INVALID_ARG, "tonemap_film: null buffer or bad pixel count");
+    cudaSetDevice(h->device);
+    size_t bytes = size_t(pixels) * sizeof(float4);
+    rc_status s = grow(h, &h->dTone, &h->capTone, tone_partials_bytes(pixels), "allocate tone scratch");
+    if (s != RC_OK)
+        return s;
+    if ((s = grow(h, &h->dImage, &h->capImage, 2 * bytes, "allocate image")) != RC_OK)
+        return s;
+    float4* dIn = static_cast<float4*>(h->dImage);
+    float4* dOut = dIn + pixels;
+    const rc_tonemapper& t = h->tonemapper;
+    RC_CUDA_TRY(h, cudaMemcpyAsync(dIn, film_rgbw, bytes, cudaMemcpyHostToDevice, h->stream), "upload film");
+    RC_CUDA_TRY(h,
+                launch_tonemap(dIn, pixels, t.type, t.apply_gamma, t.should_clamp, t.gamma, t.key, h->dTone, dOut,
+                               h->stream, h->numSMs),
+                "launch tone mapping");
+    RC_CUDA_TRY(h, cudaMemcpyAsync(out_rgba, dOut, bytes, cudaMemcpyDeviceToHost, h->stream), "download image");
+    RC_CUDA_TRY(h, cudaStreamSynchronize(h->stream), "tonemap_film");
+    return RC_OK;
+}
+
+rc_status rc_read_linear(rc_tracer* h, float* out_rgba)
+{
+    if (!h)
+        return RC_INVALID_ARG;
+    if (!h->dFilm || !out_rgba)
+        return fail(h, RC_NOT_READY, "read_linear: no film or null output");
+    cudaSetDevice(h->device);
+    rc_status s = grow(h, &h->dImage, &h->capImage, size_t(h->filmPixels) * sizeof(float4), "allocate image");
+    if (s != RC_OK)
+        return s;
+    RC_CUDA_TRY(h, launch_linear(h->dFilm, h->filmPixels, static_cast<float4*>(h->dImage), h->stream),
+                "launch linear resolve");
+    RC_CUDA_TRY(h,
+                cudaMemcpyAsync(out_rgba, h->dImage, size_t(h->filmPixels) * sizeof(float4), cudaMemcpyDeviceToHost,
+                                h->stream),
+                "download linear image");
+    RC_CUDA_TRY(h, cudaStreamSynchronize(h->stream), "read_linear");
+    return RC_OK;
+}
+
+rc_status rc_read_film(rc_tracer* h, float* out_rgbw)
+{
+    if (!h)
+        return RC_INVALID_ARG;
+    if (!h->dFilm || !out_rgbw)
+        return fail(h, RC_NOT_READY, "read_film: no film or null output");
+    cudaSetDevice(h->device);
+    RC_CUDA_TRY(h,
+                cudaMemcpyAsync(out_rgbw, h->dFilm, size_t(h->filmPixels) * sizeof(float4), cudaMemcpyDeviceToHost,
+                                h->stream),
+                "download film");
+    RC_CUDA_TRY(h, cudaStreamSynchronize(h->stream), "read_film");
+    return RC_OK;
+}
+
+}  // extern "C"

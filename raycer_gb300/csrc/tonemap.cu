@@ -1,0 +1,212 @@
+// Film resolve + Reinhard tone mapping (Film::generateToneMappedImage,
+// Film.cpp:61-69; ReinhardToneMapper::apply, ReinhardToneMapper.cpp:18-86).
+//
+//   linear = film.rgb / film.w                      (float, like Colorf)
+//   L      = 0.2126 r + 0.7152 g + 0.0722 b         (double)
+//   Lavg   = exp(mean(log(0.01 + L))),  Lmax = max(1, max L)
+//   s      = key / Lavg
+//   Lm     = s L (1 + s L / Lmax^2) / (1 + s L)
+//   out    = clamp(linear * Lm / L), then gamma via MathUtils::fastPow
+//            (MathUtils.cpp:56-68: a linear map of the double's high word).
+// All in double with explicitly rounded operations (no contraction). The two
+// global reductions are a per-block pass plus one fixed-order combine, so the
+// result does not depend on scheduling.
+
+#include <cfloat>
+
+#include "pathtrace.h"
+
+namespace rcx
+{
+namespace
+{
+
+constexpr int kToneBlock = 256;
+
+struct ToneParams
+{
+    double scale;      // key / Lavg
+    double maxL2Inv;   // 1 / Lmax^2
+    double sumLog;
+    double maxL;
+};
+
+__device__ __forceinline__ double luminance(double r, double g, double b)
+{
+    // Color::getLuminance (Color.cpp:130-133)
+    return __dadd_rn(__dadd_rn(__dmul_rn(0.2126, r), __dmul_rn(0.7152, g)), __dmul_rn(0.0722, b));
+}
+
+__device__ __forceinline__ float4 linear_of(float4 f)
+{
+    return make_float4(__fdiv_rn(f.x, f.w), __fdiv_rn(f.y, f.w), __fdiv_rn(f.z, f.w), 1.0f);
+}
+
+// std::max(0.0, std::min(x, 1.0)) (Color::clamped, Color.cpp:166-176).
+__device__ __forceinline__ double clamp01(double x)
+{
+    double m = (1.0 < x) ? 1.0 : x;
+    return (0.0 < m) ? m : 0.0;
+}
+
+// MathUtils::fastPow (MathUtils.cpp:56-68).
+__device__ __forceinline__ double fast_pow(double a, double b)
+{
+    long long bits = __double_as_longlong(a);
+    int hi = int(bits >> 32);
+    double r = __dadd_rn(__dmul_rn(b, double(hi - 1072632447)), 1072632447.0);
+    int nh = __double2int_rz(r);
+    return __longlong_as_double((long long)((unsigned long long)(unsigned)nh << 32));
+}
+
+__global__ void __launch_bounds__(kToneBlock) k_tone_reduce(const float4* __restrict__ film, uint64_t pixels,
+                                                           double2* __restrict__ partial)
+{
+    __shared__ double sSum[kToneBlock];
+    __shared__ double sMax[kToneBlock];
+    double sum = 0.0, mx = 0.0;
+    for (uint64_t i = uint64_t(blockIdx.x) * kToneBlock + threadIdx.x; i < pixels;
+         i += uint64_t(gridDim.x) * kToneBlock)
+    {
+        float4 c = linear_of(film[i]);
+        double L = luminance(double(c.x), double(c.y), double(c.z));
+        sum = __dadd_rn(sum, log(__dadd_rn(0.01, L)));
+        if (L > mx)
+            mx = L;
+    }
+    sSum[threadIdx.x] = sum;
+    sMax[threadIdx.x] = mx;
+    __syncthreads();
+    for (int s = kToneBlock / 2; s > 0; s >>= 1)
+    {
+        if (int(threadIdx.x) < s)
+        {
+            sSum[threadIdx.x] = __dadd_rn(sSum[threadIdx.x], sSum[threadIdx.x + s]);
+            if (sMax[threadIdx.x + s] > sMax[threadIdx.x])
+                sMax[threadIdx.x] = sMax[threadIdx.x + s];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        partial[blockIdx.x] = make_double2(sSum[0], sMax[0]);
+}
+
+__global__ void __launch_bounds__(kToneBlock) k_tone_combine(const double2* __restrict__ partial, int blocks,
+                                                            uint64_t pixels, double key, ToneParams* out)
+{
+    __shared__ double sSum[kToneBlock];
+    __shared__ double sMax[kToneBlock];
+    double sum = 0.0, mx = 0.0;
+    for (int i = threadIdx.x; i < blocks; i += kToneBlock)
+    {
+        sum = __dadd_rn(sum, partial[i].x);
+        if (partial[i].y > mx)
+            mx = partial[i].y;
+    }
+    sSum[threadIdx.x] = sum;
+    sMax[threadIdx.x] = mx;
+    __syncthreads();
+    for (int s = kToneBlock / 2; s > 0; s >>= 1)
+    {
+        if (int(threadIdx.x) < s)
+        {
+            sSum[threadIdx.x] = __dadd_rn(sSum[threadIdx.x], sSum[threadIdx.x + s]);
+            if (sMax[threadIdx.x + s] > sMax[threadIdx.x])
+                sMax[threadIdx.x] = sMax[threadIdx.x + s];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+    {
+        double maxL = 1.0;  // ReinhardToneMapper.cpp:26 starts from 1
+        if (sMax[0] > maxL)
+            maxL = sMax[0];
+        double avg = exp(__ddiv_rn(sSum[0], double(pixels)));
+        ToneParams p;
+        p.scale = __ddiv_rn(key, avg);
+        p.maxL2Inv = __ddiv_rn(1.0, __dmul_rn(maxL, maxL));
+        p.sumLog = sSum[0];
+        p.maxL = maxL;
+        *out = p;
+    }
+}
+
+__global__ void __launch_bounds__(kToneBlock) k_tone_apply(const float4* __restrict__ film, uint64_t pixels,
+                                                          const ToneParams* __restrict__ tp, int applyGamma,
+                                                          int shouldClamp, double invGamma, float4* __restrict__ out)
+{
+    uint64_t i = uint64_t(blockIdx.x) * kToneBlock + threadIdx.x;
+    if (i >= pixels)
+        return;
+    ToneParams p = *tp;
+    float4 c = linear_of(film[i]);
+    double r = double(c.x), g = double(c.y), b = double(c.z);
+    double L = luminance(r, g, b);
+    double sL = __dmul_rn(p.scale, L);
+    double mapped = __ddiv_rn(__dmul_rn(sL, __dadd_rn(1.0, __dmul_rn(sL, p.maxL2Inv))), __dadd_rn(1.0, sL));
+    double cs = __ddiv_rn(mapped, L);
+    r = __dmul_rn(r, cs);
+    g = __dmul_rn(g, cs);
+    b = __dmul_rn(b, cs);
+    if (shouldClamp)
+    {
+        r = clamp01(r);
+        g = clamp01(g);
+        b = clamp01(b);
+    }
+    if (applyGamma)
+    {
+        r = fast_pow(r, invGamma);
+        g = fast_pow(g, invGamma);
+        b = fast_pow(b, invGamma);
+    }
+    out[i] = make_float4(float(r), float(g), float(b), 1.0f);
+}
+
+__global__ void k_linear(const float4* __restrict__ film, uint64_t pixels, float4* __restrict__ out)
+{
+    uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < pixels)
+        out[i] = linear_of(film[i]);
+}
+
+int reduce_blocks(uint64_t pixels, int numSMs)
+{
+    uint64_t need = (pixels + kToneBlock - 1) / kToneBlock;
+    uint64_t cap = uint64_t(numSMs) * 8;
+    return int(need < cap ? (need > 0 ? need : 1) : cap);
+}
+
+}  // namespace
+
+size_t tone_partials_bytes(uint64_t pixels)
+{
+    (void)pixels;
+    return sizeof(double2) * 4096 + sizeof(ToneParams);
+}
+
+cudaError_t launch_tonemap(const float4* film, uint64_t pixels, int type, int applyGamma, int shouldClamp,
+                           double gamma, double key, void* partials, float4* out, cudaStream_t stream, int numSMs)
+{
+    if (type == RC_TONEMAP_PASSTHROUGH)
+        return launch_linear(film, pixels, out, stream);
+    int blocks = reduce_blocks(pixels, numSMs);
+    if (blocks > 4096)
+        blocks = 4096;
+    double2* part = static_cast<double2*>(partials);
+    ToneParams* tp = reinterpret_cast<ToneParams*>(part + 4096);
+    k_tone_reduce<<<blocks, kToneBlock, 0, stream>>>(film, pixels, part);
+    k_tone_combine<<<1, kToneBlock, 0, stream>>>(part, blocks, pixels, key, tp);
+    double invGamma = 1.0 / gamma;  // ReinhardToneMapper.cpp:61
+    k_tone_apply<<<unsigned((pixels + kToneBlock - 1) / kToneBlock), kToneBlock, 0, stream>>>(
+        film, pixels, tp, applyGamma, shouldClamp, invGamma, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_linear(const float4* film, uint64_t pixels, float4* out, cudaStream_t stream)
+{
+    k_linear<<<unsigned((pixels + 255) / 256), 256, 0, stream>>>(film, pixels, out);
+    return cudaGetLastError();
+}
+
+}  // namespace rcx

@@ -1,0 +1,267 @@
+// Ray-casting kernels: generic closest/any-hit queries and the RAY tracer's
+// frame (one primary ray per pixel + one shadow ray per hit).
+//
+// Work distribution: persistent blocks (occupancy x SM count) whose warps
+// take 32 rays at a time from a global atomic work counter; the shadow
+// stage is fed by a queue that the primary stage fills with one atomicAdd
+// per warp after a ballot over the lanes that hit (warp-aggregated
+// compaction), so shadow warps carry no missed pixels.
+
+#include <cfloat>
+
+#include "kernels.h"
+#include "traverse.cuh"
+
+namespace rcx
+{
+namespace
+{
+
+constexpr int kBlock = 128;
+
+__device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
+
+__device__ __forceinline__ unsigned warp_fetch(unsigned* head, unsigned amount)
+{
+    unsigned base = 0;
+    if (lane_id() == 0)
+        base = atomicAdd(head, amount);
+    return __shfl_sync(0xffffffffu, base, 0);
+}
+
+__device__ __forceinline__ void flush_counts(DevControl* ctl, unsigned long long rays, const TravCount& c, int err)
+{
+    unsigned long long n = c.nodes, t = c.tris;
+    for (int o = 16; o > 0; o >>= 1)
+    {
+        rays += __shfl_down_sync(0xffffffffu, rays, o);
+        n += __shfl_down_sync(0xffffffffu, n, o);
+        t += __shfl_down_sync(0xffffffffu, t, o);
+    }
+    if (lane_id() == 0)
+    {
+        atomicAdd(&ctl->stats[0], rays);
+        if (n)
+            atomicAdd(&ctl->stats[1], n);
+        if (t)
+            atomicAdd(&ctl->stats[2], t);
+    }
+    if (err)
+        atomicOr(&ctl->error, 1);
+}
+
+__device__ __forceinline__ int caller_index(const DevScene& sc, int slot)
+{
+    return __float_as_int(__ldg(&sc.tris[slot].c.z));
+}
+
+template <bool ANY, int ORDER, bool COUNT>
+__global__ void __launch_bounds__(kBlock) k_cast(DevScene sc, const rc_ray* __restrict__ rays, int n,
+                                                 rc_hit* __restrict__ hits, DevControl* ctl)
+{
+    TravCount cnt{ 0, 0 };
+    int err = 0;
+    unsigned long long done = 0;
+    while (true)
+    {
+        unsigned base = warp_fetch(&ctl->head[0], 32u);
+        if (base >= unsigned(n))
+            break;
+        int i = int(base + lane_id());
+        if (i < n)
+        {
+            const float4* rp = reinterpret_cast<const float4*>(rays + i);
+            float4 r0 = __ldg(rp);
+            float4 r1 = __ldg(rp + 1);
+            RayF ray = make_ray(v3(r0.x, r0.y, r0.z), v3(r1.x, r1.y, r1.z), r0.w, r1.w);
+            HitF h{ -1, FLT_MAX, 0.0f, 0.0f };
+            bool found = traverse<ANY, ORDER, COUNT>(sc, ray, h, cnt, err);
+            int4 out;
+            out.x = found ? caller_index(sc, h.slot) : -1;
+            out.y = __float_as_int(found ? h.t : -1.0f);
+            out.z = __float_as_int(found ? h.u : 0.0f);
+            out.w = __float_as_int(found ? h.v : 0.0f);
+            reinterpret_cast<int4*>(hits)[i] = out;
+            done++;
+        }
+    }
+    flush_counts(ctl, done, cnt, err);
+}
+
+__device__ __forceinline__ RayF primary_ray(const DevCamera& cam, const rc_ray* __restrict__ rays, uint64_t pixel,
+                                            int64_t local, int64_t width)
+{
+    if (rays)
+    {
+        const float4* rp = reinterpret_cast<const float4*>(rays + local);
+        float4 r0 = __ldg(rp);
+        float4 r1 = __ldg(rp + 1);
+        return make_ray(v3(r0.x, r0.y, r0.z), v3(r1.x, r1.y, r1.z), r0.w, r1.w);
+    }
+    float px = float(pixel % uint64_t(width));
+    float py = float(pixel / uint64_t(width));
+    V3 d = camera_dir(cam, px, py);
+    return make_ray(v3(cam.pos[0], cam.pos[1], cam.pos[2]), d, 0.0f, FLT_MAX);
+}
+
+// Stage 1 of the RAY frame: closest hit of every pixel's primary ray.
+template <int ORDER, bool COUNT>
+__global__ void __launch_bounds__(kBlock) k_raycast_primary(DevScene sc, DevCamera cam, const rc_ray* __restrict__ rays,
+                                                            uint64_t pixelStart, int64_t count, int64_t width,
+                                                            int castShadow, rc_cast_pixel* __restrict__ out,
+                                                            int* __restrict__ queue, DevControl* ctl)
+{
+    TravCount cnt{ 0, 0 };
+    int err = 0;
+    unsigned long long done = 0;
+    while (true)
+    {
+        unsigned base = warp_fetch(&ctl->head[0], 32u);
+        if (int64_t(base) >= count)
+            break;
+        int64_t i = int64_t(base) + lane_id();
+        bool hitAny = false;
+        if (i < count)
+        {
+            RayF ray = primary_ray(cam, rays, pixelStart + uint64_t(i), i, width);
+            HitF h{ -1, FLT_MAX, 0.0f, 0.0f };
+            bool found = traverse<false, ORDER, COUNT>(sc, ray, h, cnt, err);
+            int4 o;
+            o.x = found ? caller_index(sc, h.slot) : -1;
+            o.y = __float_as_int(found ? h.t : -1.0f);
+            o.z = -1;
+            o.w = found ? 1 : 0;
+            reinterpret_cast<int4*>(out)[i] = o;
+            hitAny = found && castShadow;
+            done++;
+        }
+        // Warp-aggregated compaction of the hit pixels into the shadow queue.
+        unsigned mask = __ballot_sync(0xffffffffu, hitAny);
+        if (mask)
+        {
+            unsigned qbase = 0;
+            if (lane_id() == 0)
+                qbase = atomicAdd(&ctl->head[1], unsigned(__popc(mask)));
+            qbase = __shfl_sync(0xffffffffu, qbase, 0);
+            if (hitAny)
+                queue[qbase + __popc(mask & ((1u << lane_id()) - 1u))] = int(i);
+        }
+    }
+    flush_counts(ctl, done, cnt, err);
+}
+
+// Stage 2: one any-hit shadow ray toward the light per queued pixel
+// (Raytracer::calculateShadowAmount, Raytracer.cpp:497-522 /
+// lighting.cl:28-48): origin = hit position + dirToLight * rayStartOffset.
+template <bool COUNT>
+__global__ void __launch_bounds__(kBlock) k_raycast_shadow(DevScene sc, DevCamera cam, const rc_ray* __restrict__ rays,
+                                                           uint64_t pixelStart, int64_t width, float3 L,
+                                                           float rayStartOffset, rc_cast_pixel* __restrict__ out,
+                                                           const int* __restrict__ queue, DevControl* ctl)
+{
+    TravCount cnt{ 0, 0 };
+    int err = 0;
+    unsigned long long done = 0;
+    const unsigned total = *reinterpret_cast<volatile unsigned*>(&ctl->head[1]);
+    while (true)
+    {
+        unsigned base = warp_fetch(&ctl->head[2], 32u);
+        if (base >= total)
+            break;
+        unsigned q = base + lane_id();
+        if (q < total)
+        {
+            int i = queue[q];
+            RayF pr = primary_ray(cam, rays, pixelStart + uint64_t(i), i, width);
+            float t = out[i].t;
+            // ip = origin + t * direction (intersections.cl:85)
+            V3 ip = vfma(pr.d, t, pr.o);
+            V3 dl = v3(L.x, L.y, L.z);
+            RayF sr = make_ray(vfma(dl, rayStartOffset, ip), dl, 0.0f, FLT_MAX);
+            HitF h{ -1, FLT_MAX, 0.0f, 0.0f };
+            bool occ = traverse<true, ORDER_REF, COUNT>(sc, sr, h, cnt, err);
+            out[i].occluder = occ ? caller_index(sc, h.slot) : -1;
+            out[i].flags = 1 | 2 | (occ ? 4 : 0);
+            done++;
+        }
+    }
+    flush_counts(ctl, done, cnt, err);
+}
+
+template <typename K>
+int persistent_blocks(K kernel, int numSMs)
+{
+    int perSM = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kernel, kBlock, 0) != cudaSuccess || perSM < 1)
+        perSM = 1;
+    return perSM * numSMs;
+}
+
+template <bool ANY, int ORDER, bool COUNT>
+cudaError_t cast_t(const LaunchInfo& li, const DevScene& sc, const rc_ray* rays, int64_t n, rc_hit* hits,
+                   DevControl* ctl)
+{
+    auto k = k_cast<ANY, ORDER, COUNT>;
+    static int grid = 0;
+    if (grid == 0)
+        grid = persistent_blocks(k, li.numSMs);
+    k<<<grid, kBlock, 0, li.stream>>>(sc, rays, int(n), hits, ctl);
+    return cudaGetLastError();
+}
+
+template <int ORDER, bool COUNT>
+cudaError_t raycast_t(const LaunchInfo& li, const DevScene& sc, const DevCamera& cam, const rc_ray* rays,
+                      uint64_t pixelStart, int64_t count, int64_t width, int castShadow, float3 L, float off,
+                      rc_cast_pixel* out, int* queue, DevControl* ctl)
+{
+    auto kp = k_raycast_primary<ORDER, COUNT>;
+    auto ks = k_raycast_shadow<COUNT>;
+    static int gp = 0, gs = 0;
+    if (gp == 0)
+        gp = persistent_blocks(kp, li.numSMs);
+    if (gs == 0)
+        gs = persistent_blocks(ks, li.numSMs);
+    kp<<<gp, kBlock, 0, li.stream>>>(sc, cam, rays, pixelStart, count, width, castShadow, out, queue, ctl);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess || !castShadow)
+        return e;
+    ks<<<gs, kBlock, 0, li.stream>>>(sc, cam, rays, pixelStart, width, L, off, out, queue, ctl);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_cast(const LaunchInfo& li, const DevScene& sc, const rc_ray* rays, int64_t n, int anyHit,
+                        int order, rc_hit* hits, DevControl* ctl)
+{
+    if (n <= 0)
+        return cudaSuccess;
+    if (anyHit)
+        return li.counting ? cast_t<true, ORDER_REF, true>(li, sc, rays, n, hits, ctl)
+                           : cast_t<true, ORDER_REF, false>(li, sc, rays, n, hits, ctl);
+    if (order == ORDER_NEAREST)
+        return li.counting ? cast_t<false, ORDER_NEAREST, true>(li, sc, rays, n, hits, ctl)
+                           : cast_t<false, ORDER_NEAREST, false>(li, sc, rays, n, hits, ctl);
+    return li.counting ? cast_t<false, ORDER_REF, true>(li, sc, rays, n, hits, ctl)
+                       : cast_t<false, ORDER_REF, false>(li, sc, rays, n, hits, ctl);
+}
+
+cudaError_t launch_raycast(const LaunchInfo& li, const DevScene& sc, const DevCamera& cam, const rc_ray* rays,
+                           uint64_t pixelStart, int64_t count, int64_t width, int order, int castShadow,
+                           float3 dirToLight, float rayStartOffset, rc_cast_pixel* out, int* shadowQueue,
+                           DevControl* ctl)
+{
+    if (count <= 0)
+        return cudaSuccess;
+    if (order == ORDER_NEAREST)
+        return li.counting ? raycast_t<ORDER_NEAREST, true>(li, sc, cam, rays, pixelStart, count, width, castShadow,
+                                                            dirToLight, rayStartOffset, out, shadowQueue, ctl)
+                           : raycast_t<ORDER_NEAREST, false>(li, sc, cam, rays, pixelStart, count, width, castShadow,
+                                                             dirToLight, rayStartOffset, out, shadowQueue, ctl);
+    return li.counting ? raycast_t<ORDER_REF, true>(li, sc, cam, rays, pixelStart, count, width, castShadow,
+                                                    dirToLight, rayStartOffset, out, shadowQueue, ctl)
+                       : raycast_t<ORDER_REF, false>(li, sc, cam, rays, pixelStart, count, width, castShadow,
+                                                     dirToLight, rayStartOffset, out, shadowQueue, ctl);
+}
+
+}  // namespace rcx

@@ -1,0 +1,180 @@
+// BVH traversal of the flat SAH BVH (device side).
+//
+// The reference traverses with an explicit stack: pop a node; a leaf tests
+// its triangles in order; an inner node tests the right child's box and
+// pushes it, then the left child's box and pushes it, so the left subtree is
+// finished first (FlatBVH::intersect FlatBVH.cpp:22-75, intersectBVH
+// intersections.cl:98-148). The root's own box is never tested.
+//
+// Here the node is the 64-B two-child record of device_types.h, so one fetch
+// tests both children:
+//   ORDER_REF      descend left, push right (the reference's visit order;
+//                  the same boxes are tested, the same triangles in the same
+//                  order, the same closest hit — ties to the later triangle,
+//                  Triangle.cpp:93 `t > distance` rejects only farther hits).
+//   ORDER_NEAREST  descend into the nearer child, push the farther one with
+//                  its entry distance, and skip boxes whose entry distance is
+//                  beyond the current closest hit. The accepted hit is the
+//                  same: minimum t, ties resolved to the larger BVH-order
+//                  slot, which is what the reference's order yields.
+// Any-hit (shadow rays: isShadowRay + fastOcclusion) always uses the
+// reference order and stops at the first triangle found; triangles whose
+// material is nonShadowing are skipped (Triangle.cpp:55).
+#pragma once
+
+#include "rc_math.cuh"
+
+namespace rcx
+{
+
+enum TraversalOrder
+{
+    ORDER_REF = 0,
+    ORDER_NEAREST = 1
+};
+
+struct HitF
+{
+    int slot;  // BVH-order triangle slot, -1 = none
+    float t;
+    float u;
+    float v;
+};
+
+struct TravCount
+{
+    uint32_t nodes;  // inner nodes fetched (child-pair box tests)
+    uint32_t tris;   // triangle tests
+};
+
+__device__ __forceinline__ void load_node(const DevNode* __restrict__ nodes, int i, float4& a, float4& b, float4& c,
+                                          int4& l)
+{
+    const float4* p = reinterpret_cast<const float4*>(nodes + i);
+    a = __ldg(p + 0);
+    b = __ldg(p + 1);
+    c = __ldg(p + 2);
+    l = __ldg(reinterpret_cast<const int4*>(p + 3));
+}
+
+// Returns true if any triangle was accepted. `hit` must be initialised by
+// the caller (slot -1, t = FLT_MAX for a fresh query). `err` is set to 1 on
+// a stack overflow (the ray is then abandoned; the host reports it).
+template <bool ANY_HIT, int ORDER, bool COUNT>
+__device__ __forceinline__ bool traverse(const DevScene& sc, const RayF& ray, HitF& hit, TravCount& cnt, int& err)
+{
+    int stack[kMaxStack];
+    float sdist[ORDER == ORDER_NEAREST && !ANY_HIT ? kMaxStack : 1];
+    int sp = 0;
+    int cur = sc.rootLink;
+    bool found = false;
+
+    while (true)
+    {
+        if (cur >= 0)
+        {
+            float4 a, b, c;
+            int4 l;
+            load_node(sc.nodes, cur, a, b, c, l);
+            if (COUNT)
+                cnt.nodes++;
+            float e0, e1;
+            bool h0 = slab(ray, a.x, a.y, a.z, a.w, c.x, c.y, e0);
+            bool h1 = slab(ray, b.x, b.y, b.z, b.w, c.z, c.w, e1);
+            if (ORDER == ORDER_NEAREST && !ANY_HIT)
+            {
+                h0 = h0 && !(e0 > hit.t);
+                h1 = h1 && !(e1 > hit.t);
+            }
+            if (h0 && h1)
+            {
+                int nearC = l.x, farC = l.y;
+                float farD = e1;
+                if (ORDER == ORDER_NEAREST && !ANY_HIT && e1 < e0)
+                {
+                    nearC = l.y;
+                    farC = l.x;
+                    farD = e0;
+                }
+                if (sp >= kMaxStack)
+                {
+                    err = 1;
+                    return found;
+                }
+                stack[sp] = farC;
+                if (ORDER == ORDER_NEAREST && !ANY_HIT)
+                    sdist[sp] = farD;
+                sp++;
+                cur = nearC;
+                continue;
+            }
+            if (h0)
+            {
+                cur = l.x;
+                continue;
+            }
+            if (h1)
+            {
+                cur = l.y;
+                continue;
+            }
+        }
+        else
+        {
+            int leaf = ~cur;
+            int start = leaf >> kLeafCountBits;
+            int count = leaf & ((1 << kLeafCountBits) - 1);
+            for (int i = 0; i < count; ++i)
+            {
+                int slot = start + i;
+                const float4* tp = reinterpret_cast<const float4*>(sc.tris + slot);
+                float4 ta = __ldg(tp + 0);
+                float4 tb = __ldg(tp + 1);
+                float4 tc = __ldg(tp + 2);
+                if (ANY_HIT && (__float_as_uint(tc.y) & kMetaNonShadowing))
+                    continue;
+                if (COUNT)
+                    cnt.tris++;
+                float t, u, v;
+                if (tri_hit(ray, v3(ta.x, ta.y, ta.z), v3(ta.w, tb.x, tb.y), v3(tb.z, tb.w, tc.x), t, u, v))
+                {
+                    if (ANY_HIT)
+                    {
+                        hit.slot = slot;
+                        hit.t = t;
+                        hit.u = u;
+                        hit.v = v;
+                        return true;
+                    }
+                    bool take;
+                    if (ORDER == ORDER_REF)
+                        take = !(t > hit.t);
+                    else
+                        take = t < hit.t || (t == hit.t && slot > hit.slot);
+                    if (take)
+                    {
+                        hit.slot = slot;
+                        hit.t = t;
+                        hit.u = u;
+                        hit.v = v;
+                        found = true;
+                    }
+                }
+            }
+        }
+
+        // pop
+        while (true)
+        {
+            if (sp == 0)
+                return found;
+            sp--;
+            cur = stack[sp];
+            if (ORDER == ORDER_NEAREST && !ANY_HIT && sdist[sp] > hit.t)
+                continue;
+            break;
+        }
+    }
+}
+
+}  // namespace rcx

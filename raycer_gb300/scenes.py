@@ -1,0 +1,282 @@
+"""Seeded synthetic scenes for the benchmark workloads.
+
+No public dataset is involved: every scene is generated from a seed. Vertex
+coordinates are computed in float64 and rounded to float32 (the workloads are
+specified in float32), so the reference's float64 code and the device see the
+same triangles.
+
+* ``room_scene`` — 320x240 path-tracing workload: an axis-aligned room
+  [-1,1]^3 (5 walls, 10 triangles, inward-facing), an emissive 0.5x0.5 ceiling
+  quad 1e-3 below the ceiling (2 triangles, radiance 15), and 2,000 random
+  clutter triangles (centres U[-0.8,0.8]^3, vertices at uniform unit
+  directions scaled by U(0.05,0.2), diffuse albedo U(0.2,0.8)^3). Camera at
+  (0,0,3.5) looking down -z, 45 degree horizontal field of view.
+* ``heightfield_scene`` — 1920x1080 ray-casting workload: a 1024x512-vertex
+  grid over x in [-10,10], z in [-5,5] (2*1023*511 = 1,045,506 triangles),
+  height 1.5 * fBm(6 octaves, lacunarity 2, gain 0.5) of the reference's value
+  noise with seed 2 (ValueNoise::getNoise / getFbmNoise,
+  src/Utils/ValueNoise.cpp:26-97), one directional light toward
+  normalize(0.3,1,0.2), camera at (0,4,12) aimed at the origin.
+
+Random draws for the room come from Python's ``random.Random`` (Mersenne
+Twister, documented as reproducible for a given seed). The value noise
+restates the reference: each lattice corner seeds a std::mt19937 with
+``uint32(seed*16381 + x*17389 + y*18313 + z*19423)`` and takes its first
+``uniform_real_distribution<double>(0,1)`` draw, i.e. libstdc++'s
+generate_canonical<double, 53> over two 32-bit outputs; the needed outputs of
+a freshly seeded generator are computed directly (vectorised), which gives the
+same numbers as seeding a generator per corner.
+"""
+
+from __future__ import annotations
+
+import math
+import random
+from dataclasses import dataclass, field
+
+import numpy as np
+
+# ---------------------------------------------------------------------------
+# Scene description (plain arrays; what rc_upload_scene consumes).
+
+
+@dataclass
+class Material:
+    diffuse: tuple = (0.0, 0.0, 0.0)
+    emittance: tuple = (0.0, 0.0, 0.0)
+    is_emissive: bool = False
+    non_shadowing: bool = False
+    invert_normal: bool = False
+
+
+@dataclass
+class CameraDesc:
+    position: tuple = (0.0, 0.0, 0.0)
+    pitch: float = 0.0
+    yaw: float = 0.0
+    roll: float = 0.0
+    fov: float = 75.0
+
+
+@dataclass
+class SceneDesc:
+    name: str
+    vertices: np.ndarray          # (n, 9) float64, float32-exact values
+    material_index: np.ndarray    # (n,) uint32
+    materials: list               # [Material]
+    camera: CameraDesc
+    width: int
+    height: int
+    light_direction: tuple | None = None   # DirectionalLight.direction (travel direction)
+    max_leaf_size: int = 4
+    settings: dict = field(default_factory=dict)
+
+    @property
+    def triangle_count(self) -> int:
+        return int(self.vertices.shape[0])
+
+
+def _f32(a: np.ndarray) -> np.ndarray:
+    return np.asarray(a, dtype=np.float64).astype(np.float32).astype(np.float64)
+
+
+# ---------------------------------------------------------------------------
+# Room (path tracing).
+
+
+def _quad(p0, u, v):
+    p0, u, v = map(np.asarray, (p0, u, v))
+    a, b, c, d = p0, p0 + u, p0 + u + v, p0 + v
+    return [np.concatenate([a, b, c]), np.concatenate([a, c, d])]
+
+
+def room_scene(seed: int = 1, clutter: int = 2000, width: int = 320, height: int = 240) -> SceneDesc:
+    rng = random.Random(seed)
+    tris = []
+    mats = [
+        Material(diffuse=(0.75, 0.75, 0.75)),
+        Material(diffuse=(0.75, 0.25, 0.25)),
+        Material(diffuse=(0.25, 0.75, 0.25)),
+        Material(diffuse=(0.0, 0.0, 0.0), emittance=(15.0, 15.0, 15.0), is_emissive=True),
+    ]
+    midx = []
+    # Walls: (p0, u, v) with u x v pointing into the room.
+    walls = [
+        ((-1, -1, -1), (0, 0, 2), (2, 0, 0), 0),   # floor, +y
+        ((-1, 1, -1), (2, 0, 0), (0, 0, 2), 0),    # ceiling, -y
+        ((-1, -1, -1), (2, 0, 0), (0, 2, 0), 0),   # back, +z
+        ((-1, -1, -1), (0, 2, 0), (0, 0, 2), 1),   # left, +x
+        ((1, -1, -1), (0, 0, 2), (0, 2, 0), 2),    # right, -x
+    ]
+    for p0, u, v, m in walls:
+        for t in _quad(np.array(p0, float), np.array(u, float), np.array(v, float)):
+            tris.append(t)
+            midx.append(m)
+    for t in _quad(np.array([-0.25, 1.0 - 1e-3, -0.25]), np.array([0.5, 0.0, 0.0]), np.array([0.0, 0.0, 0.5])):
+        tris.append(t)
+        midx.append(3)
+    for _ in range(clutter):
+        c = np.array([rng.uniform(-0.8, 0.8) for _ in range(3)])
+        verts = []
+        for _k in range(3):
+            z = rng.uniform(-1.0, 1.0)
+            phi = rng.uniform(0.0, 2.0 * math.pi)
+            r = math.sqrt(max(0.0, 1.0 - z * z))
+            d = np.array([r * math.cos(phi), r * math.sin(phi), z])
+            s = rng.uniform(0.05, 0.2)
+            verts.append(c + d * s)
+        albedo = tuple(rng.uniform(0.2, 0.8) for _ in range(3))
+        mats.append(Material(diffuse=albedo))
+        tris.append(np.concatenate(verts))
+        midx.append(len(mats) - 1)
+    v = _f32(np.array(tris))
+    return SceneDesc(
+        name=f"room(seed={seed}, clutter={clutter})",
+        vertices=v,
+        material_index=np.array(midx, dtype=np.uint32),
+        materials=mats,
+        camera=CameraDesc(position=(0.0, 0.0, 3.5), pitch=0.0, yaw=0.0, roll=0.0, fov=45.0),
+        width=width,
+        height=height,
+        light_direction=None,
+        max_leaf_size=4,
+        settings=dict(tracer="path", max_path_length=4, multi_sample_count_sqrt=4, path_sample_count=1,
+                      sampler="cmj", filter="box", tonemap="reinhard", key=0.18, gamma=2.2),
+    )
+
+
+# ---------------------------------------------------------------------------
+# Value noise (src/Utils/ValueNoise.cpp restated, vectorised).
+
+_MT_MULT = np.uint64(1812433253)
+_MASK32 = np.uint64(0xFFFFFFFF)
+
+
+def _mt19937_first_two(seeds: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+    """First two outputs of std::mt19937(seed) for an array of uint32 seeds."""
+    s = seeds.astype(np.uint64)
+    need = {0, 1, 2, 397, 398}
+    state = {0: s}
+    prev = s
+    for i in range(1, 399):
+        prev = (_MT_MULT * (prev ^ (prev >> np.uint64(30))) + np.uint64(i)) & _MASK32
+        if i in need:
+            state[i] = prev
+    upper = np.uint64(0x80000000)
+    lower = np.uint64(0x7FFFFFFF)
+    mag = np.uint64(0x9908B0DF)
+    outs = []
+    for k in (0, 1):
+        y = (state[k] & upper) | (state[k + 1] & lower)
+        x = state[k + 397] ^ (y >> np.uint64(1)) ^ np.where((y & np.uint64(1)) != 0, mag, np.uint64(0))
+        x = x ^ (x >> np.uint64(11))
+        x = x ^ ((x << np.uint64(7)) & np.uint64(0x9D2C5680))
+        x = x ^ ((x << np.uint64(15)) & np.uint64(0xEFC60000))
+        x = x ^ (x >> np.uint64(18))
+        outs.append(x & _MASK32)
+    return outs[0], outs[1]
+
+
+def _canonical(seeds: np.ndarray) -> np.ndarray:
+    """uniform_real_distribution<double>(0, 1) first draw of mt19937(seed)."""
+    o0, o1 = _mt19937_first_two(seeds)
+    r = (o0.astype(np.float64) + o1.astype(np.float64) * 4294967296.0) / 18446744073709551616.0
+    return np.where(r >= 1.0, np.nextafter(1.0, 0.0), r)
+
+
+def _hash(seed: int, x: np.ndarray, y: np.ndarray, z: np.ndarray) -> np.ndarray:
+    # ValueNoise::getHashcode: uint32((seed*16381) + x*17389 + y*18313 + z*19423)
+    h = (np.int64(seed) * 16381) + x * 17389 + y * 18313 + z * 19423
+    return (h & 0xFFFFFFFF).astype(np.uint64)
+
+
+def value_noise(seed: int, x: np.ndarray, y: np.ndarray, z: np.ndarray) -> np.ndarray:
+    """ValueNoise(seed).getNoise(x, y, z) for arrays of points."""
+    x = np.asarray(x, np.float64)
+    y = np.asarray(y, np.float64)
+    z = np.asarray(z, np.float64)
+    ix = np.floor(x).astype(np.int64)
+    iy = np.floor(y).astype(np.int64)
+    iz = np.floor(z).astype(np.int64)
+    tx = x - ix
+    ty = y - iy
+    tz = z - iz
+    txi = 1.0 - tx
+    tyi = 1.0 - ty
+    tzi = 1.0 - tz
+    corners = {}
+    keys = []
+    for dx in (0, 1):
+        for dy in (0, 1):
+            for dz in (0, 1):
+                keys.append(_hash(seed, ix + dx, iy + dy, iz + dz))
+    allk = np.concatenate(keys)
+    uniq, inv = np.unique(allk, return_inverse=True)
+    vals = _canonical(uniq)[inv].reshape(8, -1)
+    i = 0
+    for dx in (0, 1):
+        for dy in (0, 1):
+            for dz in (0, 1):
+                corners[(dx, dy, dz)] = vals[i]
+                i += 1
+    c00 = corners[0, 0, 0] * txi + corners[1, 0, 0] * tx
+    c01 = corners[0, 0, 1] * txi + corners[1, 0, 1] * tx
+    c10 = corners[0, 1, 0] * txi + corners[1, 1, 0] * tx
+    c11 = corners[0, 1, 1] * txi + corners[1, 1, 1] * tx
+    c0 = c00 * tyi + c10 * ty
+    c1 = c01 * tyi + c11 * ty
+    c = c0 * tzi + c1 * tz
+    return np.maximum(0.0, np.minimum(c, 1.0))
+
+
+def fbm_noise(seed: int, octaves: int, lacunarity: float, persistence: float, x, y, z) -> np.ndarray:
+    """ValueNoise::getFbmNoise (ValueNoise.cpp:78-92)."""
+    x = np.asarray(x, np.float64)
+    y = np.asarray(y, np.float64)
+    z = np.asarray(z, np.float64)
+    result = np.zeros_like(x)
+    frequency = 1.0
+    amplitude = 1.0
+    for _ in range(octaves):
+        result = result + value_noise(seed, x * frequency, y * frequency, z * frequency) * amplitude
+        frequency *= lacunarity
+        amplitude *= persistence
+    return result
+
+
+# ---------------------------------------------------------------------------
+# Heightfield (ray casting).
+
+
+def heightfield_scene(seed: int = 2, nx: int = 1024, nz: int = 512, width: int = 1920, height: int = 1080,
+                      extent=(-10.0, 10.0, -5.0, 5.0), amplitude: float = 1.5) -> SceneDesc:
+    x0, x1, z0, z1 = extent
+    xs = x0 + (x1 - x0) * np.arange(nx, dtype=np.float64) / (nx - 1)
+    zs = z0 + (z1 - z0) * np.arange(nz, dtype=np.float64) / (nz - 1)
+    X, Z = np.meshgrid(xs, zs, indexing="xy")          # (nz, nx)
+    Y = amplitude * fbm_noise(seed, 6, 2.0, 0.5, X.ravel(), np.zeros(X.size), Z.ravel()).reshape(X.shape)
+    P = np.stack([X, Y, Z], axis=-1)                     # (nz, nx, 3)
+    a = P[:-1, :-1]   # (j, i)
+    b = P[:-1, 1:]    # (j, i+1)
+    c = P[1:, :-1]    # (j+1, i)
+    d = P[1:, 1:]     # (j+1, i+1)
+    # Two triangles per cell, upward geometric normals: (a, c, b) and (b, c, d).
+    t1 = np.concatenate([a, c, b], axis=-1).reshape(-1, 9)
+    t2 = np.concatenate([b, c, d], axis=-1).reshape(-1, 9)
+    tris = np.stack([t1, t2], axis=1).reshape(-1, 9)
+    v = _f32(tris)
+    pitch = -math.degrees(math.atan(4.0 / 12.0))
+    ld = np.array([0.3, 1.0, 0.2])
+    ld = ld / np.linalg.norm(ld)
+    return SceneDesc(
+        name=f"heightfield(seed={seed}, {nx}x{nz} vertices)",
+        vertices=v,
+        material_index=np.zeros(v.shape[0], dtype=np.uint32),
+        materials=[Material(diffuse=(0.8, 0.8, 0.8))],
+        camera=CameraDesc(position=(0.0, 4.0, 12.0), pitch=pitch, yaw=0.0, roll=0.0, fov=45.0),
+        width=width,
+        height=height,
+        light_direction=tuple(float(c) for c in -ld),
+        max_leaf_size=4,
+        settings=dict(tracer="ray"),
+    )

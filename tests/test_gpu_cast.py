@@ -1,0 +1,63 @@
+"""GPU ray queries vs the float32 oracle (bit-exact) — closest and any hit,
+both traversal orders, the RAY frame (primary + shadow) and the generic cast."""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import oracle
+from raycer_gb300 import _native as N
+from raycer_gb300 import scenes
+from raycer_gb300.tracer import CudaTracer, TracerState, camera_record
+
+from helpers import camera_floats, small_heightfield, small_room
+
+pytestmark = pytest.mark.gpu
+
+
+def _frame(sc, order):
+    with CudaTracer(0) as t:
+        t.initializeBuffers(sc)
+        t.set_traversal_order(order)
+        t.initializeImageBuffers(sc.width, sc.height)
+        st = TracerState(scene=sc, filmWidth=sc.width, filmHeight=sc.height, pixelCount=sc.width * sc.height)
+        t.run(st)
+        assert st.pixelsProcessed == sc.width * sc.height
+        return t.read_cast().view(np.int32).reshape(-1, 4), camera_floats(camera_record(sc))
+
+
+@pytest.mark.parametrize("order", [N.RC_ORDER_REFERENCE, N.RC_ORDER_NEAREST])
+@pytest.mark.parametrize("which", ["room", "heightfield"])
+def test_raycast_frame_bit_exact(which, order):
+    sc = small_room() if which == "room" else small_heightfield()
+    if which == "room":
+        sc.light_direction = (-0.3, -1.0, -0.2)
+    gpu, cam = _frame(sc, order)
+    orc = oracle.Oracle(sc)
+    L = -np.array(sc.light_direction, np.float32)
+    ref, _ = orc.raycast32(cam, sc.width, sc.width * sc.height, L, order=order)
+    assert np.array_equal(gpu, ref), f"{(gpu != ref).any(axis=1).sum()} pixels differ"
+
+
+@pytest.mark.parametrize("any_hit", [False, True])
+@pytest.mark.parametrize("order", [N.RC_ORDER_REFERENCE, N.RC_ORDER_NEAREST])
+def test_cast_random_rays_bit_exact(any_hit, order):
+    sc = small_room(clutter=1000)
+    rng = np.random.default_rng(5)
+    n = 200_000
+    rays = np.zeros(n, dtype=[("origin", "<f4", 3), ("t_min", "<f4"), ("direction", "<f4", 3), ("t_max", "<f4")])
+    rays["origin"] = rng.uniform(-0.95, 0.95, size=(n, 3))
+    d = rng.normal(size=(n, 3))
+    rays["direction"] = d / np.linalg.norm(d, axis=1, keepdims=True)
+    rays["t_min"] = 0.0
+    rays["t_max"] = np.where(rng.uniform(size=n) < 0.5, np.float32(3.0e38), rng.uniform(0.1, 2.0, size=n))
+    with CudaTracer(0) as t:
+        t.initializeBuffers(sc)
+        hits = t.cast(rays, any_hit=any_hit, order=order)
+    orc = oracle.Oracle(sc)
+    prim, tt, u, v, _ = orc.cast32(rays, any_hit=any_hit, order=order)
+    assert np.array_equal(hits["prim"], prim)
+    assert np.array_equal(hits["t"], tt)
+    assert np.array_equal(hits["u"], u)
+    assert np.array_equal(hits["v"], v)

@@ -1,0 +1,31 @@
+"""GPU path tracer vs the float32 oracle (bit-exact film)."""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import oracle
+from raycer_gb300.tracer import CudaTracer, TracerState, camera_record
+
+from helpers import camera_floats, small_room
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("ms,P,depth,sampler", [(1, 1, 4, 4), (2, 1, 4, 4), (3, 2, 5, 4), (2, 1, 3, 1)])
+def test_film_bit_exact(ms, P, depth, sampler):
+    sc = small_room(width=48, height=36)
+    sc.settings.update(multi_sample_count_sqrt=ms, path_sample_count=P, max_path_length=depth,
+                       sampler={4: "cmj", 1: "random"}[sampler])
+    with CudaTracer(0) as t:
+        t.initializeBuffers(sc, seed=11)
+        t.initializeImageBuffers(sc.width, sc.height)
+        st = TracerState(scene=sc, filmWidth=sc.width, filmHeight=sc.height, pixelCount=sc.width * sc.height)
+        t.run(st)
+        film = t.read_film()
+        cam = camera_floats(camera_record(sc))
+    orc = oracle.Oracle(sc)
+    ref, _ = orc.render_path32(cam, sc.width, sc.width * sc.height, ms, P, sampler, (0.5, 0.5), 1e-5, depth, 0, 1,
+                               11, 0)
+    assert np.array_equal(film, ref), f"{(film != ref).any(axis=1).sum()} pixels differ"
