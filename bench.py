@@ -1,0 +1,386 @@
+"""Benchmark: ray casting on the 1,045,506-triangle heightfield at 1920x1080.
+
+One step = one RAY frame: a closest-hit primary ray for every pixel and, for
+every pixel that hits, one any-hit shadow ray toward the directional light
+(the RAY tracer's ray set, Raytracer.cpp:27-97 + 497-522). Metric: Mrays/s =
+BVH queries (primary + shadow) per second.
+
+  value     device time of the frame (CUDA events on the tracer's stream, the
+            scene resident in HBM, L2 flushed by a 512 MB write before every
+            step, outside the timed events)
+  e2e       the same frame through the C ABI with host buffers:
+            rc_cast_with_shadow(pinned host rays -> pinned host results), the
+            copies inside the timed region
+  roofline  the primary closest-hit kernel: algorithmic bytes per launch
+            (64 B per inner-node fetch + 48 B per triangle test, counted by a
+            counting render that equals the float32 oracle's count, + 16 B
+            result and 8 B queue entry per pixel) / its average event time
+
+`--impl reference` times the reference's CPU ray casting on this host's cores
+(the reference's own code where it was compiled, else the float64 port) on
+the same workload, one full frame per step.
+
+Multi-GPU: replicas only (every rank renders the full frame on its own GPU).
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Mrays/s"
+WORKLOAD = "heightfield ray cast 1920x1080: primary closest hit + directional shadow any-hit, 1,045,506 tris, SAH leaf<=4"
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--order", choices=["nearest", "reference"], default="nearest")
+    return ap.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)), int(os.environ.get("WORLD_SIZE", 1))
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples every 200 ms while running."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[3:7]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """DRAM bytes per launch of the primary kernel from the committed ncu summary."""
+    f = ROOT / "profiles" / "raycast_primary_heightfield_1080p.md"
+    if not f.exists():
+        return None
+    m = re.search(r"dram_bytes_per_launch:\s*([0-9.eE+]+)", f.read_text())
+    return float(m.group(1)) if m else None
+
+
+def cpu_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+# ---------------------------------------------------------------------------
+# CPU reference / port timing (one full frame per step)
+
+def cpu_raycast(sc, steps, warmup, bvh):
+    import oracle
+    from raycer_gb300.tracer import camera_record
+
+    threads = cpu_threads()
+    if oracle.ref_available(fast=True):
+        kind = "reference"
+        ref = oracle.RefScene(sc, fast=True)
+        ref.set_general(0, 3, 1, 1)
+
+        def frame():
+            _, _, rays, sec = ref.render(sc.width, sc.height, threads=threads)
+            return rays, sec
+    else:
+        kind = "port"
+        orc = oracle.Oracle(sc, prebuilt=bvh)
+        cam = camera_record(sc)
+        cam64 = np.array(list(cam.position) + list(cam.right) + list(cam.up) + list(cam.image_plane_center) +
+                         [cam.aspect_ratio, cam.image_plane_width, cam.image_plane_height], np.float64)
+        L = -np.array(sc.light_direction, np.float64)
+        n = sc.width * sc.height
+
+        def frame():
+            _, _, _, rays, sec = orc.raycast64(cam64, sc.width, n, L, 1e-5, threads=threads)
+            return rays, sec
+    for _ in range(warmup):
+        frame()
+    tot_rays, tot_sec, best = 0, 0.0, 0.0
+    for _ in range(steps):
+        rays, sec = frame()
+        tot_rays += rays
+        tot_sec += sec
+        best = max(best, rays / sec / 1e6)
+    return {"kind": kind, "cores": threads, "value": tot_rays / tot_sec / 1e6, "best": best,
+            "rays_per_frame": tot_rays // max(steps, 1), "sec_per_frame": tot_sec / max(steps, 1)}
+
+
+# ---------------------------------------------------------------------------
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return 0
+    from raycer_gb300 import scenes
+    sc = scenes.heightfield_scene()
+    bvh = None
+    try:
+        import oracle
+        if not oracle.ref_available(fast=True):
+            import ctypes as C
+            from raycer_gb300 import _native as N
+            v = np.ascontiguousarray(sc.vertices)
+            cnt = C.c_int64(0)
+            N.lib().rc_build_bvh(C.c_void_p(v.ctypes.data), v.shape[0], 4, None, 0, C.byref(cnt), None, None)
+            nodes = np.empty(cnt.value, oracle.NODE_DTYPE)
+            order = np.empty(v.shape[0], np.uint64)
+            N.lib().rc_build_bvh(C.c_void_p(v.ctypes.data), v.shape[0], 4, C.c_void_p(nodes.ctypes.data),
+                                 cnt.value, C.byref(cnt), C.c_void_p(order.ctypes.data), None)
+            bvh = (nodes, order)
+    except ImportError as e:
+        print(json.dumps({"impl": "reference", "unavailable": f"oracle not built: {e}"}))
+        return 0
+    res = cpu_raycast(sc, args.steps, args.warmup, bvh)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(res["value"], 3), "unit": METRIC,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(res["sec_per_frame"] * 1e3, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded fBm heightfield)",
+        "config": {"workload": WORKLOAD, "rays_per_step": int(res["rays_per_frame"])},
+        "cpu_baseline": {"value": round(res["value"], 3), "unit": METRIC, "cores": res["cores"], "kind": res["kind"],
+                         "sample": "full 1920x1080 frame per step (all pixels, primary + shadow rays)"},
+        "e2e": {"value": round(res["value"], 3), "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_ours(args, rank, local_rank, world):
+    import ctypes as C
+
+    import torch
+
+    from raycer_gb300 import _native as N
+    from raycer_gb300 import scenes
+    from raycer_gb300.tracer import CAST_DTYPE, RAY_DTYPE, CudaTracer, TracerState, camera_record
+
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+
+    sc = scenes.heightfield_scene()
+    n_pix = sc.width * sc.height
+    tracer = CudaTracer(local_rank)
+    tracer.initializeBuffers(sc)
+    tracer.initializeImageBuffers(sc.width, sc.height)
+    tracer.set_traversal_order(N.RC_ORDER_NEAREST if args.order == "nearest" else N.RC_ORDER_REFERENCE)
+    state = TracerState(scene=sc, filmWidth=sc.width, filmHeight=sc.height, pixelCount=n_pix)
+
+    # Traversal counts of one frame (deterministic; equal to the float32
+    # oracle's counters) for the roofline's algorithmic bytes.
+    tracer.set_counting(True)
+    tracer.run(state)
+    counted = tracer.stats()
+    tracer.set_counting(False)
+
+    stream = torch.cuda.ExternalStream(N.lib().rc_stream(tracer.handle), device=torch.device("cuda", local_rank))
+    flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device=torch.device("cuda", local_rank))
+
+    def flush_l2():
+        with torch.cuda.stream(stream):
+            flush.zero_()
+
+    for _ in range(args.warmup):
+        flush_l2()
+        tracer.run(state)
+
+    frame_ms, prim_ms, shadow_ms, rays = [], [], [], []
+    barrier()
+    with ClockSampler(local_rank) as clocks:
+        t_wall0 = time.perf_counter()
+        for _ in range(args.steps):
+            flush_l2()
+            tracer.run(state)
+            s = tracer.stats()
+            frame_ms.append(s["last_ms"])
+            prim_ms.append(s["stage_ms"][0])
+            shadow_ms.append(s["stage_ms"][1])
+            rays.append(s["rays_traced"])
+        barrier()
+        t_wall = time.perf_counter() - t_wall0
+    dev_sec = sum(frame_ms) / 1e3
+    total_rays = sum(rays)
+
+    # e2e: host rays in, host results out, through rc_cast_with_shadow.
+    cam = camera_record(sc)
+    pos = np.array(cam.position, np.float32)
+    ys, xs = np.divmod(np.arange(n_pix), sc.width)
+    dx = xs.astype(np.float32) / np.float32(cam.image_plane_width) - np.float32(0.5)
+    dy = ys.astype(np.float32) / np.float32(cam.image_plane_height) - np.float32(0.5)
+    p = (np.array(cam.image_plane_center, np.float32)[None, :] + dx[:, None] * np.array(cam.right, np.float32) +
+         (dy * np.float32(cam.aspect_ratio))[:, None] * np.array(cam.up, np.float32))
+    d = p - pos[None, :]
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    rays_pinned = torch.empty((n_pix, 8), dtype=torch.float32, pin_memory=True)
+    rays_np = rays_pinned.numpy()
+    rays_np[:, 0:3] = pos
+    rays_np[:, 3] = 0.0
+    rays_np[:, 4:7] = d
+    rays_np[:, 7] = np.float32(3.4028234663852886e38)
+    out_pinned = torch.empty((n_pix, 4), dtype=torch.int32, pin_memory=True)
+    rp = C.c_void_p(rays_pinned.data_ptr())
+    op = C.c_void_p(out_pinned.data_ptr())
+    order = N.RC_ORDER_NEAREST if args.order == "nearest" else N.RC_ORDER_REFERENCE
+    for _ in range(max(1, args.warmup)):
+        assert N.lib().rc_cast_with_shadow(tracer.handle, rp, n_pix, order, op) == N.RC_OK
+    e2e_rays = 0
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        st = N.lib().rc_cast_with_shadow(tracer.handle, rp, n_pix, order, op)
+        if st != N.RC_OK:
+            raise RuntimeError(N.lib().rc_last_error(tracer.handle).decode())
+        e2e_rays += tracer.stats()["rays_traced"]
+    barrier()
+    e2e_sec = time.perf_counter() - t0
+
+    bvh = tracer.get_bvh() if rank == 0 else None
+
+    # max over ranks of the timed regions
+    times = torch.tensor([dev_sec, e2e_sec, t_wall], dtype=torch.float64, device=torch.device("cuda", local_rank))
+    rays_t = torch.tensor([float(total_rays), float(e2e_rays)], dtype=torch.float64,
+                          device=torch.device("cuda", local_rank))
+    if world > 1:
+        torch.distributed.all_reduce(times, op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.all_reduce(rays_t, op=torch.distributed.ReduceOp.SUM)
+    dev_sec, e2e_sec, t_wall = times.tolist()
+    total_rays, e2e_rays = rays_t.tolist()
+
+    line = None
+    if rank == 0:
+        peak, peak_kind = measured_peaks()
+        s0_nodes, s0_tris = counted["stage_nodes"][0], counted["stage_tris"][0]
+        hits = counted["stage_rays"][1]
+        prim_bytes = 64 * s0_nodes + 48 * s0_tris + 16 * n_pix + 8 * hits
+        prim_avg = statistics.mean(prim_ms) / 1e3
+        achieved = prim_bytes / prim_avg / 1e9
+        traffic = profiled_traffic()
+        line = {
+            "metric": METRIC, "value": round(total_rays / dev_sec / 1e6, 2), "unit": METRIC,
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(dev_sec / args.steps * 1e3, 4), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded fBm heightfield, value noise seed 2)",
+            "config": {"workload": WORKLOAD, "rays_per_step": int(rays[0]), "pixels": n_pix,
+                       "traversal_order": args.order, "l2": "flushed (512 MB write) before every step",
+                       "parallelism": f"replicas x{world}"},
+            "e2e": {"value": round(e2e_rays / e2e_sec / 1e6, 2), "unit": METRIC,
+                    "h2d_bytes_per_step": n_pix * 32, "d2h_bytes_per_step": n_pix * 16},
+            "gpu_launches": 2 * args.steps,
+            "roofline": {"bound": "hbm", "kernel": "k_raycast_primary (closest hit)", "achieved": round(achieved, 1),
+                         "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                         "algorithmic_bytes_per_launch": int(prim_bytes),
+                         "avg_launch_ms": round(prim_avg * 1e3, 4),
+                         "traffic": traffic,
+                         "node_fetches": int(s0_nodes), "triangle_tests": int(s0_tris)},
+            "stages_ms": {"primary": round(statistics.mean(prim_ms), 4), "shadow": round(statistics.mean(shadow_ms), 4)},
+            "wall_s": round(t_wall, 3),
+            "clocks": clocks.summary(),
+        }
+    if world > 1:
+        torch.distributed.barrier()
+        torch.distributed.destroy_process_group()
+    tracer.close()
+    if rank == 0:
+        if world == 1:
+            try:
+                res = cpu_raycast(sc, 2, 1, bvh)
+                line["cpu_baseline"] = {"value": round(res["value"], 3), "unit": METRIC, "cores": res["cores"],
+                                        "kind": res["kind"],
+                                        "sample": "full 1920x1080 frame (primary + shadow rays), 1 warm-up + 2 "
+                                                  "timed frames"}
+            except ImportError as e:
+                line["cpu_baseline"] = {"value": None, "unit": METRIC, "cores": cpu_threads(), "kind": "port",
+                                        "sample": f"unavailable: {e}"}
+        print(json.dumps(line))
+    return 0
+
+
+def main():
+    args = parse_args()
+    rank, local_rank, world = dist_env()
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+    return run_ours(args, rank, local_rank, world)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

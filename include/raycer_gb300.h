@@ -186,6 +186,14 @@ typedef struct rc_stats
     uint64_t bvh_inner_nodes;  /* inner nodes of the device BVH                */
     uint64_t bvh_depth;        /* depth of the uploaded BVH                    */
     uint64_t device_bytes;     /* device memory held by the handle             */
+    /* Per stage of the last call. RAY render / cast_with_shadow: 0 = primary
+     * closest-hit kernel, 1 = shadow any-hit kernel. PATH render: 0 = the
+     * extend (closest-hit) kernels of all segments, 1 = everything else
+     * (generate, shade, accumulate). cast: 0 = the cast kernel. */
+    uint64_t stage_rays[2];
+    uint64_t stage_nodes[2];   /* when counting is on */
+    uint64_t stage_tris[2];    /* when counting is on */
+    double stage_ms[2];        /* device time from CUDA events around the stage's launches */
 } rc_stats;
 
 /* ------------------------------------------------------------------------ */

@@ -62,6 +62,8 @@ _ORACLE_PROTOS = {
     "or32_render_path": (None, [P, P, u64, u64, u64, C.c_int, C.c_int, C.c_int, f32, f32, f32, C.c_int, C.c_int,
                                 C.c_int, u64, u32, P, P, C.c_int]),
     "or32_sincos_turn": (None, [i64, P, P, P]),
+    "or64_cmj": (None, [u64, u64, u64, u64, f64, f64, P]),
+    "or32_cmj_permute": (u64, [u64, u64, u64]),
 }
 
 _REF_PROTOS = {
@@ -87,7 +89,7 @@ _REF_PROTOS = {
     "ref_tonemap_reinhard": (None, [i64, P, f64, f64, C.c_int, C.c_int, P]),
     "ref_fastpow": (f64, [f64, f64]),
     "ref_value_noise": (None, [u32, i64, P, u64, f64, f64, P]),
-    "ref_cmj_pattern": (None, [u64, u64, u32, P]),
+    "ref_cmj_pattern": (None, [u64, u64, u32, P, P]),
 }
 
 _oracle = None

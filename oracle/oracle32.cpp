@@ -147,7 +147,8 @@ bool tri32(const float* tr, const Ray32& r, float& t, float& u, float& v)
 // intersectBVH (intersections.cl:98-148) over the reference's flat node
 // array. order 0: the reference's visit order; order 1: nearer child first
 // with distance culling (the device's alternative order).
-bool traverse32(const Scene32& s, const Ray32& r, bool anyHit, int order, Hit32& h, uint64_t* nodes, uint64_t* tris)
+bool traverse32(const Scene32& s, const Ray32& r, bool anyHit, int order, Hit32& h, uint64_t* nodes, uint64_t* tris,
+                int64_t skip)
 {
     const std::vector<Node64>& N = s.src->nodes;
     struct Entry
@@ -169,6 +170,8 @@ bool traverse32(const Scene32& s, const Ray32& r, bool anyHit, int order, Hit32&
             for (uint64_t i = 0; i < nd.count; ++i)
             {
                 uint64_t slot = nd.start + i;
+                if (int64_t(slot) == skip)
+                    continue;
                 if (anyHit && (s.meta[slot] & 0x80000000u))
                     continue;
                 if (tris)
@@ -398,7 +401,7 @@ void raycast32(const Scene32& s, const Camera32& cam, uint64_t width, uint64_t p
         Ray32 r = make_ray32(o, d, 0.0f, FLT_MAX);
         Hit32 h;
         uint64_t nn = 0, nt = 0;
-        bool found = traverse32(s, r, false, order, h, &nn, &nt);
+        bool found = traverse32(s, r, false, order, h, &nn, &nt, -1);
         totalRays++;
         int32_t* w = out4 + i * 4;
         w[0] = found ? s.caller[size_t(h.slot)] : -1;
@@ -414,7 +417,9 @@ void raycast32(const Scene32& s, const Camera32& cam, uint64_t width, uint64_t p
                     std::fmaf(dl.z, rayStartOffset, ip.z) };
             Ray32 sr = make_ray32(so, dl, 0.0f, FLT_MAX);
             Hit32 sh;
-            bool occ = traverse32(s, sr, true, 0, sh, &nn, &nt);
+            // the shadow ray skips the triangle it leaves from (exact-arithmetic
+            // semantics of the offset origin; same as the device)
+            bool occ = traverse32(s, sr, true, 0, sh, &nn, &nt, h.slot);
             totalRays++;
             w[2] = occ ? s.caller[size_t(sh.slot)] : -1;
             w[3] = 1 | 2 | (occ ? 4 : 0);
@@ -443,7 +448,7 @@ void cast32(const Scene32& s, int64_t n, const float* rays8, int anyHit, int ord
         Ray32 r = make_ray32(V3f{ q[0], q[1], q[2] }, V3f{ q[4], q[5], q[6] }, q[3], q[7]);
         Hit32 h;
         uint64_t nn = 0, nt = 0;
-        bool found = traverse32(s, r, anyHit != 0, order, h, &nn, &nt);
+        bool found = traverse32(s, r, anyHit != 0, order, h, &nn, &nt, -1);
         prim[i] = found ? s.caller[size_t(h.slot)] : -1;
         t[i] = found ? h.t : -1.0f;
         u[i] = found ? h.u : 0.0f;
@@ -525,6 +530,7 @@ void render_path32(const Scene32& s, const Camera32& cam, const PathSettings32& 
                 uint32_t key = stream_key(ps.seed, ps.frame, pg, sample);
                 V3f o{ cam.pos[0], cam.pos[1], cam.pos[2] };
                 V3f d = d0;
+                int64_t from = -1;
                 float thr[3] = { 1.0f, 1.0f, 1.0f };
                 float res[3] = { 0.0f, 0.0f, 0.0f };
                 for (int seg = 0; seg < ps.maxPathLength; ++seg)
@@ -532,7 +538,7 @@ void render_path32(const Scene32& s, const Camera32& cam, const PathSettings32& 
                     Ray32 r = make_ray32(o, d, 0.0f, FLT_MAX);
                     Hit32 h;
                     totalRays++;
-                    if (!traverse32(s, r, false, ps.order, h, nullptr, nullptr))
+                    if (!traverse32(s, r, false, ps.order, h, nullptr, nullptr, from))
                         break;
                     const Material& m = s.src->mats[s.meta[size_t(h.slot)] & 0x00ffffffu];
                     if (m.flags & 1)
@@ -566,6 +572,7 @@ void render_path32(const Scene32& s, const Camera32& cam, const PathSettings32& 
                     o = V3f{ std::fmaf(dir.x, ps.rayStartOffset, ip.x), std::fmaf(dir.y, ps.rayStartOffset, ip.y),
                              std::fmaf(dir.z, ps.rayStartOffset, ip.z) };
                     d = dir;
+                    from = h.slot;
                     float alpha = std::fabs(dot3(dir, nrm));
                     thr[0] = thr[0] * ((2.0f * m.diffuse[0]) * alpha);
                     thr[1] = thr[1] * ((2.0f * m.diffuse[1]) * alpha);

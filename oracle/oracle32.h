@@ -50,7 +50,8 @@ struct PathSettings32
 };
 
 Ray32 make_ray32(V3f o, V3f d, float tmin, float tmax);
-bool traverse32(const Scene32& s, const Ray32& r, bool anyHit, int order, Hit32& h, uint64_t* nodes, uint64_t* tris);
+bool traverse32(const Scene32& s, const Ray32& r, bool anyHit, int order, Hit32& h, uint64_t* nodes, uint64_t* tris,
+                int64_t skip);
 V3f camera_dir32(const Camera32& c, float px, float py);
 void raycast32(const Scene32& s, const Camera32& cam, uint64_t width, uint64_t pixelStart, uint64_t count,
                const float* L, float rayStartOffset, int order, int32_t* out4, uint64_t* counters, int threads);

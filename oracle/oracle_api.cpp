@@ -263,6 +263,15 @@ void or32_render_path(void* hp, const float* cam, uint64_t width, uint64_t pixel
     render_path32(H(hp)->s32, cam32(cam), ps, width, pixelStart, count, film, counters, threads);
 }
 
+// CMJSampler::getSample2D restated (float64 port) for given jitter values.
+void or64_cmj(uint64_t x, uint64_t y, uint64_t n, uint64_t permutation, double jx, double jy, double* out)
+{
+    out[0] = cmj_component(x, y, n, permutation, jx, jy, 0);
+    out[1] = cmj_component(x, y, n, permutation, jx, jy, 1);
+}
+
+uint64_t or32_cmj_permute(uint64_t i, uint64_t l, uint64_t p) { return cmj_permute32(i, l, p); }
+
 void or32_sincos_turn(int64_t n, const float* x, float* s, float* c)
 {
     for (int64_t i = 0; i < n; ++i)

@@ -529,8 +529,17 @@ void ref_value_noise(uint32_t seed, int64_t n, const double* xyz, uint64_t octav
 
 // CMJSampler::getSample2D for every (x, y) of an n x n pattern with the given
 // permutation; the random jitter comes from std::mt19937(seed). out: n*n*2.
-void ref_cmj_pattern(uint64_t n, uint64_t permutation, uint32_t seed, double* out)
+// jitter (optional, n*n*2): the uniform draws the sampler consumed, in order
+// (taken from a second generator with the same seed).
+void ref_cmj_pattern(uint64_t n, uint64_t permutation, uint32_t seed, double* out, double* jitter)
 {
+    if (jitter)
+    {
+        std::mt19937 twin(seed);
+        std::uniform_real_distribution<double> u(0.0, 1.0);
+        for (uint64_t i = 0; i < n * n * 2; ++i)
+            jitter[i] = u(twin);
+    }
     CMJSampler sampler;
     std::mt19937 gen(seed);
     for (uint64_t y = 0; y < n; ++y)

@@ -90,7 +90,8 @@ class rc_cast_pixel(C.Structure):
 class rc_stats(C.Structure):
     _fields_ = [("rays_traced", C.c_uint64), ("node_visits", C.c_uint64), ("tri_tests", C.c_uint64),
                 ("last_ms", C.c_double), ("bvh_inner_nodes", C.c_uint64), ("bvh_depth", C.c_uint64),
-                ("device_bytes", C.c_uint64)]
+                ("device_bytes", C.c_uint64), ("stage_rays", C.c_uint64 * 2), ("stage_nodes", C.c_uint64 * 2),
+                ("stage_tris", C.c_uint64 * 2), ("stage_ms", C.c_double * 2)]
 
 
 P = C.c_void_p

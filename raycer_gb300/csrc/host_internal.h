@@ -19,6 +19,8 @@ struct rc_tracer
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr;
     cudaEvent_t ev1 = nullptr;
+    cudaEvent_t evMid = nullptr;           // between the RAY frame's two kernels
+    std::vector<cudaEvent_t> evPool;       // around each PATH extend launch
     std::string err;
 
     // Scene (device layout of device_types.h) and its host flat-BVH copy.

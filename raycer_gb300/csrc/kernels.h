@@ -15,7 +15,7 @@ namespace rcx
 struct DevControl
 {
     unsigned int head[8];          // work-queue heads / queue counts
-    unsigned long long stats[4];   // rays, node fetches, triangle tests, spare
+    unsigned long long stats[8];   // per stage s: [3s] rays, [3s+1] node fetches, [3s+2] triangle tests
     int error;                     // bit0: traversal stack overflow
     int pad[3];
 };
@@ -34,10 +34,10 @@ cudaError_t launch_cast(const LaunchInfo& li, const DevScene& sc, const rc_ray* 
 // Ray-cast frame: primary closest hit per pixel + shadow any-hit per hit.
 // Primary rays come from the camera (rays == nullptr) or from `rays`
 // (one per pixel, caller order). Writes out[0..count); shadowQueue needs
-// `count` entries. ctl->head[0], head[1], head[2] must be zero on entry.
+// 2 * `count` ints (pixel, hit slot). ctl->head[0], head[1], head[2] must be zero on entry.
 cudaError_t launch_raycast(const LaunchInfo& li, const DevScene& sc, const DevCamera& cam, const rc_ray* rays,
                            uint64_t pixelStart, int64_t count, int64_t width, int order, int castShadow,
                            float3 dirToLight, float rayStartOffset, rc_cast_pixel* out, int* shadowQueue,
-                           DevControl* ctl);
+                           DevControl* ctl, cudaEvent_t between);
 
 }  // namespace rcx

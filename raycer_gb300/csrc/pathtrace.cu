@@ -5,7 +5,8 @@
 // to sample (s % spp) of it, where spp = n*n camera samples (Tracer.cpp:
 // 115-144, CMJ + box filter) x pathSampleCount paths per camera sample
 // (PathTracer.cpp:19). Path state lives in SoA arrays indexed by slot:
-//   o, d       ray (float4 each)
+//   o, d       ray (float4 each); o.w = the triangle the ray leaves from
+//              (skipped by its closest-hit query, see traverse.cuh)
 //   thr        path throughput (rgb)
 //   res        radiance result (rgb) + the camera sample's filter weight (w)
 //   hit        closest hit of the last extend (slot, t, u, v)
@@ -119,7 +120,7 @@ __global__ void __launch_bounds__(256) k_generate(PathParams p)
         py = __fadd_rn(py, oy);
     }
     V3 d = camera_dir(p.cam, px, py);
-    p.o[s] = make_float4(p.cam.pos[0], p.cam.pos[1], p.cam.pos[2], 0.0f);
+    p.o[s] = make_float4(p.cam.pos[0], p.cam.pos[1], p.cam.pos[2], __int_as_float(-1));
     p.d[s] = make_float4(d.x, d.y, d.z, 0.0f);
     p.thr[s] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
     p.res[s] = make_float4(0.0f, 0.0f, 0.0f, w);
@@ -147,7 +148,7 @@ __global__ void __launch_bounds__(kBlock) k_extend(PathParams p, int segment)
             float4 d = p.d[s];
             RayF ray = make_ray(v3(o.x, o.y, o.z), v3(d.x, d.y, d.z), 0.0f, FLT_MAX);
             HitF h{ -1, FLT_MAX, 0.0f, 0.0f };
-            bool found = traverse<false, ORDER, COUNT>(p.sc, ray, h, cnt, err);
+            bool found = traverse<false, ORDER, COUNT>(p.sc, ray, h, cnt, err, __float_as_int(o.w));
             p.hit[s] = make_int4(found ? h.slot : -1, __float_as_int(h.t), __float_as_int(h.u), __float_as_int(h.v));
             done++;
         }
@@ -250,7 +251,7 @@ __global__ void __launch_bounds__(kBlock) k_shade(PathParams p, int segment)
                         thr.x = __fmul_rn(thr.x, __fmul_rn(__fmul_rn(2.0f, md.x), alpha));
                         thr.y = __fmul_rn(thr.y, __fmul_rn(__fmul_rn(2.0f, md.y), alpha));
                         thr.z = __fmul_rn(thr.z, __fmul_rn(__fmul_rn(2.0f, md.z), alpha));
-                        p.o[s] = make_float4(no.x, no.y, no.z, 0.0f);
+                        p.o[s] = make_float4(no.x, no.y, no.z, __int_as_float(h.x));
                         p.d[s] = make_float4(dir.x, dir.y, dir.z, 0.0f);
                         p.thr[s] = thr;
                         cont = true;
@@ -324,7 +325,7 @@ cudaError_t extend_t(const PathParams& p, int segment, cudaStream_t stream, int 
 }  // namespace
 
 cudaError_t launch_path_pass(const PathParams& p, int pixelsInPass, int order, int counting, cudaStream_t stream,
-                             int numSMs)
+                             int numSMs, const cudaEvent_t* extendEvents)
 {
     k_generate<<<unsigned((p.nslots + 255) / 256), 256, 0, stream>>>(p);
     cudaError_t e = cudaGetLastError();
@@ -335,6 +336,8 @@ cudaError_t launch_path_pass(const PathParams& p, int pixelsInPass, int order, i
         shadeGrid = persistent_blocks(k_shade, numSMs);
     for (int seg = 0; seg < p.maxPathLength; ++seg)
     {
+        if (extendEvents && (e = cudaEventRecord(extendEvents[2 * seg], stream)) != cudaSuccess)
+            return e;
         if (order == ORDER_NEAREST)
             e = counting ? extend_t<ORDER_NEAREST, true>(p, seg, stream, numSMs)
                          : extend_t<ORDER_NEAREST, false>(p, seg, stream, numSMs);
@@ -342,6 +345,8 @@ cudaError_t launch_path_pass(const PathParams& p, int pixelsInPass, int order, i
             e = counting ? extend_t<ORDER_REF, true>(p, seg, stream, numSMs)
                          : extend_t<ORDER_REF, false>(p, seg, stream, numSMs);
         if (e != cudaSuccess)
+            return e;
+        if (extendEvents && (e = cudaEventRecord(extendEvents[2 * seg + 1], stream)) != cudaSuccess)
             return e;
         k_shade<<<shadeGrid, kBlock, 0, stream>>>(p, seg);
         if ((e = cudaGetLastError()) != cudaSuccess)

@@ -45,8 +45,10 @@ struct PathParams
 // Bytes of path state per slot (o, d, thr, res, hit, two queue entries).
 constexpr size_t kPathBytesPerSlot = 5 * 16 + 2 * 4;
 
+// extendEvents: 2 * maxPathLength events recorded around each extend launch
+// (or nullptr).
 cudaError_t launch_path_pass(const PathParams& p, int pixelsInPass, int order, int counting, cudaStream_t stream,
-                             int numSMs);
+                             int numSMs, const cudaEvent_t* extendEvents);
 
 // Reinhard / passthrough resolve of the film into out (float4 per pixel).
 // partials needs tone_partials_bytes(pixels) bytes.

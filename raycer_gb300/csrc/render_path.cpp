@@ -163,9 +163,21 @@ rc_status render_path(rc_tracer* h, uint64_t pixelStart, uint64_t count, const v
     p.seed = g.seed;
     p.frame = h->frameIndex;
 
+    // Events around every extend launch of every pass (stage 0 timing).
+    const uint64_t passes = (count + pixelsPerPass - 1) / pixelsPerPass;
+    const size_t needEvents = size_t(passes) * size_t(2 * std::max(g.max_path_length, 0));
+    const bool timeStages = needEvents <= 4096;
+    while (timeStages && h->evPool.size() < needEvents)
+    {
+        cudaEvent_t e;
+        RC_CUDA_TRY(h, cudaEventCreate(&e), "create event");
+        h->evPool.push_back(e);
+    }
+
     RC_CUDA_TRY(h, cudaMemsetAsync(h->dCtl, 0, sizeof(DevControl), h->stream), "reset control block");
     RC_CUDA_TRY(h, cudaEventRecord(h->ev0, h->stream), "record start event");
-    for (uint64_t done = 0; done < count; done += pixelsPerPass)
+    uint64_t pass = 0;
+    for (uint64_t done = 0; done < count; done += pixelsPerPass, ++pass)
     {
         if (done > 0 && cancel && *cancel)
         {
@@ -177,7 +189,8 @@ rc_status render_path(rc_tracer* h, uint64_t pixelStart, uint64_t count, const v
         p.passPixel = done;
         p.nslots = int(np * spp);
         RC_CUDA_TRY(h, cudaMemsetAsync(h->dCounts, 0, countsBytes, h->stream), "reset queue counters");
-        RC_CUDA_TRY(h, launch_path_pass(p, int(np), h->order, h->counting, h->stream, h->numSMs),
+        const cudaEvent_t* ev = timeStages ? h->evPool.data() + pass * size_t(2 * g.max_path_length) : nullptr;
+        RC_CUDA_TRY(h, launch_path_pass(p, int(np), h->order, h->counting, h->stream, h->numSMs, ev),
                     "launch path-tracing pass");
     }
     RC_CUDA_TRY(h, cudaEventRecord(h->ev1, h->stream), "record end event");
@@ -187,10 +200,26 @@ rc_status render_path(rc_tracer* h, uint64_t pixelStart, uint64_t count, const v
     RC_CUDA_TRY(h, cudaStreamSynchronize(h->stream), "path tracing");
     float ms = 0.0f;
     cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+    double extendMs = 0.0;
+    if (timeStages)
+    {
+        for (size_t i = 0; i + 1 < needEvents; i += 2)
+        {
+            float m = 0.0f;
+            cudaEventElapsedTime(&m, h->evPool[i], h->evPool[i + 1]);
+            extendMs += double(m);
+        }
+    }
     h->stats.last_ms = double(ms);
+    h->stats.stage_ms[0] = extendMs;
+    h->stats.stage_ms[1] = double(ms) - extendMs;
     h->stats.rays_traced = ctl.stats[0];
     h->stats.node_visits = ctl.stats[1];
     h->stats.tri_tests = ctl.stats[2];
+    h->stats.stage_rays[0] = ctl.stats[0];
+    h->stats.stage_nodes[0] = ctl.stats[1];
+    h->stats.stage_tris[0] = ctl.stats[2];
+    h->stats.stage_rays[1] = h->stats.stage_nodes[1] = h->stats.stage_tris[1] = 0;
     h->frameIndex++;
     if (ctl.error & 1)
         return fail(h, RC_DEVICE_ERROR, "path tracing: traversal stack overflow");

@@ -29,7 +29,8 @@ __device__ __forceinline__ unsigned warp_fetch(unsigned* head, unsigned amount)
     return __shfl_sync(0xffffffffu, base, 0);
 }
 
-__device__ __forceinline__ void flush_counts(DevControl* ctl, unsigned long long rays, const TravCount& c, int err)
+__device__ __forceinline__ void flush_counts(DevControl* ctl, int stage, unsigned long long rays, const TravCount& c,
+                                             int err)
 {
     unsigned long long n = c.nodes, t = c.tris;
     for (int o = 16; o > 0; o >>= 1)
@@ -40,11 +41,11 @@ __device__ __forceinline__ void flush_counts(DevControl* ctl, unsigned long long
     }
     if (lane_id() == 0)
     {
-        atomicAdd(&ctl->stats[0], rays);
+        atomicAdd(&ctl->stats[3 * stage + 0], rays);
         if (n)
-            atomicAdd(&ctl->stats[1], n);
+            atomicAdd(&ctl->stats[3 * stage + 1], n);
         if (t)
-            atomicAdd(&ctl->stats[2], t);
+            atomicAdd(&ctl->stats[3 * stage + 2], t);
     }
     if (err)
         atomicOr(&ctl->error, 1);
@@ -85,7 +86,7 @@ __global__ void __launch_bounds__(kBlock) k_cast(DevScene sc, const rc_ray* __re
             done++;
         }
     }
-    flush_counts(ctl, done, cnt, err);
+    flush_counts(ctl, 0, done, cnt, err);
 }
 
 __device__ __forceinline__ RayF primary_ray(const DevCamera& cam, const rc_ray* __restrict__ rays, uint64_t pixel,
@@ -121,6 +122,7 @@ __global__ void __launch_bounds__(kBlock) k_raycast_primary(DevScene sc, DevCame
             break;
         int64_t i = int64_t(base) + lane_id();
         bool hitAny = false;
+        int hitSlot = -1;
         if (i < count)
         {
             RayF ray = primary_ray(cam, rays, pixelStart + uint64_t(i), i, width);
@@ -133,6 +135,7 @@ __global__ void __launch_bounds__(kBlock) k_raycast_primary(DevScene sc, DevCame
             o.w = found ? 1 : 0;
             reinterpret_cast<int4*>(out)[i] = o;
             hitAny = found && castShadow;
+            hitSlot = h.slot;
             done++;
         }
         // Warp-aggregated compaction of the hit pixels into the shadow queue.
@@ -144,15 +147,17 @@ __global__ void __launch_bounds__(kBlock) k_raycast_primary(DevScene sc, DevCame
                 qbase = atomicAdd(&ctl->head[1], unsigned(__popc(mask)));
             qbase = __shfl_sync(0xffffffffu, qbase, 0);
             if (hitAny)
-                queue[qbase + __popc(mask & ((1u << lane_id()) - 1u))] = int(i);
+                reinterpret_cast<int2*>(queue)[qbase + __popc(mask & ((1u << lane_id()) - 1u))] =
+                    make_int2(int(i), hitSlot);
         }
     }
-    flush_counts(ctl, done, cnt, err);
+    flush_counts(ctl, 0, done, cnt, err);
 }
 
 // Stage 2: one any-hit shadow ray toward the light per queued pixel
 // (Raytracer::calculateShadowAmount, Raytracer.cpp:497-522 /
-// lighting.cl:28-48): origin = hit position + dirToLight * rayStartOffset.
+// lighting.cl:28-48): origin = hit position + dirToLight * rayStartOffset;
+// the primary hit's own triangle is skipped (see traverse.cuh).
 template <bool COUNT>
 __global__ void __launch_bounds__(kBlock) k_raycast_shadow(DevScene sc, DevCamera cam, const rc_ray* __restrict__ rays,
                                                            uint64_t pixelStart, int64_t width, float3 L,
@@ -171,7 +176,8 @@ __global__ void __launch_bounds__(kBlock) k_raycast_shadow(DevScene sc, DevCamer
         unsigned q = base + lane_id();
         if (q < total)
         {
-            int i = queue[q];
+            int2 e = reinterpret_cast<const int2*>(queue)[q];
+            int i = e.x;
             RayF pr = primary_ray(cam, rays, pixelStart + uint64_t(i), i, width);
             float t = out[i].t;
             // ip = origin + t * direction (intersections.cl:85)
@@ -179,13 +185,13 @@ __global__ void __launch_bounds__(kBlock) k_raycast_shadow(DevScene sc, DevCamer
             V3 dl = v3(L.x, L.y, L.z);
             RayF sr = make_ray(vfma(dl, rayStartOffset, ip), dl, 0.0f, FLT_MAX);
             HitF h{ -1, FLT_MAX, 0.0f, 0.0f };
-            bool occ = traverse<true, ORDER_REF, COUNT>(sc, sr, h, cnt, err);
+            bool occ = traverse<true, ORDER_REF, COUNT>(sc, sr, h, cnt, err, e.y);
             out[i].occluder = occ ? caller_index(sc, h.slot) : -1;
             out[i].flags = 1 | 2 | (occ ? 4 : 0);
             done++;
         }
     }
-    flush_counts(ctl, done, cnt, err);
+    flush_counts(ctl, 1, done, cnt, err);
 }
 
 template <typename K>
@@ -212,7 +218,7 @@ cudaError_t cast_t(const LaunchInfo& li, const DevScene& sc, const rc_ray* rays,
 template <int ORDER, bool COUNT>
 cudaError_t raycast_t(const LaunchInfo& li, const DevScene& sc, const DevCamera& cam, const rc_ray* rays,
                       uint64_t pixelStart, int64_t count, int64_t width, int castShadow, float3 L, float off,
-                      rc_cast_pixel* out, int* queue, DevControl* ctl)
+                      rc_cast_pixel* out, int* queue, DevControl* ctl, cudaEvent_t between)
 {
     auto kp = k_raycast_primary<ORDER, COUNT>;
     auto ks = k_raycast_shadow<COUNT>;
@@ -223,6 +229,8 @@ cudaError_t raycast_t(const LaunchInfo& li, const DevScene& sc, const DevCamera&
         gs = persistent_blocks(ks, li.numSMs);
     kp<<<gp, kBlock, 0, li.stream>>>(sc, cam, rays, pixelStart, count, width, castShadow, out, queue, ctl);
     cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess && between)
+        e = cudaEventRecord(between, li.stream);
     if (e != cudaSuccess || !castShadow)
         return e;
     ks<<<gs, kBlock, 0, li.stream>>>(sc, cam, rays, pixelStart, width, L, off, out, queue, ctl);
@@ -249,19 +257,19 @@ cudaError_t launch_cast(const LaunchInfo& li, const DevScene& sc, const rc_ray* 
 cudaError_t launch_raycast(const LaunchInfo& li, const DevScene& sc, const DevCamera& cam, const rc_ray* rays,
                            uint64_t pixelStart, int64_t count, int64_t width, int order, int castShadow,
                            float3 dirToLight, float rayStartOffset, rc_cast_pixel* out, int* shadowQueue,
-                           DevControl* ctl)
+                           DevControl* ctl, cudaEvent_t between)
 {
     if (count <= 0)
         return cudaSuccess;
     if (order == ORDER_NEAREST)
         return li.counting ? raycast_t<ORDER_NEAREST, true>(li, sc, cam, rays, pixelStart, count, width, castShadow,
-                                                            dirToLight, rayStartOffset, out, shadowQueue, ctl)
+                                                            dirToLight, rayStartOffset, out, shadowQueue, ctl, between)
                            : raycast_t<ORDER_NEAREST, false>(li, sc, cam, rays, pixelStart, count, width, castShadow,
-                                                             dirToLight, rayStartOffset, out, shadowQueue, ctl);
+                                                             dirToLight, rayStartOffset, out, shadowQueue, ctl, between);
     return li.counting ? raycast_t<ORDER_REF, true>(li, sc, cam, rays, pixelStart, count, width, castShadow,
-                                                    dirToLight, rayStartOffset, out, shadowQueue, ctl)
+                                                    dirToLight, rayStartOffset, out, shadowQueue, ctl, between)
                        : raycast_t<ORDER_REF, false>(li, sc, cam, rays, pixelStart, count, width, castShadow,
-                                                     dirToLight, rayStartOffset, out, shadowQueue, ctl);
+                                                     dirToLight, rayStartOffset, out, shadowQueue, ctl, between);
 }
 
 }  // namespace rcx

@@ -118,7 +118,7 @@ void release_film(rc_tracer* h)
 {
     dev_free(h, &h->dFilm, size_t(h->filmPixels));
     dev_free(h, &h->dCast, size_t(h->filmPixels));
-    dev_free(h, &h->dQueue, size_t(h->filmPixels));
+    dev_free(h, &h->dQueue, size_t(h->filmPixels) * 2);
     h->filmPixels = 0;
     h->width = 0;
     h->height = 0;
@@ -403,19 +403,36 @@ rc_status begin_launch(rc_tracer* h)
     return RC_OK;
 }
 
-rc_status end_launch(rc_tracer* h, const char* what)
+rc_status end_launch(rc_tracer* h, const char* what, bool twoStage)
 {
     RC_CUDA_TRY(h, cudaEventRecord(h->ev1, h->stream), "record end event");
     DevControl ctl;
     RC_CUDA_TRY(h, cudaMemcpyAsync(&ctl, h->dCtl, sizeof(ctl), cudaMemcpyDeviceToHost, h->stream),
                 "read control block");
     RC_CUDA_TRY(h, cudaStreamSynchronize(h->stream), what);
-    float ms = 0.0f;
+    float ms = 0.0f, ms0 = 0.0f;
     cudaEventElapsedTime(&ms, h->ev0, h->ev1);
     h->stats.last_ms = double(ms);
-    h->stats.rays_traced = ctl.stats[0];
-    h->stats.node_visits = ctl.stats[1];
-    h->stats.tri_tests = ctl.stats[2];
+    if (twoStage)
+    {
+        cudaEventElapsedTime(&ms0, h->ev0, h->evMid);
+        h->stats.stage_ms[0] = double(ms0);
+        h->stats.stage_ms[1] = double(ms - ms0);
+    }
+    else
+    {
+        h->stats.stage_ms[0] = double(ms);
+        h->stats.stage_ms[1] = 0.0;
+    }
+    for (int k = 0; k < 2; ++k)
+    {
+        h->stats.stage_rays[k] = ctl.stats[3 * k + 0];
+        h->stats.stage_nodes[k] = ctl.stats[3 * k + 1];
+        h->stats.stage_tris[k] = ctl.stats[3 * k + 2];
+    }
+    h->stats.rays_traced = ctl.stats[0] + ctl.stats[3];
+    h->stats.node_visits = ctl.stats[1] + ctl.stats[4];
+    h->stats.tri_tests = ctl.stats[2] + ctl.stats[5];
     if (ctl.error & 1)
         return fail(h, RC_DEVICE_ERROR, std::string(what) + ": traversal stack overflow");
     return RC_OK;
@@ -447,6 +464,8 @@ rc_status rc_create(rc_tracer** out, int device)
         e = cudaEventCreate(&h->ev0);
     if (e == cudaSuccess)
         e = cudaEventCreate(&h->ev1);
+    if (e == cudaSuccess)
+        e = cudaEventCreate(&h->evMid);
     if (e == cudaSuccess)
         e = cudaMalloc(reinterpret_cast<void**>(&h->dCtl), sizeof(DevControl));
     if (e != cudaSuccess)
@@ -483,6 +502,10 @@ void rc_destroy(rc_tracer* h)
         cudaEventDestroy(h->ev0);
     if (h->ev1)
         cudaEventDestroy(h->ev1);
+    if (h->evMid)
+        cudaEventDestroy(h->evMid);
+    for (cudaEvent_t e : h->evPool)
+        cudaEventDestroy(e);
     if (h->stream)
         cudaStreamDestroy(h->stream);
     delete h;
@@ -795,7 +818,7 @@ rc_status rc_resize(rc_tracer* h, uint64_t width, uint64_t height)
     rc_status s;
     if ((s = dev_alloc(h, &h->dFilm, size_t(px), "allocate film")) != RC_OK ||
         (s = dev_alloc(h, &h->dCast, size_t(px), "allocate cast buffer")) != RC_OK ||
-        (s = dev_alloc(h, &h->dQueue, size_t(px), "allocate shadow queue")) != RC_OK)
+        (s = dev_alloc(h, &h->dQueue, size_t(px) * 2, "allocate shadow queue")) != RC_OK)
     {
         release_film(h);
         return s;
@@ -884,7 +907,7 @@ rc_status rc_cast_device(rc_tracer* h, const rc_ray* d_rays, int64_t n, int32_t 
         return s;
     RC_CUDA_TRY(h, launch_cast(launch_info(h), dev_scene(h), d_rays, n, any_hit, order, d_hits, h->dCtl),
                 "launch cast kernel");
-    return end_launch(h, "cast");
+    return end_launch(h, "cast", false);
 }
 
 rc_status rc_cast(rc_tracer* h, const rc_ray* rays, int64_t n, int32_t any_hit, int32_t order, rc_hit* hits)
@@ -924,7 +947,7 @@ rc_status rc_cast_with_shadow(rc_tracer* h, const rc_ray* rays, int64_t n, int32
     cudaSetDevice(h->device);
     rc_status s;
     size_t rayBytes = size_t(n) * sizeof(rc_ray);
-    size_t outBytes = size_t(n) * (sizeof(rc_cast_pixel) + sizeof(int));
+    size_t outBytes = size_t(n) * (sizeof(rc_cast_pixel) + 2 * sizeof(int));
     if ((s = ensure_bytes(h, &h->dTmpA, &h->capTmpA, rayBytes, "allocate ray buffer")) != RC_OK ||
         (s = ensure_bytes(h, &h->dTmpB, &h->capTmpB, outBytes, "allocate output buffer")) != RC_OK)
         return s;
@@ -1005,9 +1028,9 @@ rc_status raycast_into(rc_tracer* h, const rc_ray* dRays, uint64_t pixelStart, u
         return s;
     RC_CUDA_TRY(h,
                 launch_raycast(launch_info(h), dev_scene(h), cam, dRays, pixelStart, int64_t(count), width, order,
-                               castShadow, L, h->general.ray_start_offset, dOut, dQueue, h->dCtl),
+                               castShadow, L, h->general.ray_start_offset, dOut, dQueue, h->dCtl, h->evMid),
                 "launch ray-cast kernels");
-    return end_launch(h, "ray cast");
+    return end_launch(h, "ray cast", true);
 }
 
 rc_status render_raycast(rc_tracer* h, uint64_t pixelStart, uint64_t count, const rc_ray* dRays)

@@ -20,6 +20,13 @@
 // Any-hit (shadow rays: isShadowRay + fastOcclusion) always uses the
 // reference order and stops at the first triangle found; triangles whose
 // material is nonShadowing are skipped (Triangle.cpp:55).
+//
+// `skip` names the triangle a secondary ray leaves from (-1 for none). Its
+// origin is the hit point moved by rayStartOffset along the ray direction, so
+// in exact arithmetic the ray travels away from that triangle's plane and
+// cannot hit it; in float32 the hit point's rounding (about 1e-6 at
+// coordinates of 10) can exceed the 1e-5 offset at grazing angles and report
+// the ray's own triangle. Skipping it gives the float64 reference's answer.
 #pragma once
 
 #include "rc_math.cuh"
@@ -61,7 +68,8 @@ __device__ __forceinline__ void load_node(const DevNode* __restrict__ nodes, int
 // the caller (slot -1, t = FLT_MAX for a fresh query). `err` is set to 1 on
 // a stack overflow (the ray is then abandoned; the host reports it).
 template <bool ANY_HIT, int ORDER, bool COUNT>
-__device__ __forceinline__ bool traverse(const DevScene& sc, const RayF& ray, HitF& hit, TravCount& cnt, int& err)
+__device__ __forceinline__ bool traverse(const DevScene& sc, const RayF& ray, HitF& hit, TravCount& cnt, int& err,
+                                         int skip = -1)
 {
     int stack[kMaxStack];
     float sdist[ORDER == ORDER_NEAREST && !ANY_HIT ? kMaxStack : 1];
@@ -127,6 +135,8 @@ __device__ __forceinline__ bool traverse(const DevScene& sc, const RayF& ray, Hi
             for (int i = 0; i < count; ++i)
             {
                 int slot = start + i;
+                if (slot == skip)
+                    continue;
                 const float4* tp = reinterpret_cast<const float4*>(sc.tris + slot);
                 float4 ta = __ldg(tp + 0);
                 float4 tb = __ldg(tp + 1);

@@ -125,7 +125,7 @@ def room_scene(seed: int = 1, clutter: int = 2000, width: int = 320, height: int
             d = np.array([r * math.cos(phi), r * math.sin(phi), z])
             s = rng.uniform(0.05, 0.2)
             verts.append(c + d * s)
-        albedo = tuple(rng.uniform(0.2, 0.8) for _ in range(3))
+        albedo = tuple(float(np.float32(rng.uniform(0.2, 0.8))) for _ in range(3))
         mats.append(Material(diffuse=albedo))
         tris.append(np.concatenate(verts))
         midx.append(len(mats) - 1)

@@ -324,7 +324,11 @@ class CudaTracer:
     def stats(self) -> dict:
         s = N.rc_stats()
         self._check(self._lib.rc_get_stats(self._h, C.byref(s)), "stats")
-        return {k: getattr(s, k) for k, _ in N.rc_stats._fields_}
+        out = {}
+        for k, _ in N.rc_stats._fields_:
+            v = getattr(s, k)
+            out[k] = list(v) if isinstance(v, C.Array) else v
+        return out
 
     def sync(self) -> None:
         self._check(self._lib.rc_sync(self._h), "sync")
@@ -352,7 +356,9 @@ class _GpuTracerAdapter:
             t.initializeBuffers(scene)
         if (t.imageWidth, t.imageHeight) != (state.filmWidth, state.filmHeight):
             t.initializeImageBuffers(state.filmWidth, state.filmHeight)
-        g = general_record(scene)
+        # a new random stream per call, like the CPU tracer's continuing generators
+        self.runs = getattr(self, "runs", 0) + 1
+        g = general_record(scene, seed=self.runs)
         g.tracer_type = int(self.type)
         t.set_general(g)
         t.clear()

@@ -31,6 +31,7 @@ def _frame(sc, order):
 @pytest.mark.parametrize("which", ["room", "heightfield"])
 def test_raycast_frame_bit_exact(which, order):
     sc = small_room() if which == "room" else small_heightfield()
+    sc.settings["tracer"] = "ray"
     if which == "room":
         sc.light_direction = (-0.3, -1.0, -0.2)
     gpu, cam = _frame(sc, order)
