@@ -608,6 +608,12 @@ void tonemap_reinhard64(int64_t pixels, const float* linear, double key, double 
         double sL = scaleL * L;
         double mapped = (sL * (1.0 + (sL * maxL2Inv))) / (1.0 + sL);
         double cs = mapped / L;
+        // A black pixel gives 0/0. The reference's build (x86-64) produces the
+        // default NaN with the sign bit set, which MathUtils::fastPow maps to
+        // a tiny value (0 in float) when clamping is off; other hosts' default
+        // NaN is positive and would map to +inf. Use the reference's NaN.
+        if (std::isnan(cs))
+            cs = -std::numeric_limits<double>::quiet_NaN();
         for (int k = 0; k < 3; ++k)
         {
             double x = c[k] * cs;

@@ -36,6 +36,10 @@ namespace
 
 constexpr int kBlock = 128;
 
+#ifndef RC_TRACE_MIN_BLOCKS
+#define RC_TRACE_MIN_BLOCKS 10
+#endif
+
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
 
 __device__ __forceinline__ unsigned warp_fetch(unsigned* head, unsigned amount)
@@ -128,7 +132,7 @@ __global__ void __launch_bounds__(256) k_generate(PathParams p)
 }
 
 template <int ORDER, bool COUNT>
-__global__ void __launch_bounds__(kBlock) k_extend(PathParams p, int segment)
+__global__ void __launch_bounds__(kBlock, RC_TRACE_MIN_BLOCKS) k_extend(PathParams p, int segment)
 {
     const unsigned total = *reinterpret_cast<volatile unsigned*>(&p.counts[segment * 4 + 0]);
     const int* __restrict__ queue = (segment & 1) ? p.qb : p.qa;

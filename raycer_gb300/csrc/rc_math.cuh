@@ -58,6 +58,7 @@ struct RayF
     V3 inv;  // 1 / d per component (Ray::precalculate, Ray.cpp:10)
     float tmin;
     float tmax;
+    bool finite;  // all of inv finite: no slab product can be NaN
 };
 
 __device__ __forceinline__ RayF make_ray(V3 o, V3 d, float tmin, float tmax)
@@ -68,6 +69,7 @@ __device__ __forceinline__ RayF make_ray(V3 o, V3 d, float tmin, float tmax)
     r.inv = v3(__frcp_rn(d.x), __frcp_rn(d.y), __frcp_rn(d.z));
     r.tmin = tmin;
     r.tmax = tmax;
+    r.finite = isfinite(r.inv.x) && isfinite(r.inv.y) && isfinite(r.inv.z);
     return r;
 }
 
@@ -89,6 +91,27 @@ __device__ __forceinline__ bool slab(const RayF& r, float lox, float hix, float 
     tmin = smax(tmin, smin(tz0, tz1));
     tmax = smin(tmax, smax(tz0, tz1));
     entry = smax(tmin, 0.0f);
+    return !(tmax < entry);
+}
+
+// The same test for a ray whose inverse direction is finite. Then every
+// product (lo - o) * inv is a number (finite or an overflowed infinity, never
+// NaN), and for non-NaN operands fminf/fmaxf pick the same value as the
+// compare-and-select of std::min/std::max up to the sign of a zero, which no
+// comparison below can see. So the decision and the entry distance's order
+// relations are identical, at one FMNMX instruction per min/max.
+__device__ __forceinline__ bool slab_finite(const RayF& r, float lox, float hix, float loy, float hiy, float loz,
+                                            float hiz, float& entry)
+{
+    float tx0 = __fmul_rn(__fsub_rn(lox, r.o.x), r.inv.x);
+    float tx1 = __fmul_rn(__fsub_rn(hix, r.o.x), r.inv.x);
+    float ty0 = __fmul_rn(__fsub_rn(loy, r.o.y), r.inv.y);
+    float ty1 = __fmul_rn(__fsub_rn(hiy, r.o.y), r.inv.y);
+    float tz0 = __fmul_rn(__fsub_rn(loz, r.o.z), r.inv.z);
+    float tz1 = __fmul_rn(__fsub_rn(hiz, r.o.z), r.inv.z);
+    float tmin = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fminf(tz0, tz1));
+    float tmax = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fmaxf(tz0, tz1));
+    entry = fmaxf(tmin, 0.0f);
     return !(tmax < entry);
 }
 

@@ -19,6 +19,15 @@ namespace
 
 constexpr int kBlock = 128;
 
+// Minimum resident blocks per SM the ray kernels are compiled for (register
+// budget: 10 blocks x 128 threads -> at most 48 registers, no spills).
+#ifndef RC_TRACE_MIN_BLOCKS
+#define RC_TRACE_MIN_BLOCKS 10
+#endif
+#ifndef RC_TRACE_TILES
+#define RC_TRACE_TILES 1
+#endif
+
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
 
 __device__ __forceinline__ unsigned warp_fetch(unsigned* head, unsigned amount)
@@ -57,7 +66,7 @@ __device__ __forceinline__ int caller_index(const DevScene& sc, int slot)
 }
 
 template <bool ANY, int ORDER, bool COUNT>
-__global__ void __launch_bounds__(kBlock) k_cast(DevScene sc, const rc_ray* __restrict__ rays, int n,
+__global__ void __launch_bounds__(kBlock, RC_TRACE_MIN_BLOCKS) k_cast(DevScene sc, const rc_ray* __restrict__ rays, int n,
                                                  rc_hit* __restrict__ hits, DevControl* ctl)
 {
     TravCount cnt{ 0, 0 };
@@ -106,24 +115,38 @@ __device__ __forceinline__ RayF primary_ray(const DevCamera& cam, const rc_ray* 
 }
 
 // Stage 1 of the RAY frame: closest hit of every pixel's primary ray.
+// Whole frames from the camera (tilesX > 0) are walked in 8x4-pixel tiles, one
+// tile per warp fetch, so a warp's rays are spatially coherent; pixel ranges
+// and caller rays are walked in order.
 template <int ORDER, bool COUNT>
-__global__ void __launch_bounds__(kBlock) k_raycast_primary(DevScene sc, DevCamera cam, const rc_ray* __restrict__ rays,
+__global__ void __launch_bounds__(kBlock, RC_TRACE_MIN_BLOCKS) k_raycast_primary(DevScene sc, DevCamera cam, const rc_ray* __restrict__ rays,
                                                             uint64_t pixelStart, int64_t count, int64_t width,
-                                                            int castShadow, rc_cast_pixel* __restrict__ out,
-                                                            int* __restrict__ queue, DevControl* ctl)
+                                                            int64_t height, int64_t tilesX, int castShadow,
+                                                            rc_cast_pixel* __restrict__ out, int* __restrict__ queue,
+                                                            DevControl* ctl)
 {
     TravCount cnt{ 0, 0 };
     int err = 0;
     unsigned long long done = 0;
+    const int64_t items = tilesX > 0 ? tilesX * ((height + 3) / 4) * 32 : count;
     while (true)
     {
         unsigned base = warp_fetch(&ctl->head[0], 32u);
-        if (int64_t(base) >= count)
+        if (int64_t(base) >= items)
             break;
         int64_t i = int64_t(base) + lane_id();
+        bool valid = i < items;
+        if (tilesX > 0 && valid)
+        {
+            int64_t tile = i >> 5;
+            int64_t px = (tile % tilesX) * 8 + (i & 7);
+            int64_t py = (tile / tilesX) * 4 + ((i >> 3) & 3);
+            valid = px < width && py < height;
+            i = py * width + px;
+        }
         bool hitAny = false;
         int hitSlot = -1;
-        if (i < count)
+        if (valid)
         {
             RayF ray = primary_ray(cam, rays, pixelStart + uint64_t(i), i, width);
             HitF h{ -1, FLT_MAX, 0.0f, 0.0f };
@@ -159,7 +182,7 @@ __global__ void __launch_bounds__(kBlock) k_raycast_primary(DevScene sc, DevCame
 // lighting.cl:28-48): origin = hit position + dirToLight * rayStartOffset;
 // the primary hit's own triangle is skipped (see traverse.cuh).
 template <bool COUNT>
-__global__ void __launch_bounds__(kBlock) k_raycast_shadow(DevScene sc, DevCamera cam, const rc_ray* __restrict__ rays,
+__global__ void __launch_bounds__(kBlock, RC_TRACE_MIN_BLOCKS) k_raycast_shadow(DevScene sc, DevCamera cam, const rc_ray* __restrict__ rays,
                                                            uint64_t pixelStart, int64_t width, float3 L,
                                                            float rayStartOffset, rc_cast_pixel* __restrict__ out,
                                                            const int* __restrict__ queue, DevControl* ctl)
@@ -227,7 +250,13 @@ cudaError_t raycast_t(const LaunchInfo& li, const DevScene& sc, const DevCamera&
         gp = persistent_blocks(kp, li.numSMs);
     if (gs == 0)
         gs = persistent_blocks(ks, li.numSMs);
-    kp<<<gp, kBlock, 0, li.stream>>>(sc, cam, rays, pixelStart, count, width, castShadow, out, queue, ctl);
+    // Tile a whole camera frame (pixel range = the full image).
+    int64_t height = width > 0 ? count / width : 0;
+    int64_t tilesX = (RC_TRACE_TILES && !rays && pixelStart == 0 && width > 0 && height * width == count)
+                         ? (width + 7) / 8
+                         : 0;
+    kp<<<gp, kBlock, 0, li.stream>>>(sc, cam, rays, pixelStart, count, width, height, tilesX, castShadow, out, queue,
+                                     ctl);
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess && between)
         e = cudaEventRecord(between, li.stream);

@@ -87,8 +87,21 @@ __device__ __forceinline__ bool traverse(const DevScene& sc, const RayF& ray, Hi
             if (COUNT)
                 cnt.nodes++;
             float e0, e1;
-            bool h0 = slab(ray, a.x, a.y, a.z, a.w, c.x, c.y, e0);
-            bool h1 = slab(ray, b.x, b.y, b.z, b.w, c.z, c.w, e1);
+            bool h0, h1;
+#ifndef RC_EXACT_SLAB_ONLY
+            if (ray.finite)
+#else
+            if (false)
+#endif
+            {
+                h0 = slab_finite(ray, a.x, a.y, a.z, a.w, c.x, c.y, e0);
+                h1 = slab_finite(ray, b.x, b.y, b.z, b.w, c.z, c.w, e1);
+            }
+            else
+            {
+                h0 = slab(ray, a.x, a.y, a.z, a.w, c.x, c.y, e0);
+                h1 = slab(ray, b.x, b.y, b.z, b.w, c.z, c.w, e1);
+            }
             if (ORDER == ORDER_NEAREST && !ANY_HIT)
             {
                 h0 = h0 && !(e0 > hit.t);
