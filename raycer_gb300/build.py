@@ -5,7 +5,7 @@
 * ``oracle/lib/liboracle.so`` — the CPU oracle (test infrastructure; only the
   tests and bench.py's CPU baseline load it).
 * ``oracle/_ref/*.so`` — the reference's own hot path compiled from its
-  sources, only where those sources exist (not on the GPU host).
+  sources, only where those sources are present.
 
 Translation units are compiled in parallel; objects go to ``_build/``.
 """
