@@ -48,8 +48,8 @@ WORKLOAD = "heightfield ray cast 1920x1080: primary closest hit + directional sh
 def parse_args():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
-    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--order", choices=["nearest", "reference"], default="nearest")
     return ap.parse_args()
@@ -60,7 +60,11 @@ def dist_env():
 
 
 class ClockSampler:
-    """nvidia-smi clock / throttle samples every 200 ms while running."""
+    """nvidia-smi clock / throttle samples every 20 ms from before the warm-up
+    to the end of the timed region. The summary uses the samples taken inside
+    the timed region; when that region is shorter than a few sampling periods
+    it widens the window backwards into the warm-up frames just before it (the
+    same kernels at the same load) and says so."""
 
     FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
               "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
@@ -69,14 +73,15 @@ class ClockSampler:
     def __init__(self, device: int):
         self.device = device
         self.proc = None
-        self.lines = []
+        self.samples = []   # (host time, line)
         self.thread = None
+        self.t0 = self.t1 = None
 
-    def __enter__(self):
+    def start(self):
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "20"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
         except (OSError, FileNotFoundError):
@@ -85,9 +90,16 @@ class ClockSampler:
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.samples.append((time.perf_counter(), line.strip()))
 
-    def __exit__(self, *exc):
+    def mark_start(self):
+        self.t0 = time.perf_counter()
+
+    def mark_end(self):
+        self.t1 = time.perf_counter()
+        time.sleep(0.05)
+
+    def stop(self):
         if self.proc:
             self.proc.terminate()
             try:
@@ -96,23 +108,31 @@ class ClockSampler:
                 self.proc.kill()
 
     def summary(self):
-        sm, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        parsed = []
+        for ts, ln in self.samples:
             parts = [p.strip() for p in ln.split(",")]
             if len(parts) < 7:
                 continue
             try:
-                sm.append(float(parts[0]))
-                mx = float(parts[1])
+                parsed.append((ts, float(parts[0]), float(parts[1]), parts[3:7]))
             except ValueError:
                 continue
-            for name, val in zip(names, parts[3:7]):
+        if not parsed or self.t0 is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        window = "timed region"
+        inside = [p for p in parsed if self.t0 <= p[0] <= self.t1]
+        if len(inside) < 3:
+            before = [p for p in parsed if p[0] <= self.t1]
+            inside = before[-5:]
+            window = "timed region + the warm-up frames before it (region shorter than the sampling period)"
+        reasons = set()
+        for _, _, _, flags in inside:
+            for name, val in zip(names, flags):
                 if val.lower() == "active":
                     reasons.add(name)
-        if not sm:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+        return {"sm_mhz": statistics.median(p[1] for p in inside), "sm_max_mhz": inside[-1][2],
+                "reasons": sorted(reasons), "samples": len(inside), "window": window}
 
 
 def measured_peaks():
@@ -259,24 +279,28 @@ def run_ours(args, rank, local_rank, world):
         with torch.cuda.stream(stream):
             flush.zero_()
 
+    clocks = ClockSampler(local_rank).start()
+    time.sleep(0.3)   # the sampler's first reading
     for _ in range(args.warmup):
         flush_l2()
         tracer.run(state)
 
     frame_ms, prim_ms, shadow_ms, rays = [], [], [], []
     barrier()
-    with ClockSampler(local_rank) as clocks:
-        t_wall0 = time.perf_counter()
-        for _ in range(args.steps):
-            flush_l2()
-            tracer.run(state)
-            s = tracer.stats()
-            frame_ms.append(s["last_ms"])
-            prim_ms.append(s["stage_ms"][0])
-            shadow_ms.append(s["stage_ms"][1])
-            rays.append(s["rays_traced"])
-        barrier()
-        t_wall = time.perf_counter() - t_wall0
+    clocks.mark_start()
+    t_wall0 = time.perf_counter()
+    for _ in range(args.steps):
+        flush_l2()
+        tracer.run(state)
+        s = tracer.stats()
+        frame_ms.append(s["last_ms"])
+        prim_ms.append(s["stage_ms"][0])
+        shadow_ms.append(s["stage_ms"][1])
+        rays.append(s["rays_traced"])
+    barrier()
+    t_wall = time.perf_counter() - t_wall0
+    clocks.mark_end()
+    clocks.stop()
     dev_sec = sum(frame_ms) / 1e3
     total_rays = sum(rays)
 
