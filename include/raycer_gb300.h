@@ -320,6 +320,21 @@ rc_status rc_cast_device(rc_tracer* h, const rc_ray* d_rays, int64_t n, int32_t 
  * host buffers, copies included). Uses the first directional light. */
 rc_status rc_cast_with_shadow(rc_tracer* h, const rc_ray* rays, int64_t n, int32_t order, rc_cast_pixel* out);
 
+/* Allocation-free form of rc_cast_with_shadow on device buffers. No
+ * counterpart in the reference: it is for callers that cannot allocate device
+ * memory when they trace — an application whose GPU memory belongs to its own
+ * pool allocator, or a per-frame callback that cannot take cudaMalloc's
+ * implicit synchronisation. d_rays / d_out: n device records (16-byte
+ * aligned), on the handle's stream; blocks until done. The work counters and
+ * the shadow-ray queue live in a static device array of the library (8 MiB per
+ * GPU, held while the process runs): at most 1,048,576 rays per call, larger n
+ * returns RC_INVALID_ARG. Every call on every handle shares that array, so
+ * calls that overlap on the GPU race. The first call on a device looks up the
+ * array's address (once per device); make that first call before any stream
+ * capture begins. */
+rc_status rc_cast_with_shadow_device_noalloc(rc_tracer* h, const rc_ray* d_rays, int64_t n, int32_t order,
+                                             rc_cast_pixel* d_out);
+
 /* ------------------------------------------------------------------------ */
 /* Options, statistics, synchronisation.                                     */
 

@@ -127,6 +127,7 @@ PROTOTYPES = {
     "rc_cast": (i32, [P, P, i64, i32, i32, P]),
     "rc_cast_device": (i32, [P, P, i64, i32, i32, P]),
     "rc_cast_with_shadow": (i32, [P, P, i64, i32, P]),
+    "rc_cast_with_shadow_device_noalloc": (i32, [P, P, i64, i32, P]),
     "rc_set_traversal_order": (i32, [P, i32]),
     "rc_set_counting": (i32, [P, i32]),
     "rc_get_stats": (i32, [P, C.POINTER(rc_stats)]),
