@@ -336,6 +336,65 @@ rc_status rc_cast_with_shadow_device_noalloc(rc_tracer* h, const rc_ray* d_rays,
                                              rc_cast_pixel* d_out);
 
 /* ------------------------------------------------------------------------ */
+/* Batched path tracing: many independent scenes of uneven size rendered as
+ * one CUDA-graph launch. No counterpart in the reference (its Tracer::run
+ * renders one scene per call); each scene's film equals what a handle of its
+ * own would render for the same records (same kernels, same random streams). */
+
+typedef struct rc_batch rc_batch;
+
+typedef struct rc_batch_stats
+{
+    uint64_t rays_traced;    /* BVH queries of the last rc_batch_render              */
+    uint64_t paths;          /* paths started (pixels x samples over all scenes)     */
+    double last_ms;          /* device time of the last rc_batch_render              */
+    int32_t passes;          /* passes in the graph                                  */
+    int32_t scenes;
+    int32_t graph_nodes;     /* nodes of the captured graph                          */
+    int32_t reserved;
+} rc_batch_stats;
+
+/* Per scene-size bucket (by triangle count: < 16k, < 128k, < 1M, >= 1M) the
+ * autotuner's choice: path slots per pass (queue size) and threads per block
+ * of the extend / shade kernels. */
+typedef struct rc_batch_tuning
+{
+    uint32_t bucket_min_triangles[4];
+    uint32_t slots[4];
+    int32_t extend_block[4];
+    int32_t shade_block[4];
+    double measured_paths_per_ms[4];  /* of the chosen configuration (0 = not tuned) */
+} rc_batch_tuning;
+
+rc_status rc_batch_create(rc_batch** out, int device);
+void rc_batch_destroy(rc_batch* b);
+const char* rc_batch_last_error(const rc_batch* b);
+
+/* Adds one scene (triangles and materials as rc_upload_scene; the SAH BVH is
+ * built on the host), its camera, its PATH settings and its film size.
+ * index receives the scene's index. Invalidates a captured graph. */
+rc_status rc_batch_add_scene(rc_batch* b, const double* vertices, const uint32_t* material_index, int64_t n,
+                             const rc_material* materials, int32_t material_count, uint32_t max_leaf_size,
+                             const rc_camera* camera, const rc_general* general, uint64_t width, uint64_t height,
+                             int32_t* index);
+
+/* Times candidate configurations (pass sizes 1M/2M/4M slots x 64/128/256
+ * threads per block) on each bucket's first paths and keeps the fastest per
+ * bucket; spends at most about budget_ms of device time. Clears the films. */
+rc_status rc_batch_autotune(rc_batch* b, double budget_ms);
+rc_status rc_batch_get_tuning(const rc_batch* b, rc_batch_tuning* out);
+
+/* One frame of every scene (adds filter-weighted samples to each film) as
+ * one graph launch; the graph is captured on the first call after a change.
+ * scene_done_ms (optional, `scenes` entries): device time from the launch's
+ * start until each scene's last pass finished. Blocks until done. */
+rc_status rc_batch_render(rc_batch* b, double* scene_done_ms);
+rc_status rc_batch_clear(rc_batch* b);
+rc_status rc_batch_read_film(rc_batch* b, int32_t index, float* out_rgbw);
+rc_status rc_batch_resolve(rc_batch* b, int32_t index, const rc_tonemapper* tonemapper, float* out_rgba);
+rc_status rc_batch_get_stats(const rc_batch* b, rc_batch_stats* out);
+
+/* ------------------------------------------------------------------------ */
 /* Options, statistics, synchronisation.                                     */
 
 /* Closest-hit traversal order for renders (rc_traversal_order). */

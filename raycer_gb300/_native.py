@@ -94,6 +94,16 @@ class rc_stats(C.Structure):
                 ("stage_tris", C.c_uint64 * 2), ("stage_ms", C.c_double * 2)]
 
 
+class rc_batch_stats(C.Structure):
+    _fields_ = [("rays_traced", C.c_uint64), ("paths", C.c_uint64), ("last_ms", C.c_double), ("passes", C.c_int32),
+                ("scenes", C.c_int32), ("graph_nodes", C.c_int32), ("reserved", C.c_int32)]
+
+
+class rc_batch_tuning(C.Structure):
+    _fields_ = [("bucket_min_triangles", C.c_uint32 * 4), ("slots", C.c_uint32 * 4), ("extend_block", C.c_int32 * 4),
+                ("shade_block", C.c_int32 * 4), ("measured_paths_per_ms", C.c_double * 4)]
+
+
 P = C.c_void_p
 i32, i64, u32, u64 = C.c_int32, C.c_int64, C.c_uint32, C.c_uint64
 
@@ -128,6 +138,18 @@ PROTOTYPES = {
     "rc_cast_device": (i32, [P, P, i64, i32, i32, P]),
     "rc_cast_with_shadow": (i32, [P, P, i64, i32, P]),
     "rc_cast_with_shadow_device_noalloc": (i32, [P, P, i64, i32, P]),
+    "rc_batch_create": (i32, [C.POINTER(P), C.c_int]),
+    "rc_batch_destroy": (None, [P]),
+    "rc_batch_last_error": (C.c_char_p, [P]),
+    "rc_batch_add_scene": (i32, [P, P, P, i64, P, i32, u32, C.POINTER(rc_camera), C.POINTER(rc_general), u64, u64,
+                                 C.POINTER(i32)]),
+    "rc_batch_autotune": (i32, [P, C.c_double]),
+    "rc_batch_get_tuning": (i32, [P, C.POINTER(rc_batch_tuning)]),
+    "rc_batch_render": (i32, [P, P]),
+    "rc_batch_clear": (i32, [P]),
+    "rc_batch_read_film": (i32, [P, i32, P]),
+    "rc_batch_resolve": (i32, [P, i32, C.POINTER(rc_tonemapper), P]),
+    "rc_batch_get_stats": (i32, [P, C.POINTER(rc_batch_stats)]),
     "rc_set_traversal_order": (i32, [P, i32]),
     "rc_set_counting": (i32, [P, i32]),
     "rc_get_stats": (i32, [P, C.POINTER(rc_stats)]),

@@ -63,6 +63,8 @@ struct rc_tracer
     uint64_t pathSlots = 0;
     unsigned* dCounts = nullptr;
     size_t capCounts = 0;
+    void* dTables = nullptr;   // scene record + per-pass chunk records
+    size_t capTables = 0;
 
     // Tone-mapping scratch (partial sums) and output staging.
     void* dTone = nullptr;
@@ -89,5 +91,12 @@ rc_status raycast_into(rc_tracer* h, const rc_ray* dRays, uint64_t pixelStart, u
 rc_status render_raycast(rc_tracer* h, uint64_t pixelStart, uint64_t count, const rc_ray* dRays);
 rc_status render_path(rc_tracer* h, uint64_t pixelStart, uint64_t count, const volatile int32_t* cancel);
 void release_render_buffers(rc_tracer* h);
+
+struct PathScene;
+struct PassParams;
+// The pass kernels' record of a handle's scene, camera, PATH settings and film.
+PathScene path_scene(const rc_tracer* h, uint64_t pixelStart);
+// Slot arrays of a path-state buffer of `slots` slots (pathtrace.h layout).
+PassParams pass_params(void* state, uint64_t slots, unsigned* counts, DevControl* ctl);
 
 }  // namespace rcx

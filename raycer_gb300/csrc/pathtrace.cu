@@ -1,10 +1,12 @@
 // Wavefront path tracer (PathTracer, src/Raytracing/Tracers/PathTracer.cpp:13-75;
-// pathtrace.cl:1-80) for one pass of paths.
+// pathtrace.cl:1-80): the kernels of one pass (see pathtrace.h for passes,
+// chunks and the scene table).
 //
-// A pass holds whole pixels: slot s belongs to pixel s / spp of the pass and
-// to sample (s % spp) of it, where spp = n*n camera samples (Tracer.cpp:
-// 115-144, CMJ + box filter) x pathSampleCount paths per camera sample
-// (PathTracer.cpp:19). Path state lives in SoA arrays indexed by slot:
+// Slot s of a pass belongs to chunk c = chunkOf[s], pixel (s - slotBegin) / spp
+// of the chunk and sample (s - slotBegin) % spp of that pixel, where
+// spp = n*n camera samples (Tracer.cpp:115-144, CMJ + box filter) x
+// pathSampleCount paths per camera sample (PathTracer.cpp:19). Path state
+// lives in SoA arrays indexed by slot:
 //   o, d       ray (float4 each); o.w = the triangle the ray leaves from
 //              (skipped by its closest-hit query, see traverse.cuh)
 //   thr        path throughput (rgb)
@@ -13,15 +15,15 @@
 // Stages (one launch each, per segment):
 //   generate   camera rays for every slot; queue 0 = all slots
 //   extend     closest hit for every queued slot              (persistent)
-//   shade      miss -> 0; emissive -> res = thr * emittance; last segment
-//              -> 0; else cosine bounce, thr *= 2*rho*|w.n| (PathTracer.cpp:
-//              58-72), optional Russian roulette, and the slot is appended
-//              to the next queue (warp-ballot compaction)      (persistent)
+//   shade      miss -> 0; emissive -> res = thr * emittance; the scene's last
+//              segment -> 0; else optional Russian roulette, cosine bounce,
+//              thr *= 2*rho*|w.n| (PathTracer.cpp:58-72), and the slot is
+//              appended to the next queue (warp-ballot compaction) (persistent)
 //   accumulate per pixel, in sample order: c_j = (sum_k L_jk) / P,
 //              film.rgb += w_j * c_j, film.w += w_j (Film::addSample,
 //              Film.cpp:54-59). One thread owns one pixel: deterministic.
-// Queue counts live on the device, so the host launches a fixed sequence
-// without reading them back.
+// Queue counts live on the device, so a pass is a fixed launch sequence the
+// host never waits on (and can be captured in a CUDA graph).
 
 #include <cfloat>
 
@@ -33,8 +35,6 @@ namespace rcx
 {
 namespace
 {
-
-constexpr int kBlock = 128;
 
 #ifndef RC_TRACE_MIN_BLOCKS
 #define RC_TRACE_MIN_BLOCKS 10
@@ -50,22 +50,50 @@ __device__ __forceinline__ unsigned warp_fetch(unsigned* head, unsigned amount)
     return __shfl_sync(0xffffffffu, base, 0);
 }
 
+// Largest chunk whose first slot (pixel) is <= s.
+__device__ __forceinline__ int chunk_of_slot(const PassParams& p, uint32_t s)
+{
+    int lo = 0, hi = p.numChunks - 1;
+    while (lo < hi)
+    {
+        int mid = (lo + hi + 1) >> 1;
+        if (p.chunks[mid].slotBegin <= s)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ int chunk_of_pixel(const PassParams& p, uint32_t pix)
+{
+    int lo = 0, hi = p.numChunks - 1;
+    while (lo < hi)
+    {
+        int mid = (lo + hi + 1) >> 1;
+        if (p.chunks[mid].pixelPassBegin <= pix)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
+
 struct SlotInfo
 {
     uint64_t pixelGlobal;
-    uint64_t pixelLocal;
     uint32_t sample;  // j * P + k
     uint32_t j;
 };
 
-__device__ __forceinline__ SlotInfo slot_info(const PathParams& p, uint32_t s)
+__device__ __forceinline__ SlotInfo slot_info(const PathChunk& ch, const PathScene& sc, uint32_t s)
 {
     SlotInfo si;
-    uint32_t pix = s / uint32_t(p.spp);
-    si.sample = s - pix * uint32_t(p.spp);
-    si.j = si.sample / uint32_t(p.P);
-    si.pixelLocal = p.passPixel + pix;
-    si.pixelGlobal = p.pixelStart + si.pixelLocal;
+    uint32_t rel = s - ch.slotBegin;
+    uint32_t pix = rel / uint32_t(sc.spp);
+    si.sample = rel - pix * uint32_t(sc.spp);
+    si.j = si.sample / uint32_t(sc.P);
+    si.pixelGlobal = sc.pixelStart + ch.pixelLocalBegin + pix;
     return si;
 }
 
@@ -75,38 +103,42 @@ __device__ __forceinline__ float box_weight(float x, float r, float w)
     return (x >= -r && x < r) ? w : 0.0f;
 }
 
-__global__ void __launch_bounds__(256) k_generate(PathParams p)
+__global__ void __launch_bounds__(256) k_generate(PassParams p)
 {
     uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s == 0)
         p.counts[0] = uint32_t(p.nslots);
     if (s >= uint32_t(p.nslots))
         return;
-    SlotInfo si = slot_info(p, s);
-    float px = float(si.pixelGlobal % uint64_t(p.width));
-    float py = float(si.pixelGlobal / uint64_t(p.width));
+    const int c = chunk_of_slot(p, s);
+    p.chunkOf[s] = c;
+    const PathChunk ch = p.chunks[c];
+    const PathScene& sc = p.scenes[ch.scene];
+    SlotInfo si = slot_info(ch, sc, s);
+    float px = float(si.pixelGlobal % uint64_t(sc.width));
+    float py = float(si.pixelGlobal / uint64_t(sc.width));
     float w = 1.0f;
-    if (p.n > 1)
+    if (sc.n > 1)
     {
-        uint32_t gx = si.j % uint32_t(p.n);
-        uint32_t gy = si.j / uint32_t(p.n);
-        uint32_t jkey = stream_key(p.seed, p.frame, si.pixelGlobal, 0x80000000u | si.j);
+        uint32_t gx = si.j % uint32_t(sc.n);
+        uint32_t gy = si.j / uint32_t(sc.n);
+        uint32_t jkey = stream_key(sc.seed, sc.frame, si.pixelGlobal, 0x80000000u | si.j);
         float jx = stream_float(jkey, kCounterJitter + 0);
         float jy = stream_float(jkey, kCounterJitter + 1);
         float sx, sy;
-        if (p.samplerType == RC_SAMPLER_CMJ)
+        if (sc.samplerType == RC_SAMPLER_CMJ)
         {
             // CMJSampler::getSample2D (CMJSampler.cpp:61-76), permutation per pixel.
-            uint32_t pkey = stream_key(p.seed, p.frame, si.pixelGlobal, 0xffffffffu);
+            uint32_t pkey = stream_key(sc.seed, sc.frame, si.pixelGlobal, 0xffffffffu);
             uint64_t perm = (uint64_t(stream_u32(pkey, 1)) << 32) | stream_u32(pkey, 2);
-            uint64_t n = uint64_t(p.n);
+            uint64_t n = uint64_t(sc.n);
             uint64_t sxp = cmj_permute(gx, n, perm * 0x68bc21ebull);
             uint64_t syp = cmj_permute(gy, n, perm * 0x02e5be93ull);
-            float fn = float(p.n);
+            float fn = float(sc.n);
             sx = __fdiv_rn(__fadd_rn(float(gx), __fdiv_rn(__fadd_rn(float(syp), jx), fn)), fn);
             sy = __fdiv_rn(__fadd_rn(float(gy), __fdiv_rn(__fadd_rn(float(sxp), jy), fn)), fn);
         }
-        else if (p.samplerType == RC_SAMPLER_RANDOM)
+        else if (sc.samplerType == RC_SAMPLER_RANDOM)
         {
             sx = jx;
             sy = jy;
@@ -117,22 +149,27 @@ __global__ void __launch_bounds__(256) k_generate(PathParams p)
             sy = 0.5f;
         }
         // sampleOffset = (sample - 0.5) * 2 * radius (Tracer.cpp:138)
-        float ox = __fmul_rn(__fmul_rn(__fsub_rn(sx, 0.5f), 2.0f), p.rx);
-        float oy = __fmul_rn(__fmul_rn(__fsub_rn(sy, 0.5f), 2.0f), p.ry);
-        w = __fmul_rn(box_weight(ox, p.rx, p.wx), box_weight(oy, p.ry, p.wy));
+        float ox = __fmul_rn(__fmul_rn(__fsub_rn(sx, 0.5f), 2.0f), sc.rx);
+        float oy = __fmul_rn(__fmul_rn(__fsub_rn(sy, 0.5f), 2.0f), sc.ry);
+        w = __fmul_rn(box_weight(ox, sc.rx, sc.wx), box_weight(oy, sc.ry, sc.wy));
         px = __fadd_rn(px, ox);
         py = __fadd_rn(py, oy);
     }
-    V3 d = camera_dir(p.cam, px, py);
-    p.o[s] = make_float4(p.cam.pos[0], p.cam.pos[1], p.cam.pos[2], __int_as_float(-1));
+    V3 d = camera_dir(sc.cam, px, py);
+    p.o[s] = make_float4(sc.cam.pos[0], sc.cam.pos[1], sc.cam.pos[2], __int_as_float(-1));
     p.d[s] = make_float4(d.x, d.y, d.z, 0.0f);
     p.thr[s] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
     p.res[s] = make_float4(0.0f, 0.0f, 0.0f, w);
     p.qa[s] = int(s);
 }
 
-template <int ORDER, bool COUNT>
-__global__ void __launch_bounds__(kBlock, RC_TRACE_MIN_BLOCKS) k_extend(PathParams p, int segment)
+__device__ __forceinline__ DevScene scene_of_slot(const PassParams& p, int s)
+{
+    return p.scenes[p.chunks[p.chunkOf[s]].scene].sc;
+}
+
+template <int ORDER, bool COUNT, int BLOCK>
+__global__ void __launch_bounds__(BLOCK, (RC_TRACE_MIN_BLOCKS * 128) / BLOCK) k_extend(PassParams p, int segment)
 {
     const unsigned total = *reinterpret_cast<volatile unsigned*>(&p.counts[segment * 4 + 0]);
     const int* __restrict__ queue = (segment & 1) ? p.qb : p.qa;
@@ -148,11 +185,12 @@ __global__ void __launch_bounds__(kBlock, RC_TRACE_MIN_BLOCKS) k_extend(PathPara
         if (q < total)
         {
             int s = queue[q];
+            const DevScene sc = scene_of_slot(p, s);
             float4 o = p.o[s];
             float4 d = p.d[s];
             RayF ray = make_ray(v3(o.x, o.y, o.z), v3(d.x, d.y, d.z), 0.0f, FLT_MAX);
             HitF h{ -1, FLT_MAX, 0.0f, 0.0f };
-            bool found = traverse<false, ORDER, COUNT>(p.sc, ray, h, cnt, err, __float_as_int(o.w));
+            bool found = traverse<false, ORDER, COUNT>(sc, ray, h, cnt, err, __float_as_int(o.w));
             p.hit[s] = make_int4(found ? h.slot : -1, __float_as_int(h.t), __float_as_int(h.u), __float_as_int(h.v));
             done++;
         }
@@ -177,13 +215,13 @@ __global__ void __launch_bounds__(kBlock, RC_TRACE_MIN_BLOCKS) k_extend(PathPara
         atomicOr(&p.ctl->error, 1);
 }
 
-__global__ void __launch_bounds__(kBlock) k_shade(PathParams p, int segment)
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK) k_shade(PassParams p, int segment)
 {
     const unsigned total = *reinterpret_cast<volatile unsigned*>(&p.counts[segment * 4 + 0]);
     const int* __restrict__ qin = (segment & 1) ? p.qb : p.qa;
     int* __restrict__ qout = (segment & 1) ? p.qa : p.qb;
     unsigned* outCount = &p.counts[(segment + 1) * 4 + 0];
-    const bool lastSegment = segment + 1 >= p.maxPathLength;
     while (true)
     {
         unsigned base = warp_fetch(&p.counts[segment * 4 + 2], 32u);
@@ -198,11 +236,14 @@ __global__ void __launch_bounds__(kBlock) k_shade(PathParams p, int segment)
             int4 h = p.hit[s];
             if (h.x >= 0)
             {
-                const float4* tp = reinterpret_cast<const float4*>(p.sc.tris + h.x);
+                const PathChunk& ch = p.chunks[p.chunkOf[s]];
+                const PathScene& scn = p.scenes[ch.scene];
+                const DevScene sc = scn.sc;
+                const float4* tp = reinterpret_cast<const float4*>(sc.tris + h.x);
                 float4 tc = __ldg(tp + 2);
                 uint32_t mi = __float_as_uint(tc.y) & kMetaMaterialMask;
-                float4 md = __ldg(&p.sc.mats[mi].diffuse);
-                float4 me = __ldg(&p.sc.mats[mi].emittance);
+                float4 md = __ldg(&sc.mats[mi].diffuse);
+                float4 me = __ldg(&sc.mats[mi].emittance);
                 uint32_t mflags = __float_as_uint(me.w);
                 float4 thr = p.thr[s];
                 if (mflags & kMatEmissive)
@@ -214,12 +255,12 @@ __global__ void __launch_bounds__(kBlock) k_shade(PathParams p, int segment)
                     r.z = __fmul_rn(thr.z, me.z);
                     p.res[s] = r;
                 }
-                else if (!lastSegment)
+                else if (segment + 1 < scn.maxPathLength)
                 {
-                    SlotInfo si = slot_info(p, uint32_t(s));
-                    uint32_t key = stream_key(p.seed, p.frame, si.pixelGlobal, si.sample);
+                    SlotInfo si = slot_info(ch, scn, uint32_t(s));
+                    uint32_t key = stream_key(scn.seed, scn.frame, si.pixelGlobal, si.sample);
                     bool alive = true;
-                    if (p.rrDepth > 0 && segment + 1 >= p.rrDepth)
+                    if (scn.rrDepth > 0 && segment + 1 >= scn.rrDepth)
                     {
                         float m = fmaxf(thr.x, fmaxf(thr.y, thr.z));
                         float qs = fminf(m, 1.0f);
@@ -235,7 +276,7 @@ __global__ void __launch_bounds__(kBlock) k_shade(PathParams p, int segment)
                     }
                     if (alive)
                     {
-                        const float4* sp = reinterpret_cast<const float4*>(p.sc.shade + h.x);
+                        const float4* sp = reinterpret_cast<const float4*>(sc.shade + h.x);
                         float4 sn = __ldg(sp + 0);
                         float4 st = __ldg(sp + 1);
                         float4 sb = __ldg(sp + 2);
@@ -249,7 +290,7 @@ __global__ void __launch_bounds__(kBlock) k_shade(PathParams p, int segment)
                         float4 d = p.d[s];
                         float t = __int_as_float(h.y);
                         V3 ip = vfma(v3(d.x, d.y, d.z), t, v3(o.x, o.y, o.z));
-                        V3 no = vfma(dir, p.rayStartOffset, ip);
+                        V3 no = vfma(dir, scn.rayStartOffset, ip);
                         float alpha = fabsf(vdot(dir, nrm));
                         // brdf = 2 * reflectance * alpha (PathTracer.cpp:70-71)
                         thr.x = __fmul_rn(thr.x, __fmul_rn(__fmul_rn(2.0f, md.x), alpha));
@@ -276,21 +317,25 @@ __global__ void __launch_bounds__(kBlock) k_shade(PathParams p, int segment)
     }
 }
 
-__global__ void __launch_bounds__(256) k_accumulate(PathParams p, int pixelsInPass)
+__global__ void __launch_bounds__(256) k_accumulate(PassParams p)
 {
     int pix = blockIdx.x * blockDim.x + threadIdx.x;
-    if (pix >= pixelsInPass)
+    if (pix >= p.npixels)
         return;
-    const int nn = p.n * p.n;
-    const float fP = float(p.P);
-    float4 f = p.film[p.passPixel + uint64_t(pix)];
-    size_t base = size_t(pix) * size_t(p.spp);
+    const PathChunk ch = p.chunks[chunk_of_pixel(p, uint32_t(pix))];
+    const PathScene& sc = p.scenes[ch.scene];
+    const uint32_t inChunk = uint32_t(pix) - ch.pixelPassBegin;
+    const int nn = sc.n * sc.n;
+    const float fP = float(sc.P);
+    float4* fp = sc.film + ch.pixelLocalBegin + inChunk;
+    float4 f = *fp;
+    size_t base = size_t(ch.slotBegin) + size_t(inChunk) * size_t(sc.spp);
     for (int j = 0; j < nn; ++j)
     {
         float sr = 0.0f, sg = 0.0f, sb = 0.0f, w = 0.0f;
-        for (int k = 0; k < p.P; ++k)
+        for (int k = 0; k < sc.P; ++k)
         {
-            float4 r = p.res[base + size_t(j) * size_t(p.P) + size_t(k)];
+            float4 r = p.res[base + size_t(j) * size_t(sc.P) + size_t(k)];
             sr = __fadd_rn(sr, r.x);
             sg = __fadd_rn(sg, r.y);
             sb = __fadd_rn(sb, r.z);
@@ -303,60 +348,86 @@ __global__ void __launch_bounds__(256) k_accumulate(PathParams p, int pixelsInPa
         f.z = __fadd_rn(f.z, __fmul_rn(__fdiv_rn(sb, fP), w));
         f.w = __fadd_rn(f.w, w);
     }
-    p.film[p.passPixel + uint64_t(pix)] = f;
+    *fp = f;
 }
 
 template <typename K>
-int persistent_blocks(K kernel, int numSMs)
+int persistent_blocks(K kernel, int block, int numSMs)
 {
     int perSM = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kernel, kBlock, 0) != cudaSuccess || perSM < 1)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kernel, block, 0) != cudaSuccess || perSM < 1)
         perSM = 1;
     return perSM * numSMs;
 }
 
-template <int ORDER, bool COUNT>
-cudaError_t extend_t(const PathParams& p, int segment, cudaStream_t stream, int numSMs)
+template <int ORDER, bool COUNT, int BLOCK>
+cudaError_t extend_b(const PassParams& p, int segment, cudaStream_t stream, int numSMs)
 {
-    auto k = k_extend<ORDER, COUNT>;
+    auto k = k_extend<ORDER, COUNT, BLOCK>;
     static int grid = 0;
     if (grid == 0)
-        grid = persistent_blocks(k, numSMs);
-    k<<<grid, kBlock, 0, stream>>>(p, segment);
+        grid = persistent_blocks(k, BLOCK, numSMs);
+    k<<<grid, BLOCK, 0, stream>>>(p, segment);
     return cudaGetLastError();
+}
+
+template <int ORDER, bool COUNT>
+cudaError_t extend_t(const PassParams& p, int segment, int block, cudaStream_t stream, int numSMs)
+{
+    if (block == 64)
+        return extend_b<ORDER, COUNT, 64>(p, segment, stream, numSMs);
+    if (block == 256)
+        return extend_b<ORDER, COUNT, 256>(p, segment, stream, numSMs);
+    return extend_b<ORDER, COUNT, 128>(p, segment, stream, numSMs);
+}
+
+template <int BLOCK>
+cudaError_t shade_b(const PassParams& p, int segment, cudaStream_t stream, int numSMs)
+{
+    auto k = k_shade<BLOCK>;
+    static int grid = 0;
+    if (grid == 0)
+        grid = persistent_blocks(k, BLOCK, numSMs);
+    k<<<grid, BLOCK, 0, stream>>>(p, segment);
+    return cudaGetLastError();
+}
+
+cudaError_t shade_t(const PassParams& p, int segment, int block, cudaStream_t stream, int numSMs)
+{
+    if (block == 64)
+        return shade_b<64>(p, segment, stream, numSMs);
+    if (block == 256)
+        return shade_b<256>(p, segment, stream, numSMs);
+    return shade_b<128>(p, segment, stream, numSMs);
 }
 
 }  // namespace
 
-cudaError_t launch_path_pass(const PathParams& p, int pixelsInPass, int order, int counting, cudaStream_t stream,
-                             int numSMs, const cudaEvent_t* extendEvents)
+cudaError_t launch_path_pass(const PassParams& p, int order, int counting, const PassShape& shape,
+                             cudaStream_t stream, int numSMs, const cudaEvent_t* extendEvents)
 {
     k_generate<<<unsigned((p.nslots + 255) / 256), 256, 0, stream>>>(p);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess)
         return e;
-    static int shadeGrid = 0;
-    if (shadeGrid == 0)
-        shadeGrid = persistent_blocks(k_shade, numSMs);
-    for (int seg = 0; seg < p.maxPathLength; ++seg)
+    for (int seg = 0; seg < p.segments; ++seg)
     {
         if (extendEvents && (e = cudaEventRecord(extendEvents[2 * seg], stream)) != cudaSuccess)
             return e;
         if (order == ORDER_NEAREST)
-            e = counting ? extend_t<ORDER_NEAREST, true>(p, seg, stream, numSMs)
-                         : extend_t<ORDER_NEAREST, false>(p, seg, stream, numSMs);
+            e = counting ? extend_t<ORDER_NEAREST, true>(p, seg, shape.extendBlock, stream, numSMs)
+                         : extend_t<ORDER_NEAREST, false>(p, seg, shape.extendBlock, stream, numSMs);
         else
-            e = counting ? extend_t<ORDER_REF, true>(p, seg, stream, numSMs)
-                         : extend_t<ORDER_REF, false>(p, seg, stream, numSMs);
+            e = counting ? extend_t<ORDER_REF, true>(p, seg, shape.extendBlock, stream, numSMs)
+                         : extend_t<ORDER_REF, false>(p, seg, shape.extendBlock, stream, numSMs);
         if (e != cudaSuccess)
             return e;
         if (extendEvents && (e = cudaEventRecord(extendEvents[2 * seg + 1], stream)) != cudaSuccess)
             return e;
-        k_shade<<<shadeGrid, kBlock, 0, stream>>>(p, seg);
-        if ((e = cudaGetLastError()) != cudaSuccess)
+        if ((e = shade_t(p, seg, shape.shadeBlock, stream, numSMs)) != cudaSuccess)
             return e;
     }
-    k_accumulate<<<unsigned((pixelsInPass + 255) / 256), 256, 0, stream>>>(p, pixelsInPass);
+    k_accumulate<<<unsigned((p.npixels + 255) / 256), 256, 0, stream>>>(p);
     return cudaGetLastError();
 }
 

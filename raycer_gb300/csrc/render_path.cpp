@@ -5,7 +5,9 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstring>
 #include <string>
+#include <vector>
 
 #include "host_internal.h"
 #include "pathtrace.h"
@@ -67,9 +69,9 @@ namespace rcx
 
 void release_render_buffers(rc_tracer* h)
 {
-    void** ptrs[] = { &h->dPath, reinterpret_cast<void**>(&h->dCounts), &h->dTone, &h->dImage };
-    size_t* caps[] = { &h->capPath, &h->capCounts, &h->capTone, &h->capImage };
-    for (int i = 0; i < 4; ++i)
+    void** ptrs[] = { &h->dPath, reinterpret_cast<void**>(&h->dCounts), &h->dTone, &h->dImage, &h->dTables };
+    size_t* caps[] = { &h->capPath, &h->capCounts, &h->capTone, &h->capImage, &h->capTables };
+    for (int i = 0; i < 5; ++i)
     {
         if (*ptrs[i])
         {
@@ -82,24 +84,81 @@ void release_render_buffers(rc_tracer* h)
     h->pathSlots = 0;
 }
 
+// Fills the per-scene record the pass kernels read (pathtrace.h).
+PathScene path_scene(const rc_tracer* h, uint64_t pixelStart)
+{
+    const rc_general& g = h->general;
+    PathScene ps{};
+    ps.sc.nodes = h->dNodes;
+    ps.sc.tris = h->dTris;
+    ps.sc.shade = h->dShade;
+    ps.sc.mats = h->dMats;
+    ps.sc.rootLink = h->rootLink;
+    ps.sc.numTris = int(h->nTris);
+    ps.sc.numMats = int(h->nMats);
+    for (int k = 0; k < 3; ++k)
+    {
+        ps.cam.pos[k] = h->camera.position[k];
+        ps.cam.fwd[k] = h->camera.forward[k];
+        ps.cam.right[k] = h->camera.right[k];
+        ps.cam.up[k] = h->camera.up[k];
+        ps.cam.center[k] = h->camera.image_plane_center[k];
+    }
+    ps.cam.aspect = h->camera.aspect_ratio;
+    ps.cam.ipw = h->camera.image_plane_width;
+    ps.cam.iph = h->camera.image_plane_height;
+    ps.film = h->dFilm;
+    ps.pixelStart = pixelStart;
+    ps.width = int64_t(h->width);
+    ps.n = g.multi_sample_count_sqrt;
+    ps.P = g.path_sample_count;
+    ps.spp = g.multi_sample_count_sqrt * g.multi_sample_count_sqrt * g.path_sample_count;
+    ps.samplerType = g.multi_sampler_type;
+    ps.rx = g.filter_radius[0];
+    ps.ry = g.filter_radius[1];
+    // BoxFilter::setRadius (BoxFilter.cpp:15-21): weight = 1 / (2 r).
+    ps.wx = 1.0f / (2.0f * g.filter_radius[0]);
+    ps.wy = 1.0f / (2.0f * g.filter_radius[1]);
+    ps.rayStartOffset = g.ray_start_offset;
+    ps.maxPathLength = g.max_path_length;
+    ps.rrDepth = g.russian_roulette_depth;
+    ps.frame = h->frameIndex;
+    ps.seed = g.seed;
+    return ps;
+}
+
+PassParams pass_params(void* state, uint64_t slots, unsigned* counts, DevControl* ctl)
+{
+    char* base = static_cast<char*>(state);
+    const size_t S = size_t(slots);
+    PassParams p{};
+    p.o = reinterpret_cast<float4*>(base);
+    p.d = reinterpret_cast<float4*>(base + S * 16);
+    p.thr = reinterpret_cast<float4*>(base + S * 32);
+    p.res = reinterpret_cast<float4*>(base + S * 48);
+    p.hit = reinterpret_cast<int4*>(base + S * 64);
+    p.qa = reinterpret_cast<int*>(base + S * 80);
+    p.qb = reinterpret_cast<int*>(base + S * 84);
+    p.chunkOf = reinterpret_cast<int*>(base + S * 88);
+    p.counts = counts;
+    p.ctl = ctl;
+    return p;
+}
+
 rc_status render_path(rc_tracer* h, uint64_t pixelStart, uint64_t count, const volatile int32_t* cancel)
 {
     const rc_general& g = h->general;
-    const int n = g.multi_sample_count_sqrt;
-    const int P = g.path_sample_count;
-    const uint64_t spp = uint64_t(n) * uint64_t(n) * uint64_t(P);
+    const uint64_t spp = uint64_t(g.multi_sample_count_sqrt) * uint64_t(g.multi_sample_count_sqrt) *
+                         uint64_t(g.path_sample_count);
     if (spp > kTargetSlots)
         return fail(h, RC_UNSUPPORTED, "render: samples per pixel exceed one pass");
     const uint64_t pixelsPerPass = std::max<uint64_t>(1, kTargetSlots / spp);
     const uint64_t slots = std::min<uint64_t>(pixelsPerPass, count) * spp;
+    const uint64_t passes = (count + pixelsPerPass - 1) / pixelsPerPass;
 
     if (h->pathSlots < slots)
     {
-        void* p = h->dPath;
-        size_t cap = h->capPath;
-        rc_status s = grow(h, &p, &cap, size_t(slots) * kPathBytesPerSlot, "allocate path state");
-        h->dPath = p;
-        h->capPath = cap;
+        rc_status s = grow(h, &h->dPath, &h->capPath, size_t(slots) * kPathBytesPerSlot, "allocate path state");
         if (s != RC_OK)
             return s;
         h->pathSlots = slots;
@@ -115,56 +174,27 @@ rc_status render_path(rc_tracer* h, uint64_t pixelStart, uint64_t count, const v
             return s;
     }
 
-    const uint64_t S = h->pathSlots;
-    char* base = static_cast<char*>(h->dPath);
-    PathParams p{};
-    p.sc.nodes = h->dNodes;
-    p.sc.tris = h->dTris;
-    p.sc.shade = h->dShade;
-    p.sc.mats = h->dMats;
-    p.sc.rootLink = h->rootLink;
-    p.sc.numTris = int(h->nTris);
-    p.sc.numMats = int(h->nMats);
-    for (int k = 0; k < 3; ++k)
+    // Scene record + one chunk per pass.
+    std::vector<unsigned char> table(sizeof(PathScene) + size_t(passes) * sizeof(PathChunk));
+    PathScene ps = path_scene(h, pixelStart);
+    std::memcpy(table.data(), &ps, sizeof(ps));
+    PathChunk* chunks = reinterpret_cast<PathChunk*>(table.data() + sizeof(PathScene));
+    for (uint64_t i = 0; i < passes; ++i)
     {
-        p.cam.pos[k] = h->camera.position[k];
-        p.cam.fwd[k] = h->camera.forward[k];
-        p.cam.right[k] = h->camera.right[k];
-        p.cam.up[k] = h->camera.up[k];
-        p.cam.center[k] = h->camera.image_plane_center[k];
+        uint64_t done = i * pixelsPerPass;
+        chunks[i] = PathChunk{ 0, 0, 0, uint32_t(std::min(pixelsPerPass, count - done)), done };
     }
-    p.cam.aspect = h->camera.aspect_ratio;
-    p.cam.ipw = h->camera.image_plane_width;
-    p.cam.iph = h->camera.image_plane_height;
-    p.o = reinterpret_cast<float4*>(base);
-    p.d = reinterpret_cast<float4*>(base + S * 16);
-    p.thr = reinterpret_cast<float4*>(base + S * 32);
-    p.res = reinterpret_cast<float4*>(base + S * 48);
-    p.hit = reinterpret_cast<int4*>(base + S * 64);
-    p.qa = reinterpret_cast<int*>(base + S * 80);
-    p.qb = reinterpret_cast<int*>(base + S * 84);
-    p.counts = h->dCounts;
-    p.film = h->dFilm;
-    p.ctl = h->dCtl;
-    p.pixelStart = pixelStart;
-    p.width = int64_t(h->width);
-    p.n = n;
-    p.P = P;
-    p.spp = int(spp);
-    p.samplerType = g.multi_sampler_type;
-    p.rx = g.filter_radius[0];
-    p.ry = g.filter_radius[1];
-    // BoxFilter::setRadius (BoxFilter.cpp:15-21): weight = 1 / (2 r).
-    p.wx = 1.0f / (2.0f * g.filter_radius[0]);
-    p.wy = 1.0f / (2.0f * g.filter_radius[1]);
-    p.rayStartOffset = g.ray_start_offset;
-    p.maxPathLength = g.max_path_length;
-    p.rrDepth = g.russian_roulette_depth;
-    p.seed = g.seed;
-    p.frame = h->frameIndex;
+    {
+        rc_status s = grow(h, &h->dTables, &h->capTables, table.size(), "allocate pass tables");
+        if (s != RC_OK)
+            return s;
+    }
+    RC_CUDA_TRY(h, cudaMemcpyAsync(h->dTables, table.data(), table.size(), cudaMemcpyHostToDevice, h->stream),
+                "upload pass tables");
+    const PathScene* dScene = static_cast<const PathScene*>(h->dTables);
+    const PathChunk* dChunks = reinterpret_cast<const PathChunk*>(static_cast<char*>(h->dTables) + sizeof(PathScene));
 
     // Events around every extend launch of every pass (stage 0 timing).
-    const uint64_t passes = (count + pixelsPerPass - 1) / pixelsPerPass;
     const size_t needEvents = size_t(passes) * size_t(2 * std::max(g.max_path_length, 0));
     const bool timeStages = needEvents <= 4096;
     while (timeStages && h->evPool.size() < needEvents)
@@ -174,23 +204,28 @@ rc_status render_path(rc_tracer* h, uint64_t pixelStart, uint64_t count, const v
         h->evPool.push_back(e);
     }
 
+    PassParams pp = pass_params(h->dPath, h->pathSlots, h->dCounts, h->dCtl);
+    pp.scenes = dScene;
+    pp.numChunks = 1;
+    pp.segments = g.max_path_length;
+    PassShape shape;
+
     RC_CUDA_TRY(h, cudaMemsetAsync(h->dCtl, 0, sizeof(DevControl), h->stream), "reset control block");
     RC_CUDA_TRY(h, cudaEventRecord(h->ev0, h->stream), "record start event");
-    uint64_t pass = 0;
-    for (uint64_t done = 0; done < count; done += pixelsPerPass, ++pass)
+    for (uint64_t pass = 0; pass < passes; ++pass)
     {
-        if (done > 0 && cancel && *cancel)
+        if (pass > 0 && cancel && *cancel)
         {
             cudaStreamSynchronize(h->stream);
             h->frameIndex++;
             return fail(h, RC_CANCELLED, "render: cancelled");
         }
-        uint64_t np = std::min(pixelsPerPass, count - done);
-        p.passPixel = done;
-        p.nslots = int(np * spp);
+        pp.chunks = dChunks + pass;
+        pp.npixels = int(chunks[pass].pixels);
+        pp.nslots = int(uint64_t(chunks[pass].pixels) * spp);
         RC_CUDA_TRY(h, cudaMemsetAsync(h->dCounts, 0, countsBytes, h->stream), "reset queue counters");
         const cudaEvent_t* ev = timeStages ? h->evPool.data() + pass * size_t(2 * g.max_path_length) : nullptr;
-        RC_CUDA_TRY(h, launch_path_pass(p, int(np), h->order, h->counting, h->stream, h->numSMs, ev),
+        RC_CUDA_TRY(h, launch_path_pass(pp, h->order, h->counting, shape, h->stream, h->numSMs, ev),
                     "launch path-tracing pass");
     }
     RC_CUDA_TRY(h, cudaEventRecord(h->ev1, h->stream), "record end event");

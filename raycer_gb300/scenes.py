@@ -280,3 +280,55 @@ def heightfield_scene(seed: int = 2, nx: int = 1024, nz: int = 512, width: int =
         max_leaf_size=4,
         settings=dict(tracer="ray"),
     )
+
+
+# ---------------------------------------------------------------------------
+# Batch of rooms (batched path tracing).
+
+
+def room_with_extra(seed: int, extra: int, width: int, height: int, ms_sqrt: int, max_path_length: int = 8,
+                    rr_depth: int = 3, palette: int = 256) -> SceneDesc:
+    """The 320x240 workload's room (seed `seed`) plus `extra` random triangles
+    drawn like its clutter (centres U[-0.8,0.8]^3, vertices at uniform unit
+    directions scaled by U(0.05,0.2)); the extra triangles take their albedo
+    U(0.2,0.8)^3 from a palette of `palette` materials. numpy PCG64 stream of
+    uniform doubles only."""
+    base = room_scene(seed=seed, width=width, height=height)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    if extra > 0:
+        c = -0.8 + 1.6 * rng.random((extra, 1, 3))
+        z = -1.0 + 2.0 * rng.random((extra, 3))
+        phi = 2.0 * math.pi * rng.random((extra, 3))
+        r = np.sqrt(np.maximum(0.0, 1.0 - z * z))
+        d = np.stack([r * np.cos(phi), r * np.sin(phi), z], axis=-1)
+        sc = 0.05 + 0.15 * rng.random((extra, 3, 1))
+        v = _f32((c + d * sc).reshape(extra, 9))
+        albedo = (0.2 + 0.6 * rng.random((palette, 3))).astype(np.float32).astype(np.float64)
+        first = len(base.materials)
+        mats = base.materials + [Material(diffuse=tuple(float(x) for x in a)) for a in albedo]
+        midx = first + (rng.random(extra) * palette).astype(np.uint32).clip(0, palette - 1)
+        base.vertices = np.concatenate([base.vertices, v])
+        base.material_index = np.concatenate([base.material_index, midx.astype(np.uint32)])
+        base.materials = mats
+    base.name = f"room(seed={seed})+{extra} tris {width}x{height} {ms_sqrt * ms_sqrt} spp"
+    base.settings.update(multi_sample_count_sqrt=ms_sqrt, max_path_length=max_path_length,
+                         russian_roulette_depth=rr_depth)
+    return base
+
+
+def batch_scenes(seed: int = 3, count: int = 64, n_min: float = 1e3, n_max: float = 2e6,
+                 resolutions=(256, 512, 768, 1024), spps=(1, 4, 16, 64)) -> list:
+    """The batched workload: `count` rooms, each with N log-uniform in
+    [n_min, n_max] extra random triangles, square film size uniform over
+    `resolutions`, samples per pixel uniform over `spps` (as n x n CMJ film
+    samples), maximum path length 8 with Russian roulette from segment 3."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    out = []
+    for i in range(count):
+        u = rng.random(3)
+        n = int(round(math.exp(math.log(n_min) + u[0] * (math.log(n_max) - math.log(n_min)))))
+        res = resolutions[min(int(u[1] * len(resolutions)), len(resolutions) - 1)]
+        spp = spps[min(int(u[2] * len(spps)), len(spps) - 1)]
+        ms = int(round(math.sqrt(spp)))
+        out.append(room_with_extra(seed * 1000 + i, n, res, res, ms))
+    return out
