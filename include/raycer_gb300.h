@@ -102,9 +102,15 @@ typedef struct rc_general
     float ray_start_offset;          /* rayStartOffset (Scene.h:95: 1e-5)           */
     float background[3];             /* backgroundColor (RAY tracer, miss)          */
     int32_t russian_roulette_depth;  /* 0 = off (reference); else first RR segment  */
-    int32_t reserved;                /* must be 0                                   */
+    int32_t flags;                   /* rc_general_flags (0 = reference behaviour)  */
     uint64_t seed;                   /* random stream seed (paths, CMJ permutation) */
 } rc_general;
+
+/* GPU-only extensions of the PATH tracer (no counterpart in the reference).
+ * RC_GENERAL_SKY: a path that leaves the scene receives `background` as
+ * radiance, times its throughput (PathTracer::traceRecursive returns black,
+ * PathTracer.cpp:43-44). */
+typedef enum rc_general_flags { RC_GENERAL_SKY = 1 } rc_general_flags;
 
 /* Scene::ToneMapper fields (src/Raytracing/Scene.h:135-159). */
 typedef struct rc_tonemapper
@@ -405,6 +411,95 @@ rc_status rc_get_stats(const rc_tracer* h, rc_stats* out);
 /* The handle's CUDA stream (cudaStream_t) as an opaque pointer. */
 void* rc_stream(rc_tracer* h);
 rc_status rc_sync(rc_tracer* h);
+
+/* ------------------------------------------------------------------------ */
+/* Neural radiance cache (GPU-only extension; no counterpart in the          */
+/* reference, whose PathTracer::traceRecursive always recurses to           */
+/* maxPathLength, PathTracer.cpp:30-75).                                     */
+/*                                                                           */
+/* A small MLP (128 encoded inputs -> 4 x 64 ReLU -> 3, exp output; BF16     */
+/* weights and activations, FP32 accumulation on the tensor cores) predicts */
+/* the radiance a path would carry from a surface point. When enabled, a    */
+/* PATH render ends every path at the hit of `terminate_segment` with a     */
+/* cache lookup, except one random slot in each run of `train_stride`,      */
+/* which traces the full plain path (and contributes it to the film) and    */
+/* records its vertices; after the pass the suffix radiance of each vertex  */
+/* becomes a training sample and `train_steps` Adam steps of `train_batch`  */
+/* random samples update the cache.                                          */
+/*                                                                           */
+/* A query is 12 floats: position[3], direction[3] (unit, from the surface  */
+/* toward where the path came from), normal[3], diffuse albedo[3].          */
+
+#define RC_NRC_PARAMS 20992       /* packed [out][in] weights: 64x128, 3 x 64x64, 8x64 (rows 3-7 zero) */
+#define RC_NRC_QUERY_FLOATS 12
+#define RC_NRC_INPUTS 128
+
+typedef struct rc_nrc_config
+{
+    int32_t enabled;            /* PATH renders use the cache                        */
+    int32_t terminate_segment;  /* paths end at the hit of this segment (2)          */
+    int32_t train_stride;       /* one training path per this many slots (16)        */
+    int32_t train_steps;        /* optimizer steps per render pass (4)               */
+    int32_t train_batch;        /* samples per step (16384)                          */
+    int32_t min_suffix;         /* vertices a depth-limited suffix needs (3)         */
+    float learning_rate;        /* Adam step size (1e-2)                             */
+    float beta1;                /* 0.9                                               */
+    float beta2;                /* 0.99                                              */
+    float epsilon;              /* 1e-8                                              */
+    float box_min[3];           /* position-encoding box; box_max <= box_min on any */
+    float box_max[3];           /*   axis = the scene's bounds at render time        */
+    uint64_t seed;              /* weight initialisation and training-slot choice    */
+} rc_nrc_config;
+
+typedef struct rc_nrc_stats
+{
+    uint64_t lookups;           /* cache lookups of the last render pass            */
+    uint64_t training_samples;  /* training samples it produced                     */
+    uint64_t steps;             /* optimizer steps taken since configure            */
+    float last_loss;            /* loss of the last step (relative L2, mean)        */
+    float reserved;
+    double train_ms;            /* time of the last render's training work          */
+} rc_nrc_stats;
+
+rc_status rc_nrc_defaults(rc_nrc_config* out);
+/* (Re)initialises the weights (seeded He-uniform) and the optimizer. */
+rc_status rc_nrc_configure(rc_tracer* h, const rc_nrc_config* cfg);
+rc_status rc_nrc_set_enabled(rc_tracer* h, int32_t enabled);
+/* FP32 master weights, RC_NRC_PARAMS floats; set also resets the optimizer. */
+rc_status rc_nrc_get_params(rc_tracer* h, float* params, int64_t count);
+rc_status rc_nrc_set_params(rc_tracer* h, const float* params, int64_t count);
+/* Cache output (rgb) of n host queries. */
+rc_status rc_nrc_infer(rc_tracer* h, const float* queries, int64_t n, float* rgb);
+/* The encoded BF16 inputs of n queries, widened to float (n x 128). */
+rc_status rc_nrc_encode(rc_tracer* h, const float* queries, int64_t n, float* features);
+/* Gradient (RC_NRC_PARAMS floats, [out][in] per layer) and value of the mean
+ * relative L2 loss sum((p - y)^2 / (p^2 + 0.01)) / (3 n), the denominator
+ * held constant, at the current weights; no update. */
+rc_status rc_nrc_gradient(rc_tracer* h, const float* queries, const float* targets, int64_t n, float* grad,
+                          float* loss);
+/* `steps` Adam steps on one host batch (n <= 1<<20); losses[steps] optional. */
+rc_status rc_nrc_train(rc_tracer* h, const float* queries, const float* targets, int64_t n, int32_t steps,
+                       float* losses);
+/* Training samples of the last render pass: 16 floats each (query[12],
+ * target rgb[3], tag), the tag's 32 bits = vertex index << 24 | training
+ * path index (slot / train_stride). Ordered by (vertex, path); *count =
+ * samples available, at most `capacity` copied. */
+rc_status rc_nrc_read_samples(rc_tracer* h, float* records, int64_t capacity, int64_t* count);
+rc_status rc_nrc_get_stats(rc_tracer* h, rc_nrc_stats* out);
+
+/* ------------------------------------------------------------------------ */
+/* High-spp ground truth and its error (GPU-only extension).                */
+
+/* d_acc (device, 4 doubles per film pixel) += the film's r, g, b, weight
+ * sums in float64; clear_film != 0 then zeroes the film (the frame counter
+ * keeps running, unlike rc_clear). */
+rc_status rc_film_accumulate_f64(rc_tracer* h, double* d_acc, int32_t clear_film);
+/* RMSE over all pixels and channels between the display images of the film
+ * and of d_truth (4 doubles per pixel): both resolved (rgb / weight) and
+ * Reinhard-mapped with the tonemapper record's key, the log-average and
+ * maximum luminance taken from d_truth, then gamma and clamp as configured;
+ * computed in float64. */
+rc_status rc_film_rmse_f64(rc_tracer* h, const double* d_truth, double* rmse);
 
 #ifdef __cplusplus
 }

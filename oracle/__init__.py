@@ -43,6 +43,11 @@ def _setup(lib: C.CDLL, protos: dict) -> C.CDLL:
 
 
 _ORACLE_PROTOS = {
+    "or_nrc_features": (None, [P, i64, P, P, C.c_int, P]),
+    "or_nrc_forward": (None, [P, P, i64, P, P, C.c_int, P]),
+    "or_nrc_loss": (f64, [P, P, P, i64, P, P, C.c_int, P]),
+    "or_nrc_gradient": (f64, [P, P, P, i64, P, P, C.c_int, P]),
+    "or_nrc_adam": (None, [P, P, P, P, i64, f32, f32, f32, f32]),
     "or_scene_new": (P, [P, P, i64, P, P, P, i32, u32, C.c_int]),
     "or_scene_set_bvh": (None, [P, i64, P, P, P, P, P]),
     "or_scene_free": (None, [P]),
@@ -375,3 +380,60 @@ def cam64_from_state(state19: np.ndarray) -> np.ndarray:
     """Camera64 input (pos, right, up, centre, aspect, ipw, iph) from the reference camera state."""
     s = np.asarray(state19, np.float64)
     return np.concatenate([s[0:3], s[6:9], s[9:12], s[12:15], s[15:18]])
+
+
+# ---------------------------------------------------------------------------
+# Radiance-cache network (oracle/nrc64.cpp). `box` = (lo[3], inv[3]).
+
+def _box(box):
+    lo = np.ascontiguousarray(box[0], np.float32)
+    inv = np.ascontiguousarray(box[1], np.float32)
+    return lo, inv
+
+
+def nrc_features(queries: np.ndarray, box, emulate: bool = False) -> np.ndarray:
+    q = np.ascontiguousarray(queries, np.float32)
+    lo, inv = _box(box)
+    out = np.empty((q.shape[0], 128), np.float64)
+    oracle_lib().or_nrc_features(_ptr(q), q.shape[0], _ptr(lo), _ptr(inv), int(emulate), _ptr(out))
+    return out
+
+
+def nrc_forward(params: np.ndarray, queries: np.ndarray, box, emulate: bool = False) -> np.ndarray:
+    w = np.ascontiguousarray(params, np.float32)
+    q = np.ascontiguousarray(queries, np.float32)
+    lo, inv = _box(box)
+    out = np.empty((q.shape[0], 3), np.float64)
+    oracle_lib().or_nrc_forward(_ptr(w), _ptr(q), q.shape[0], _ptr(lo), _ptr(inv), int(emulate), _ptr(out))
+    return out
+
+
+def nrc_loss(params, queries, targets, box, emulate: bool = False, den_pred=None) -> float:
+    w = np.ascontiguousarray(params, np.float32)
+    q = np.ascontiguousarray(queries, np.float32)
+    t = np.ascontiguousarray(targets, np.float32)
+    lo, inv = _box(box)
+    d = None if den_pred is None else np.ascontiguousarray(den_pred, np.float64)
+    return oracle_lib().or_nrc_loss(_ptr(w), _ptr(q), _ptr(t), q.shape[0], _ptr(lo), _ptr(inv), int(emulate),
+                                    None if d is None else _ptr(d))
+
+
+def nrc_gradient(params, queries, targets, box, emulate: bool = False) -> tuple[np.ndarray, float]:
+    w = np.ascontiguousarray(params, np.float32)
+    q = np.ascontiguousarray(queries, np.float32)
+    t = np.ascontiguousarray(targets, np.float32)
+    lo, inv = _box(box)
+    g = np.empty(w.size, np.float64)
+    loss = oracle_lib().or_nrc_gradient(_ptr(w), _ptr(q), _ptr(t), q.shape[0], _ptr(lo), _ptr(inv), int(emulate),
+                                        _ptr(g))
+    return g, loss
+
+
+def nrc_adam(master, m, v, grad, t: int, lr=1e-2, b1=0.9, b2=0.99, eps=1e-8):
+    """One float32 Adam step; returns (master, m, v) updated copies."""
+    w = np.array(master, np.float32)
+    mm = np.array(m, np.float32)
+    vv = np.array(v, np.float32)
+    g = np.ascontiguousarray(grad, np.float32)
+    oracle_lib().or_nrc_adam(_ptr(w), _ptr(mm), _ptr(vv), _ptr(g), int(t), lr, b1, b2, eps)
+    return w, mm, vv

@@ -56,7 +56,7 @@ class rc_general(C.Structure):
     _fields_ = [("tracer_type", C.c_int32), ("max_path_length", C.c_int32), ("path_sample_count", C.c_int32),
                 ("multi_sample_count_sqrt", C.c_int32), ("multi_sampler_type", C.c_int32),
                 ("filter_type", C.c_int32), ("filter_radius", C.c_float * 2), ("ray_start_offset", C.c_float),
-                ("background", C.c_float * 3), ("russian_roulette_depth", C.c_int32), ("reserved", C.c_int32),
+                ("background", C.c_float * 3), ("russian_roulette_depth", C.c_int32), ("flags", C.c_int32),
                 ("seed", C.c_uint64)]
 
 
@@ -103,6 +103,23 @@ class rc_batch_tuning(C.Structure):
     _fields_ = [("bucket_min_triangles", C.c_uint32 * 4), ("slots", C.c_uint32 * 4), ("extend_block", C.c_int32 * 4),
                 ("shade_block", C.c_int32 * 4), ("measured_paths_per_ms", C.c_double * 4)]
 
+
+class rc_nrc_config(C.Structure):
+    _fields_ = [("enabled", C.c_int32), ("terminate_segment", C.c_int32), ("train_stride", C.c_int32),
+                ("train_steps", C.c_int32), ("train_batch", C.c_int32), ("min_suffix", C.c_int32),
+                ("learning_rate", C.c_float), ("beta1", C.c_float), ("beta2", C.c_float), ("epsilon", C.c_float),
+                ("box_min", C.c_float * 3), ("box_max", C.c_float * 3), ("seed", C.c_uint64)]
+
+
+class rc_nrc_stats(C.Structure):
+    _fields_ = [("lookups", C.c_uint64), ("training_samples", C.c_uint64), ("steps", C.c_uint64),
+                ("last_loss", C.c_float), ("reserved", C.c_float), ("train_ms", C.c_double)]
+
+
+RC_GENERAL_SKY = 1
+RC_NRC_PARAMS = 20992
+RC_NRC_QUERY_FLOATS = 12
+RC_NRC_INPUTS = 128
 
 P = C.c_void_p
 i32, i64, u32, u64 = C.c_int32, C.c_int64, C.c_uint32, C.c_uint64
@@ -155,6 +172,19 @@ PROTOTYPES = {
     "rc_get_stats": (i32, [P, C.POINTER(rc_stats)]),
     "rc_stream": (P, [P]),
     "rc_sync": (i32, [P]),
+    "rc_nrc_defaults": (i32, [C.POINTER(rc_nrc_config)]),
+    "rc_nrc_configure": (i32, [P, C.POINTER(rc_nrc_config)]),
+    "rc_nrc_set_enabled": (i32, [P, i32]),
+    "rc_nrc_get_params": (i32, [P, P, i64]),
+    "rc_nrc_set_params": (i32, [P, P, i64]),
+    "rc_nrc_infer": (i32, [P, P, i64, P]),
+    "rc_nrc_encode": (i32, [P, P, i64, P]),
+    "rc_nrc_gradient": (i32, [P, P, P, i64, P, P]),
+    "rc_nrc_train": (i32, [P, P, P, i64, i32, P]),
+    "rc_nrc_read_samples": (i32, [P, P, i64, C.POINTER(i64)]),
+    "rc_nrc_get_stats": (i32, [P, C.POINTER(rc_nrc_stats)]),
+    "rc_film_accumulate_f64": (i32, [P, P, i32]),
+    "rc_film_rmse_f64": (i32, [P, P, C.POINTER(C.c_double)]),
 }
 
 

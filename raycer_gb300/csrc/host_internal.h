@@ -11,6 +11,48 @@
 #include "bvh_build.h"
 #include "device_types.h"
 #include "kernels.h"
+#include "nrc_kernels.h"
+
+namespace rcx
+{
+
+// Neural radiance cache state of a handle (nrc_host.cpp).
+struct NrcState
+{
+    rc_nrc_config cfg{};
+    bool configured = false;
+    uint64_t steps = 0;        // Adam steps taken (t)
+    uint64_t passes = 0;       // render passes that trained
+    float* dMaster = nullptr;  // FP32 weights, Adam m, v: kNrcParamCount each
+    float* dM = nullptr;
+    float* dV = nullptr;
+    __nv_bfloat16* dW = nullptr;
+    float* dPartials = nullptr;      // [blocks][params]
+    float* dLossPartials = nullptr;  // [blocks]
+    float* dLoss = nullptr;          // per step of the last training call
+    size_t capLoss = 0;
+    float* dGrad = nullptr;
+    unsigned* dCounters = nullptr;   // [0] lookups, [1] training samples, [2] api count
+    void* dQuery = nullptr;          // lookups, one record per slot
+    size_t capQuery = 0;
+    void* dVtx = nullptr;            // training vertices
+    size_t capVtx = 0;
+    void* dTerm = nullptr;
+    size_t capTerm = 0;
+    void* dIndex = nullptr;
+    size_t capIndex = 0;
+    void* dApi = nullptr;            // host-batch records
+    size_t capApi = 0;
+    void* dApiOut = nullptr;
+    size_t capApiOut = 0;
+    int blocks = 0;
+    int lastSteps = 0;
+    double trainMs = 0.0;
+    cudaEvent_t evTrain0 = nullptr;
+    cudaEvent_t evTrain1 = nullptr;
+};
+
+}  // namespace rcx
 
 struct rc_tracer
 {
@@ -81,6 +123,11 @@ struct rc_tracer
     rcx::DevControl* dCtl = nullptr;
     rc_stats stats{};
     size_t deviceBytes = 0;
+
+    rcx::NrcState nrc;
+    // FP64 RMSE scratch (rc_film_rmse_f64)
+    void* dRmse = nullptr;
+    size_t capRmse = 0;
 };
 
 namespace rcx
@@ -91,9 +138,20 @@ rc_status raycast_into(rc_tracer* h, const rc_ray* dRays, uint64_t pixelStart, u
 rc_status render_raycast(rc_tracer* h, uint64_t pixelStart, uint64_t count, const rc_ray* dRays);
 rc_status render_path(rc_tracer* h, uint64_t pixelStart, uint64_t count, const volatile int32_t* cancel);
 void release_render_buffers(rc_tracer* h);
+// Grow-only device buffer (frees the old one); counts into deviceBytes.
+rc_status device_grow(rc_tracer* h, void** ptr, size_t* cap, size_t bytes, const char* what);
+
+struct PassParams;
+// NRC work of a PATH render (nrc_host.cpp): buffers and per-pass state,
+// the lookups before the film update, the training after it.
+rc_status nrc_prepare(rc_tracer* h, uint64_t slots, int segments);
+void nrc_pass_state(rc_tracer* h, PassParams& pp, uint32_t passIndex);
+rc_status nrc_lookups(rc_tracer* h, const PassParams& pp);
+rc_status nrc_train_pass(rc_tracer* h, const PassParams& pp);
+bool nrc_active(const rc_tracer* h);
+void nrc_release(rc_tracer* h);
 
 struct PathScene;
-struct PassParams;
 // The pass kernels' record of a handle's scene, camera, PATH settings and film.
 PathScene path_scene(const rc_tracer* h, uint64_t pixelStart);
 // Slot arrays of a path-state buffer of `slots` slots (pathtrace.h layout).

@@ -107,9 +107,19 @@ __global__ void __launch_bounds__(256) k_generate(PassParams p)
 {
     uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s == 0)
+    {
         p.counts[0] = uint32_t(p.nslots);
+        if (p.nrc.counters)
+        {
+            p.nrc.counters[0] = 0;
+            p.nrc.counters[1] = 0;
+        }
+    }
     if (s >= uint32_t(p.nslots))
         return;
+    // Training-path records start inactive; the path's end marks them.
+    if (p.nrc.term && s % uint32_t(p.nrc.trainStride) == 0)
+        p.nrc.term[s / uint32_t(p.nrc.trainStride)] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     const int c = chunk_of_slot(p, s);
     p.chunkOf[s] = c;
     const PathChunk ch = p.chunks[c];
@@ -215,7 +225,40 @@ __global__ void __launch_bounds__(BLOCK, (RC_TRACE_MIN_BLOCKS * 128) / BLOCK) k_
         atomicOr(&p.ctl->error, 1);
 }
 
-template <int BLOCK>
+// Training-path choice of slot s: one random slot per run of trainStride.
+__device__ __forceinline__ uint32_t nrc_pick(const NrcPass& n, uint32_t g)
+{
+    return mix32(n.trainKey ^ mix32(g + 0x9e3779b9u)) % uint32_t(n.trainStride);
+}
+
+__device__ __forceinline__ bool nrc_training(const NrcPass& n, uint32_t s)
+{
+    if (n.trainStride <= 0)
+        return false;
+    uint32_t g = s / uint32_t(n.trainStride);
+    return s - g * uint32_t(n.trainStride) == nrc_pick(n, g);
+}
+
+__device__ __forceinline__ NrcRecord nrc_record(V3 x, float4 d, V3 nrm, float4 rho, float r, float g, float b,
+                                                float tag)
+{
+    NrcRecord rec;
+    rec.a = make_float4(x.x, x.y, x.z, -d.x);
+    rec.b = make_float4(-d.y, -d.z, nrm.x, nrm.y);
+    rec.c = make_float4(nrm.z, rho.x, rho.y, rho.z);
+    rec.d = make_float4(r, g, b, tag);
+    return rec;
+}
+
+__device__ __forceinline__ void nrc_end(const NrcPass& n, uint32_t g, float r, float gg, float b, uint32_t flags)
+{
+    n.term[g] = make_float4(r, gg, b, __uint_as_float(flags | kNrcTermActive));
+}
+
+// NRC: training paths record every vertex (query + bounce factor) and their
+// terminal radiance; other paths end at the hit of segment termSegment with
+// a cache lookup (res gets thr * cache after the last segment).
+template <int BLOCK, bool NRC>
 __global__ void __launch_bounds__(BLOCK) k_shade(PassParams p, int segment)
 {
     const unsigned total = *reinterpret_cast<volatile unsigned*>(&p.counts[segment * 4 + 0]);
@@ -229,15 +272,37 @@ __global__ void __launch_bounds__(BLOCK) k_shade(PassParams p, int segment)
             break;
         unsigned q = base + lane_id();
         bool cont = false;
+        bool lookup = false;
         int s = -1;
+        NrcRecord lrec;
         if (q < total)
         {
             s = qin[q];
             int4 h = p.hit[s];
-            if (h.x >= 0)
+            const PathChunk& ch = p.chunks[p.chunkOf[s]];
+            const PathScene& scn = p.scenes[ch.scene];
+            const bool train = NRC && nrc_training(p.nrc, uint32_t(s));
+            const uint32_t g = NRC ? uint32_t(s) / uint32_t(max(p.nrc.trainStride, 1)) : 0u;
+            if (h.x < 0)
             {
-                const PathChunk& ch = p.chunks[p.chunkOf[s]];
-                const PathScene& scn = p.scenes[ch.scene];
+                if (scn.skyOn)
+                {
+                    // GPU extension: misses see a constant sky radiance.
+                    float4 thr = p.thr[s];
+                    float4 r = p.res[s];
+                    r.x = __fmul_rn(thr.x, scn.sky[0]);
+                    r.y = __fmul_rn(thr.y, scn.sky[1]);
+                    r.z = __fmul_rn(thr.z, scn.sky[2]);
+                    p.res[s] = r;
+                }
+                if (train)
+                {
+                    const float on = scn.skyOn ? 1.0f : 0.0f;
+                    nrc_end(p.nrc, g, on * scn.sky[0], on * scn.sky[1], on * scn.sky[2], uint32_t(segment));
+                }
+            }
+            else
+            {
                 const DevScene sc = scn.sc;
                 const float4* tp = reinterpret_cast<const float4*>(sc.tris + h.x);
                 float4 tc = __ldg(tp + 2);
@@ -254,16 +319,32 @@ __global__ void __launch_bounds__(BLOCK) k_shade(PassParams p, int segment)
                     r.y = __fmul_rn(thr.y, me.y);
                     r.z = __fmul_rn(thr.z, me.z);
                     p.res[s] = r;
+                    if (train)
+                        nrc_end(p.nrc, g, me.x, me.y, me.z, uint32_t(segment));
+                }
+                else if (NRC && !train && segment == p.nrc.termSegment)
+                {
+                    const float4* sp = reinterpret_cast<const float4*>(sc.shade + h.x);
+                    float4 sn = __ldg(sp + 0);
+                    V3 nrm = v3(sn.x, sn.y, sn.z);
+                    if (mflags & kMatInvertNormal)
+                        nrm = v3(-nrm.x, -nrm.y, -nrm.z);
+                    float4 o = p.o[s];
+                    float4 d = p.d[s];
+                    V3 ip = vfma(v3(d.x, d.y, d.z), __int_as_float(h.y), v3(o.x, o.y, o.z));
+                    lrec = nrc_record(ip, d, nrm, md, 0.0f, 0.0f, 0.0f, __int_as_float(s));
+                    lookup = true;
                 }
                 else if (segment + 1 < scn.maxPathLength)
                 {
                     SlotInfo si = slot_info(ch, scn, uint32_t(s));
                     uint32_t key = stream_key(scn.seed, scn.frame, si.pixelGlobal, si.sample);
                     bool alive = true;
+                    float qs = 1.0f;
                     if (scn.rrDepth > 0 && segment + 1 >= scn.rrDepth)
                     {
                         float m = fmaxf(thr.x, fmaxf(thr.y, thr.z));
-                        float qs = fminf(m, 1.0f);
+                        qs = fminf(m, 1.0f);
                         float xi = stream_float(key, kCounterRoulette + uint32_t(segment));
                         if (!(xi < qs))
                             alive = false;
@@ -274,33 +355,60 @@ __global__ void __launch_bounds__(BLOCK) k_shade(PassParams p, int segment)
                             thr.z = __fdiv_rn(thr.z, qs);
                         }
                     }
+                    const float4* sp = reinterpret_cast<const float4*>(sc.shade + h.x);
+                    float4 sn = __ldg(sp + 0);
+                    V3 nrm = v3(sn.x, sn.y, sn.z);
+                    if (mflags & kMatInvertNormal)
+                        nrm = v3(-nrm.x, -nrm.y, -nrm.z);
+                    float4 o = p.o[s];
+                    float4 d = p.d[s];
+                    float t = __int_as_float(h.y);
+                    V3 ip = vfma(v3(d.x, d.y, d.z), t, v3(o.x, o.y, o.z));
                     if (alive)
                     {
-                        const float4* sp = reinterpret_cast<const float4*>(sc.shade + h.x);
-                        float4 sn = __ldg(sp + 0);
                         float4 st = __ldg(sp + 1);
                         float4 sb = __ldg(sp + 2);
-                        V3 nrm = v3(sn.x, sn.y, sn.z);
-                        if (mflags & kMatInvertNormal)
-                            nrm = v3(-nrm.x, -nrm.y, -nrm.z);
                         float xr = stream_float(key, kCounterBounce + 2u * uint32_t(segment));
                         float yr = stream_float(key, kCounterBounce + 2u * uint32_t(segment) + 1u);
                         V3 dir = hemisphere_cosine(v3(st.x, st.y, st.z), v3(sb.x, sb.y, sb.z), nrm, xr, yr);
-                        float4 o = p.o[s];
-                        float4 d = p.d[s];
-                        float t = __int_as_float(h.y);
-                        V3 ip = vfma(v3(d.x, d.y, d.z), t, v3(o.x, o.y, o.z));
                         V3 no = vfma(dir, scn.rayStartOffset, ip);
                         float alpha = fabsf(vdot(dir, nrm));
                         // brdf = 2 * reflectance * alpha (PathTracer.cpp:70-71)
-                        thr.x = __fmul_rn(thr.x, __fmul_rn(__fmul_rn(2.0f, md.x), alpha));
-                        thr.y = __fmul_rn(thr.y, __fmul_rn(__fmul_rn(2.0f, md.y), alpha));
-                        thr.z = __fmul_rn(thr.z, __fmul_rn(__fmul_rn(2.0f, md.z), alpha));
+                        float fr = __fmul_rn(__fmul_rn(2.0f, md.x), alpha);
+                        float fg = __fmul_rn(__fmul_rn(2.0f, md.y), alpha);
+                        float fb = __fmul_rn(__fmul_rn(2.0f, md.z), alpha);
+                        thr.x = __fmul_rn(thr.x, fr);
+                        thr.y = __fmul_rn(thr.y, fg);
+                        thr.z = __fmul_rn(thr.z, fb);
                         p.o[s] = make_float4(no.x, no.y, no.z, __int_as_float(h.x));
                         p.d[s] = make_float4(dir.x, dir.y, dir.z, 0.0f);
                         p.thr[s] = thr;
                         cont = true;
+                        if (train)
+                            p.nrc.vtx[size_t(segment) * size_t(p.nrc.groups) + g] =
+                                nrc_record(ip, d, nrm, md, fr / qs, fg / qs, fb / qs, 0.0f);
                     }
+                    else if (train)
+                    {
+                        p.nrc.vtx[size_t(segment) * size_t(p.nrc.groups) + g] =
+                            nrc_record(ip, d, nrm, md, 0.0f, 0.0f, 0.0f, 0.0f);
+                        nrc_end(p.nrc, g, 0.0f, 0.0f, 0.0f, uint32_t(segment + 1));
+                    }
+                }
+                else if (train)
+                {
+                    // The depth limit cuts the path: its radiance from here on is 0.
+                    const float4* sp = reinterpret_cast<const float4*>(sc.shade + h.x);
+                    float4 sn = __ldg(sp + 0);
+                    V3 nrm = v3(sn.x, sn.y, sn.z);
+                    if (mflags & kMatInvertNormal)
+                        nrm = v3(-nrm.x, -nrm.y, -nrm.z);
+                    float4 o = p.o[s];
+                    float4 d = p.d[s];
+                    V3 ip = vfma(v3(d.x, d.y, d.z), __int_as_float(h.y), v3(o.x, o.y, o.z));
+                    p.nrc.vtx[size_t(segment) * size_t(p.nrc.groups) + g] =
+                        nrc_record(ip, d, nrm, md, 0.0f, 0.0f, 0.0f, 0.0f);
+                    nrc_end(p.nrc, g, 0.0f, 0.0f, 0.0f, uint32_t(segment + 1) | kNrcTermTruncated);
                 }
             }
         }
@@ -313,6 +421,19 @@ __global__ void __launch_bounds__(BLOCK) k_shade(PassParams p, int segment)
             qbase = __shfl_sync(0xffffffffu, qbase, 0);
             if (cont)
                 qout[qbase + __popc(mask & ((1u << lane_id()) - 1u))] = s;
+        }
+        if (NRC)
+        {
+            unsigned lmask = __ballot_sync(0xffffffffu, lookup);
+            if (lmask)
+            {
+                unsigned lbase = 0;
+                if (lane_id() == 0)
+                    lbase = atomicAdd(&p.nrc.counters[0], unsigned(__popc(lmask)));
+                lbase = __shfl_sync(0xffffffffu, lbase, 0);
+                if (lookup)
+                    p.nrc.query[lbase + __popc(lmask & ((1u << lane_id()) - 1u))] = lrec;
+            }
         }
     }
 }
@@ -381,10 +502,10 @@ cudaError_t extend_t(const PassParams& p, int segment, int block, cudaStream_t s
     return extend_b<ORDER, COUNT, 128>(p, segment, stream, numSMs);
 }
 
-template <int BLOCK>
+template <int BLOCK, bool NRC>
 cudaError_t shade_b(const PassParams& p, int segment, cudaStream_t stream, int numSMs)
 {
-    auto k = k_shade<BLOCK>;
+    auto k = k_shade<BLOCK, NRC>;
     static int grid = 0;
     if (grid == 0)
         grid = persistent_blocks(k, BLOCK, numSMs);
@@ -394,17 +515,55 @@ cudaError_t shade_b(const PassParams& p, int segment, cudaStream_t stream, int n
 
 cudaError_t shade_t(const PassParams& p, int segment, int block, cudaStream_t stream, int numSMs)
 {
+    if (p.nrc.query)
+        return shade_b<128, true>(p, segment, stream, numSMs);
     if (block == 64)
-        return shade_b<64>(p, segment, stream, numSMs);
+        return shade_b<64, false>(p, segment, stream, numSMs);
     if (block == 256)
-        return shade_b<256>(p, segment, stream, numSMs);
-    return shade_b<128>(p, segment, stream, numSMs);
+        return shade_b<256, false>(p, segment, stream, numSMs);
+    return shade_b<128, false>(p, segment, stream, numSMs);
+}
+
+// One thread per training path: walks its vertices backwards, replacing
+// each bounce factor f_i by the suffix radiance L_i = f_i * L_{i+1}
+// (L_V = the terminal radiance), and lists the vertices that are samples:
+// all of them when the path ended by leaving the scene, on an emitter or
+// by Russian roulette; when the depth limit cut it, those with at least
+// minSuffix vertices from themselves to the cut.
+__global__ void __launch_bounds__(256) k_nrc_targets(PassParams p)
+{
+    const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= uint32_t(p.nrc.groups))
+        return;
+    const float4 t = p.nrc.term[g];
+    const uint32_t flags = __float_as_uint(t.w);
+    if (!(flags & kNrcTermActive))
+        return;
+    const int V = int(flags & 255u);
+    const bool truncated = (flags & kNrcTermTruncated) != 0;
+    // a suffix cut by the depth limit counts only with minSuffix vertices
+    const int last = truncated ? V - p.nrc.minSuffix : V - 1;
+    const int count = last >= 0 ? last + 1 : 0;
+    unsigned base = count > 0 ? atomicAdd(&p.nrc.counters[1], unsigned(count)) : 0u;
+    float r = t.x, gg = t.y, b = t.z;
+    for (int i = V - 1; i >= 0; --i)
+    {
+        const size_t idx = size_t(i) * size_t(p.nrc.groups) + g;
+        float4 d = p.nrc.vtx[idx].d;
+        r = __fmul_rn(d.x, r);
+        gg = __fmul_rn(d.y, gg);
+        b = __fmul_rn(d.z, b);
+        // tag: vertex index << 24 | training path (group) index
+        p.nrc.vtx[idx].d = make_float4(r, gg, b, __uint_as_float((uint32_t(i) << 24) | g));
+        if (i <= last)
+            p.nrc.index[base + unsigned(last - i)] = int(idx);
+    }
 }
 
 }  // namespace
 
-cudaError_t launch_path_pass(const PassParams& p, int order, int counting, const PassShape& shape,
-                             cudaStream_t stream, int numSMs, const cudaEvent_t* extendEvents)
+cudaError_t launch_path_segments(const PassParams& p, int order, int counting, const PassShape& shape,
+                                 cudaStream_t stream, int numSMs, const cudaEvent_t* extendEvents)
 {
     k_generate<<<unsigned((p.nslots + 255) / 256), 256, 0, stream>>>(p);
     cudaError_t e = cudaGetLastError();
@@ -427,7 +586,29 @@ cudaError_t launch_path_pass(const PassParams& p, int order, int counting, const
         if ((e = shade_t(p, seg, shape.shadeBlock, stream, numSMs)) != cudaSuccess)
             return e;
     }
+    return cudaSuccess;
+}
+
+cudaError_t launch_path_accumulate(const PassParams& p, cudaStream_t stream)
+{
     k_accumulate<<<unsigned((p.npixels + 255) / 256), 256, 0, stream>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_path_pass(const PassParams& p, int order, int counting, const PassShape& shape,
+                             cudaStream_t stream, int numSMs, const cudaEvent_t* extendEvents)
+{
+    cudaError_t e = launch_path_segments(p, order, counting, shape, stream, numSMs, extendEvents);
+    if (e != cudaSuccess)
+        return e;
+    return launch_path_accumulate(p, stream);
+}
+
+cudaError_t launch_nrc_targets(const PassParams& p, cudaStream_t stream)
+{
+    if (p.nrc.groups <= 0)
+        return cudaSuccess;
+    k_nrc_targets<<<unsigned((p.nrc.groups + 255) / 256), 256, 0, stream>>>(p);
     return cudaGetLastError();
 }
 

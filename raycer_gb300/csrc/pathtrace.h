@@ -13,6 +13,7 @@
 #include <stdint.h>
 
 #include "kernels.h"
+#include "nrc_kernels.h"
 
 namespace rcx
 {
@@ -35,6 +36,8 @@ struct PathScene
     int maxPathLength;
     int rrDepth;          // 0 = no Russian roulette
     uint32_t frame;
+    int skyOn;            // misses return `sky` (GPU extension; the reference returns black)
+    float sky[3];
     uint64_t seed;
 };
 
@@ -46,6 +49,27 @@ struct PathChunk
     uint32_t pixels;            // whole pixels in the chunk
     uint64_t pixelLocalBegin;   // render-local index of the chunk's first pixel
 };
+
+// Neural-radiance-cache state of one pass (all pointers null: plain paths).
+// Slot s is a training path when s % trainStride == pick(s / trainStride)
+// (one random slot per run of trainStride slots); every other path ends at
+// the hit of segment termSegment with a cache lookup.
+struct NrcPass
+{
+    NrcRecord* query;     // cache lookups, [nslots]; tag = slot
+    NrcRecord* vtx;       // training vertices [segments][groups]; radiance = bounce factor
+    float4* term;         // per training path: terminal radiance; w = flags (below)
+    int* index;           // training samples (vertex record indices), [segments * groups]
+    unsigned* counters;   // [0] lookups, [1] training samples
+    int termSegment;
+    int trainStride;      // 0: no training paths
+    int groups;           // ceil(nslots / trainStride)
+    int minSuffix;        // vertices a suffix cut by the depth limit needs to be a sample
+    uint32_t trainKey;    // per-pass key of the training-slot choice
+};
+// NrcPass::term flags: vertex count | truncated << 8 | active << 9.
+constexpr uint32_t kNrcTermTruncated = 1u << 8;
+constexpr uint32_t kNrcTermActive = 1u << 9;
 
 struct PassParams
 {
@@ -65,6 +89,7 @@ struct PassParams
     int* chunkOf;    // slot -> chunk (written by generate)
     unsigned* counts;  // per segment: [queue count, extend head, shade head, unused]
     DevControl* ctl;
+    NrcPass nrc;
 };
 
 // Bytes of path state per slot (o, d, thr, res, hit, two queue entries, chunk id).
@@ -86,6 +111,14 @@ struct PassShape
 // each extend launch, or nullptr. Graph-capturable (no host reads).
 cudaError_t launch_path_pass(const PassParams& p, int order, int counting, const PassShape& shape,
                              cudaStream_t stream, int numSMs, const cudaEvent_t* extendEvents);
+// The same pass in two halves, for work between the last shade and the film
+// update (cache lookups): generate + segments, then accumulate.
+cudaError_t launch_path_segments(const PassParams& p, int order, int counting, const PassShape& shape,
+                                 cudaStream_t stream, int numSMs, const cudaEvent_t* extendEvents);
+cudaError_t launch_path_accumulate(const PassParams& p, cudaStream_t stream);
+// Training targets of the pass's training paths (radiance of each vertex's
+// suffix, written over the bounce factors) and the sample index list.
+cudaError_t launch_nrc_targets(const PassParams& p, cudaStream_t stream);
 
 // Reinhard / passthrough resolve of the film into out (float4 per pixel).
 // partials needs tone_partials_bytes(pixels) bytes.
@@ -93,5 +126,11 @@ size_t tone_partials_bytes(uint64_t pixels);
 cudaError_t launch_tonemap(const float4* film, uint64_t pixels, int type, int applyGamma, int shouldClamp,
                            double gamma, double key, void* partials, float4* out, cudaStream_t stream, int numSMs);
 cudaError_t launch_linear(const float4* film, uint64_t pixels, float4* out, cudaStream_t stream);
+// acc += film (float64); clear != 0 zeroes the film afterwards.
+cudaError_t launch_film_accumulate_f64(float4* film, uint64_t pixels, double4* acc, int clear, cudaStream_t stream);
+// Display-space RMSE of film vs truth (float64), result in device memory.
+size_t rmse_scratch_bytes();
+cudaError_t launch_rmse_f64(const float4* film, const double4* truth, uint64_t pixels, int applyGamma, int shouldClamp,
+                            double gamma, double key, void* scratch, double* result, cudaStream_t stream, int numSMs);
 
 }  // namespace rcx

@@ -67,6 +67,11 @@ rc_status grow(rc_tracer* h, void** ptr, size_t* cap, size_t bytes, const char* 
 namespace rcx
 {
 
+rc_status device_grow(rc_tracer* h, void** ptr, size_t* cap, size_t bytes, const char* what)
+{
+    return grow(h, ptr, cap, bytes, what);
+}
+
 void release_render_buffers(rc_tracer* h)
 {
     void** ptrs[] = { &h->dPath, reinterpret_cast<void**>(&h->dCounts), &h->dTone, &h->dImage, &h->dTables };
@@ -123,6 +128,9 @@ PathScene path_scene(const rc_tracer* h, uint64_t pixelStart)
     ps.maxPathLength = g.max_path_length;
     ps.rrDepth = g.russian_roulette_depth;
     ps.frame = h->frameIndex;
+    ps.skyOn = (g.flags & RC_GENERAL_SKY) ? 1 : 0;
+    for (int k = 0; k < 3; ++k)
+        ps.sky[k] = g.background[k];
     ps.seed = g.seed;
     return ps;
 }
@@ -209,6 +217,13 @@ rc_status render_path(rc_tracer* h, uint64_t pixelStart, uint64_t count, const v
     pp.numChunks = 1;
     pp.segments = g.max_path_length;
     PassShape shape;
+    const bool nrc = nrc_active(h);
+    if (nrc)
+    {
+        rc_status s = nrc_prepare(h, slots, g.max_path_length);
+        if (s != RC_OK)
+            return s;
+    }
 
     RC_CUDA_TRY(h, cudaMemsetAsync(h->dCtl, 0, sizeof(DevControl), h->stream), "reset control block");
     RC_CUDA_TRY(h, cudaEventRecord(h->ev0, h->stream), "record start event");
@@ -225,8 +240,23 @@ rc_status render_path(rc_tracer* h, uint64_t pixelStart, uint64_t count, const v
         pp.nslots = int(uint64_t(chunks[pass].pixels) * spp);
         RC_CUDA_TRY(h, cudaMemsetAsync(h->dCounts, 0, countsBytes, h->stream), "reset queue counters");
         const cudaEvent_t* ev = timeStages ? h->evPool.data() + pass * size_t(2 * g.max_path_length) : nullptr;
-        RC_CUDA_TRY(h, launch_path_pass(pp, h->order, h->counting, shape, h->stream, h->numSMs, ev),
+        if (!nrc)
+        {
+            RC_CUDA_TRY(h, launch_path_pass(pp, h->order, h->counting, shape, h->stream, h->numSMs, ev),
+                        "launch path-tracing pass");
+            continue;
+        }
+        nrc_pass_state(h, pp, uint32_t(pass));
+        RC_CUDA_TRY(h, launch_path_segments(pp, h->order, h->counting, shape, h->stream, h->numSMs, ev),
                     "launch path-tracing pass");
+        rc_status s = nrc_lookups(h, pp);
+        if (s == RC_OK)
+        {
+            RC_CUDA_TRY(h, launch_path_accumulate(pp, h->stream), "launch film update");
+            s = nrc_train_pass(h, pp);
+        }
+        if (s != RC_OK)
+            return s;
     }
     RC_CUDA_TRY(h, cudaEventRecord(h->ev1, h->stream), "record end event");
     DevControl ctl;
@@ -244,6 +274,12 @@ rc_status render_path(rc_tracer* h, uint64_t pixelStart, uint64_t count, const v
             cudaEventElapsedTime(&m, h->evPool[i], h->evPool[i + 1]);
             extendMs += double(m);
         }
+    }
+    if (nrc)
+    {
+        float tm = 0.0f;
+        cudaEventElapsedTime(&tm, h->nrc.evTrain0, h->nrc.evTrain1);
+        h->nrc.trainMs = double(tm);
     }
     h->stats.last_ms = double(ms);
     h->stats.stage_ms[0] = extendMs;
@@ -333,6 +369,47 @@ rc_status rc_read_linear(rc_tracer* h, float* out_rgba)
                                 h->stream),
                 "download linear image");
     RC_CUDA_TRY(h, cudaStreamSynchronize(h->stream), "read_linear");
+    return RC_OK;
+}
+
+rc_status rc_film_accumulate_f64(rc_tracer* h, double* d_acc, int32_t clear_film)
+{
+    if (!h)
+        return RC_INVALID_ARG;
+    if (!h->dFilm || !d_acc)
+        return fail(h, RC_NOT_READY, "film_accumulate_f64: no film or null accumulator");
+    if (reinterpret_cast<uintptr_t>(d_acc) & 31u)
+        return fail(h, RC_INVALID_ARG, "film_accumulate_f64: accumulator must be 32-byte aligned");
+    cudaSetDevice(h->device);
+    RC_CUDA_TRY(h,
+                launch_film_accumulate_f64(h->dFilm, h->filmPixels, reinterpret_cast<double4*>(d_acc), clear_film,
+                                           h->stream),
+                "launch float64 accumulation");
+    RC_CUDA_TRY(h, cudaStreamSynchronize(h->stream), "film_accumulate_f64");
+    return RC_OK;
+}
+
+rc_status rc_film_rmse_f64(rc_tracer* h, const double* d_truth, double* rmse)
+{
+    if (!h)
+        return RC_INVALID_ARG;
+    if (!h->dFilm || !d_truth || !rmse)
+        return fail(h, RC_NOT_READY, "film_rmse_f64: no film or null buffer");
+    if (reinterpret_cast<uintptr_t>(d_truth) & 31u)
+        return fail(h, RC_INVALID_ARG, "film_rmse_f64: truth must be 32-byte aligned");
+    cudaSetDevice(h->device);
+    rc_status s = grow(h, &h->dRmse, &h->capRmse, rmse_scratch_bytes() + 64, "allocate rmse scratch");
+    if (s != RC_OK)
+        return s;
+    // rmse_scratch_bytes() is a multiple of 8
+    double* dResult = reinterpret_cast<double*>(static_cast<char*>(h->dRmse) + rmse_scratch_bytes());
+    const rc_tonemapper& t = h->tonemapper;
+    RC_CUDA_TRY(h,
+                launch_rmse_f64(h->dFilm, reinterpret_cast<const double4*>(d_truth), h->filmPixels, t.apply_gamma,
+                                t.should_clamp, t.gamma, t.key, h->dRmse, dResult, h->stream, h->numSMs),
+                "launch rmse");
+    RC_CUDA_TRY(h, cudaMemcpyAsync(rmse, dResult, sizeof(double), cudaMemcpyDeviceToHost, h->stream), "read rmse");
+    RC_CUDA_TRY(h, cudaStreamSynchronize(h->stream), "film_rmse_f64");
     return RC_OK;
 }
 

@@ -170,6 +170,128 @@ __global__ void k_linear(const float4* __restrict__ film, uint64_t pixels, float
         out[i] = linear_of(film[i]);
 }
 
+// ---- high-spp ground truth and display-space RMSE (float64) ----
+
+__global__ void k_film_acc64(float4* __restrict__ film, uint64_t pixels, double4* __restrict__ acc, int clear)
+{
+    uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= pixels)
+        return;
+    float4 f = film[i];
+    double4 a = acc[i];
+    a.x += double(f.x);
+    a.y += double(f.y);
+    a.z += double(f.z);
+    a.w += double(f.w);
+    acc[i] = a;
+    if (clear)
+        film[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+}
+
+__device__ __forceinline__ double3 truth_linear(double4 t)
+{
+    return make_double3(t.x / t.w, t.y / t.w, t.z / t.w);
+}
+
+__global__ void __launch_bounds__(kToneBlock) k_truth_reduce(const double4* __restrict__ truth, uint64_t pixels,
+                                                            double2* __restrict__ partial)
+{
+    __shared__ double sSum[kToneBlock];
+    __shared__ double sMax[kToneBlock];
+    double sum = 0.0, mx = 0.0;
+    for (uint64_t i = uint64_t(blockIdx.x) * kToneBlock + threadIdx.x; i < pixels;
+         i += uint64_t(gridDim.x) * kToneBlock)
+    {
+        double3 c = truth_linear(truth[i]);
+        double L = luminance(c.x, c.y, c.z);
+        sum += log(0.01 + L);
+        mx = L > mx ? L : mx;
+    }
+    sSum[threadIdx.x] = sum;
+    sMax[threadIdx.x] = mx;
+    __syncthreads();
+    for (int s = kToneBlock / 2; s > 0; s >>= 1)
+    {
+        if (int(threadIdx.x) < s)
+        {
+            sSum[threadIdx.x] += sSum[threadIdx.x + s];
+            sMax[threadIdx.x] = fmax(sMax[threadIdx.x], sMax[threadIdx.x + s]);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        partial[blockIdx.x] = make_double2(sSum[0], sMax[0]);
+}
+
+// Display value of a linear colour: Reinhard with the truth's statistics,
+// clamp, gamma (pow, not the reference's fastPow: the metric is smooth).
+__device__ __forceinline__ double3 display(double r, double g, double b, const ToneParams& p, int applyGamma,
+                                           int shouldClamp, double invGamma)
+{
+    double L = luminance(r, g, b);
+    if (!(L > 0.0))
+        return make_double3(0.0, 0.0, 0.0);
+    double sL = p.scale * L;
+    double cs = (sL * (1.0 + sL * p.maxL2Inv) / (1.0 + sL)) / L;
+    r *= cs;
+    g *= cs;
+    b *= cs;
+    if (shouldClamp)
+    {
+        r = clamp01(r);
+        g = clamp01(g);
+        b = clamp01(b);
+    }
+    if (applyGamma)
+    {
+        r = r > 0.0 ? pow(r, invGamma) : 0.0;
+        g = g > 0.0 ? pow(g, invGamma) : 0.0;
+        b = b > 0.0 ? pow(b, invGamma) : 0.0;
+    }
+    return make_double3(r, g, b);
+}
+
+__global__ void __launch_bounds__(kToneBlock) k_rmse_apply(const float4* __restrict__ film,
+                                                          const double4* __restrict__ truth, uint64_t pixels,
+                                                          const ToneParams* __restrict__ tp, int applyGamma,
+                                                          int shouldClamp, double invGamma,
+                                                          double* __restrict__ partial)
+{
+    __shared__ double sSum[kToneBlock];
+    const ToneParams p = *tp;
+    double sum = 0.0;
+    for (uint64_t i = uint64_t(blockIdx.x) * kToneBlock + threadIdx.x; i < pixels;
+         i += uint64_t(gridDim.x) * kToneBlock)
+    {
+        float4 f = film[i];
+        double w = double(f.w);
+        double3 a = display(double(f.x) / w, double(f.y) / w, double(f.z) / w, p, applyGamma, shouldClamp, invGamma);
+        double3 t = truth_linear(truth[i]);
+        double3 b = display(t.x, t.y, t.z, p, applyGamma, shouldClamp, invGamma);
+        sum += (a.x - b.x) * (a.x - b.x) + (a.y - b.y) * (a.y - b.y) + (a.z - b.z) * (a.z - b.z);
+    }
+    sSum[threadIdx.x] = sum;
+    __syncthreads();
+    for (int s = kToneBlock / 2; s > 0; s >>= 1)
+    {
+        if (int(threadIdx.x) < s)
+            sSum[threadIdx.x] += sSum[threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        partial[blockIdx.x] = sSum[0];
+}
+
+__global__ void k_rmse_combine(const double* __restrict__ partial, int blocks, uint64_t pixels, double* out)
+{
+    if (threadIdx.x != 0)
+        return;
+    double s = 0.0;
+    for (int b = 0; b < blocks; ++b)
+        s += partial[b];
+    *out = sqrt(s / (3.0 * double(pixels)));
+}
+
 int reduce_blocks(uint64_t pixels, int numSMs)
 {
     uint64_t need = (pixels + kToneBlock - 1) / kToneBlock;
@@ -200,6 +322,31 @@ cudaError_t launch_tonemap(const float4* film, uint64_t pixels, int type, int ap
     double invGamma = 1.0 / gamma;  // ReinhardToneMapper.cpp:61
     k_tone_apply<<<unsigned((pixels + kToneBlock - 1) / kToneBlock), kToneBlock, 0, stream>>>(
         film, pixels, tp, applyGamma, shouldClamp, invGamma, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_film_accumulate_f64(float4* film, uint64_t pixels, double4* acc, int clear, cudaStream_t stream)
+{
+    k_film_acc64<<<unsigned((pixels + 255) / 256), 256, 0, stream>>>(film, pixels, acc, clear);
+    return cudaGetLastError();
+}
+
+size_t rmse_scratch_bytes() { return sizeof(double2) * 4096 + sizeof(ToneParams) + sizeof(double) * 4097; }
+
+cudaError_t launch_rmse_f64(const float4* film, const double4* truth, uint64_t pixels, int applyGamma, int shouldClamp,
+                            double gamma, double key, void* scratch, double* result, cudaStream_t stream, int numSMs)
+{
+    int blocks = reduce_blocks(pixels, numSMs);
+    if (blocks > 4096)
+        blocks = 4096;
+    double2* part = static_cast<double2*>(scratch);
+    ToneParams* tp = reinterpret_cast<ToneParams*>(part + 4096);
+    double* sse = reinterpret_cast<double*>(tp + 1);
+    k_truth_reduce<<<blocks, kToneBlock, 0, stream>>>(truth, pixels, part);
+    k_tone_combine<<<1, kToneBlock, 0, stream>>>(part, blocks, pixels, key, tp);
+    k_rmse_apply<<<blocks, kToneBlock, 0, stream>>>(film, truth, pixels, tp, applyGamma, shouldClamp, 1.0 / gamma,
+                                                    sse);
+    k_rmse_combine<<<1, 32, 0, stream>>>(sse, blocks, pixels, result);
     return cudaGetLastError();
 }
 

@@ -492,6 +492,9 @@ void rc_destroy(rc_tracer* h)
     release_scene(h);
     release_film(h);
     release_render_buffers(h);
+    nrc_release(h);
+    if (h->dRmse)
+        cudaFree(h->dRmse);
     if (h->dTmpA)
         cudaFree(h->dTmpA);
     if (h->dTmpB)
@@ -688,8 +691,8 @@ rc_status rc_set_general(rc_tracer* h, const rc_general* g)
         return fail(h, RC_UNSUPPORTED, "set_general: only the box filter is supported");
     if (!(g->filter_radius[0] > 0.0f) || !(g->filter_radius[1] > 0.0f))
         return fail(h, RC_INVALID_ARG, "set_general: filter radius must be > 0");
-    if (g->russian_roulette_depth < 0 || g->reserved != 0)
-        return fail(h, RC_INVALID_ARG, "set_general: invalid russian_roulette_depth / reserved");
+    if (g->russian_roulette_depth < 0 || (g->flags & ~int32_t(RC_GENERAL_SKY)) != 0)
+        return fail(h, RC_INVALID_ARG, "set_general: invalid russian_roulette_depth / flags");
     h->general = *g;
     return RC_OK;
 }

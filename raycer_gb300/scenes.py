@@ -332,3 +332,102 @@ def batch_scenes(seed: int = 3, count: int = 64, n_min: float = 1e3, n_max: floa
         ms = int(round(math.sqrt(spp)))
         out.append(room_with_extra(seed * 1000 + i, n, res, res, ms))
     return out
+
+
+# ---------------------------------------------------------------------------
+# Heightfield + instanced blobs (radiance-cache workload).
+
+
+def icosphere(level: int) -> np.ndarray:
+    """Unit icosphere triangles (20 * 4^level, each 9 floats, outward winding)."""
+    t = (1.0 + math.sqrt(5.0)) / 2.0
+    verts = [(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t), (0, -1, -t), (0, 1, -t),
+             (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)]
+    faces = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4), (11, 10, 2),
+             (10, 7, 6), (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9), (4, 9, 5), (2, 4, 11),
+             (6, 2, 10), (8, 6, 7), (9, 8, 1)]
+    v = np.array(verts, np.float64)
+    v /= np.linalg.norm(v, axis=1, keepdims=True)
+    tris = v[np.array(faces)]                        # (F, 3, 3)
+    for _ in range(level):
+        a, b, c = tris[:, 0], tris[:, 1], tris[:, 2]
+        ab = a + b
+        bc = b + c
+        ca = c + a
+        ab /= np.linalg.norm(ab, axis=1, keepdims=True)
+        bc /= np.linalg.norm(bc, axis=1, keepdims=True)
+        ca /= np.linalg.norm(ca, axis=1, keepdims=True)
+        tris = np.concatenate([np.stack([a, ab, ca], 1), np.stack([ab, b, bc], 1), np.stack([ca, bc, c], 1),
+                               np.stack([ab, bc, ca], 1)])
+    return tris.reshape(-1, 9)
+
+
+def blob_mesh(seed: int = 5, level: int = 5, amplitude: float = 0.35) -> np.ndarray:
+    """A random blob: an icosphere (20 * 4^level triangles; level 5 = 20,480)
+    whose vertices move radially by a 3-octave value-noise field."""
+    tris = icosphere(level).reshape(-1, 3)
+    n = fbm_noise(seed, 3, 2.0, 0.5, tris[:, 0] * 1.7 + 11.0, tris[:, 1] * 1.7 + 13.0, tris[:, 2] * 1.7 + 17.0)
+    r = 1.0 + amplitude * (n / 1.75 - 0.5)
+    return (tris * r[:, None]).reshape(-1, 9)
+
+
+def _random_rotations(rng, count):
+    u1, u2, u3 = rng.random(count), rng.random(count), rng.random(count)
+    # uniform unit quaternions (Shoemake)
+    a = np.sqrt(1 - u1)
+    b = np.sqrt(u1)
+    w, x = a * np.sin(2 * math.pi * u2), a * np.cos(2 * math.pi * u2)
+    y, z = b * np.sin(2 * math.pi * u3), b * np.cos(2 * math.pi * u3)
+    R = np.empty((count, 3, 3))
+    R[:, 0, 0] = 1 - 2 * (y * y + z * z)
+    R[:, 0, 1] = 2 * (x * y - z * w)
+    R[:, 0, 2] = 2 * (x * z + y * w)
+    R[:, 1, 0] = 2 * (x * y + z * w)
+    R[:, 1, 1] = 1 - 2 * (x * x + z * z)
+    R[:, 1, 2] = 2 * (y * z - x * w)
+    R[:, 2, 0] = 2 * (x * z - y * w)
+    R[:, 2, 1] = 2 * (y * z + x * w)
+    R[:, 2, 2] = 1 - 2 * (x * x + y * y)
+    return R
+
+
+def heightfield_blobs_scene(instances: int = 200, blob_level: int = 5, seed: int = 4, hf_nx: int = 1024,
+                            hf_nz: int = 512, width: int = 1920, height: int = 1080,
+                            sky=(1.0, 1.0, 1.0)) -> SceneDesc:
+    """The radiance-cache workload: the 1,045,506-triangle heightfield (value
+    noise seed 2) plus `instances` copies of one 20,480-triangle random blob at
+    uniform random positions over the terrain, uniform random rotations,
+    scale U(0.25, 0.6) and albedo U(0.1, 0.9)^3, flattened to world-space
+    triangles. Lit by a uniform sky: a path that escapes returns `sky`."""
+    hf = heightfield_scene(seed=2, nx=hf_nx, nz=hf_nz, width=width, height=height)
+    blob = blob_mesh(seed=seed, level=blob_level).reshape(-1, 3, 3)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    R = _random_rotations(rng, instances)
+    px = -9.0 + 18.0 * rng.random(instances)
+    pz = -4.5 + 9.0 * rng.random(instances)
+    scale = 0.25 + 0.35 * rng.random(instances)
+    albedo = (0.1 + 0.8 * rng.random((instances, 3))).astype(np.float32).astype(np.float64)
+    # terrain height under each instance, from the vertex grid
+    g = hf.vertices.reshape(hf_nz - 1, hf_nx - 1, 2, 9)[:, :, 0, 0:3]   # first vertex of each cell's first tri
+    ix = np.clip(((px + 10.0) / 20.0 * (hf_nx - 1)).astype(int), 0, hf_nx - 2)
+    iz = np.clip(((pz + 5.0) / 10.0 * (hf_nz - 1)).astype(int), 0, hf_nz - 2)
+    py = g[iz, ix, 1] + scale * 0.6
+    world = np.einsum("kij,tvj->ktvi", R, blob) * scale[:, None, None, None]
+    world += np.stack([px, py, pz], axis=1)[:, None, None, :]
+    bv = _f32(world.reshape(-1, 9))
+    mats = [Material(diffuse=(0.6, 0.6, 0.6))] + [Material(diffuse=tuple(float(c) for c in a)) for a in albedo]
+    midx = np.concatenate([np.zeros(hf.triangle_count, np.uint32),
+                           np.repeat(np.arange(1, instances + 1, dtype=np.uint32), blob.shape[0])])
+    return SceneDesc(
+        name=f"heightfield + {instances} blobs x {blob.shape[0]} tris",
+        vertices=np.concatenate([hf.vertices, bv]),
+        material_index=midx,
+        materials=mats,
+        camera=hf.camera,
+        width=width,
+        height=height,
+        light_direction=None,
+        max_leaf_size=4,
+        settings=dict(tracer="path", max_path_length=12, multi_sample_count_sqrt=1, path_sample_count=1,
+                      sampler="cmj", miss_radiance=tuple(sky)),
+    )

@@ -86,6 +86,10 @@ def general_record(desc: SceneDesc, seed: int = 1) -> N.rc_general:
     g.multi_sampler_type = {"cmj": N.RC_SAMPLER_CMJ, "random": N.RC_SAMPLER_RANDOM,
                             "center": N.RC_SAMPLER_CENTER}[s.get("sampler", "cmj")]
     g.russian_roulette_depth = int(s.get("russian_roulette_depth", 0))
+    if s.get("miss_radiance") is not None:
+        # GPU extension: escaping paths see a uniform sky of this radiance
+        g.flags |= N.RC_GENERAL_SKY
+        g.background[:] = [float(x) for x in s["miss_radiance"]]
     g.seed = int(seed)
     return g
 

@@ -1,0 +1,203 @@
+"""Radiance cache on the GPU: encoding, inference, gradients and Adam vs the
+CPU oracle (oracle/nrc64.cpp); training; the cache inside PATH renders."""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import oracle
+from raycer_gb300 import scenes
+from raycer_gb300.nrc import GroundTruth, RadianceCache, unpack_layers
+from raycer_gb300.tracer import CudaTracer, TracerState, general_record
+
+from helpers import nrc_box, nrc_init_params, nrc_queries, nrc_smooth_targets
+
+pytestmark = pytest.mark.gpu
+
+LO, HI = (-10.0, -2.0, -5.0), (10.0, 3.0, 5.0)
+BOX = nrc_box(LO, HI)
+
+
+@pytest.fixture(scope="module")
+def cache():
+    t = CudaTracer(0)
+    c = RadianceCache(t, box_min=LO, box_max=HI, seed=1)
+    yield c
+    t.close()
+
+
+def test_encoding_matches_oracle(cache):
+    q = nrc_queries(1000, seed=1, lo=LO, hi=HI)
+    gpu = cache.encode(q)
+    ref = oracle.nrc_features(q, BOX)
+    # BF16 rounding (2^-9 relative) + the float32 phase of the 2^11 pi terms
+    assert np.all(np.abs(gpu - ref) <= np.abs(ref) * 2.0 ** -8 + 1.5e-3)
+    assert np.all(gpu[:, 102] == 1.0) and np.all(gpu[:, 103:] == 0.0)
+
+
+def test_inference_matches_oracle(cache):
+    w = nrc_init_params(seed=5)
+    cache.params = w
+    q = nrc_queries(5003, seed=2, lo=LO, hi=HI)  # not a multiple of the 16-query tile
+    gpu = cache.infer(q).astype(np.float64)
+    emu = oracle.nrc_forward(w, q, BOX, emulate=True)
+    pure = oracle.nrc_forward(w, q, BOX)
+    rel_e = np.abs(gpu - emu) / np.abs(emu)
+    rel_p = np.abs(gpu - pure) / np.abs(pure)
+    # same rounding points as the oracle's BF16 emulation: float32 vs float64 sums only
+    assert np.quantile(rel_e, 0.99) < 2e-3 and rel_e.max() < 2e-2, (np.quantile(rel_e, 0.99), rel_e.max())
+    # against the float64 network: BF16 weights and activations
+    assert np.median(rel_p) < 2e-2 and rel_p.max() < 0.2, (np.median(rel_p), rel_p.max())
+
+
+@pytest.mark.parametrize("n", [16, 4100, 16384])
+def test_gradient_matches_oracle(cache, n):
+    w = nrc_init_params(seed=6)
+    cache.params = w
+    q = nrc_queries(n, seed=3, lo=LO, hi=HI)
+    t = nrc_smooth_targets(q)
+    g, loss = cache.gradient(q, t)
+    ge, le = oracle.nrc_gradient(w, q, t, BOX, emulate=True)
+    gp, lp = oracle.nrc_gradient(w, q, t, BOX)
+    assert abs(loss - le) <= 2e-3 * le + 1e-7
+    assert abs(loss - lp) <= 0.05 * lp
+    assert np.all(g[20480 + 3 * 64:] == 0.0)
+    for layer, (a, b, c) in enumerate(zip(unpack_layers(g.astype(np.float64)), unpack_layers(ge), unpack_layers(gp))):
+        a, b, c = a[:3] if layer == 4 else a, b[:3] if layer == 4 else b, c[:3] if layer == 4 else c
+        err_e = np.linalg.norm(a - b) / np.linalg.norm(b)
+        cos_p = float(np.sum(a * c) / (np.linalg.norm(a) * np.linalg.norm(c)))
+        assert err_e < 1e-2, (layer, err_e)
+        assert cos_p > 0.98, (layer, cos_p)
+
+
+def test_adam_steps_match_oracle(cache):
+    w = nrc_init_params(seed=7)
+    cache.params = w
+    q = nrc_queries(4096, seed=4, lo=LO, hi=HI)
+    t = nrc_smooth_targets(q)
+    ge, _ = oracle.nrc_gradient(w, q, t, BOX, emulate=True)
+    cache.train(q, t, steps=1)
+    w1 = cache.params
+    z = np.zeros_like(w)
+    exp1, m1, v1 = oracle.nrc_adam(w, z, z, ge.astype(np.float32), 1)
+    d = np.abs(w1 - exp1)
+    big = np.abs(ge) > 1e-3 * np.abs(ge).max()
+    # the first step moves every weight by -lr * sign(g): agreement wherever
+    # the gradient is not at the rounding level
+    assert np.mean(d[big] < 1e-5) > 0.995
+    assert np.all(np.abs(w1 - w) <= 1e-2 * (1 + 1e-3) + 1e-6)
+    assert np.all(w1[20480 + 3 * 64:] == 0.0)
+
+
+def test_training_reduces_loss(cache):
+    cache.params = nrc_init_params(seed=8)
+    q = nrc_queries(16384, seed=5, lo=LO, hi=HI)
+    t = nrc_smooth_targets(q)
+    losses = cache.train(q, t, steps=300)
+    assert np.all(np.isfinite(losses))
+    assert losses[-1] < 0.1 * losses[0], (losses[0], losses[-1])
+    qh = nrc_queries(4096, seed=6, lo=LO, hi=HI)
+    pred = cache.infer(qh)
+    th = nrc_smooth_targets(qh)
+    assert np.median(np.abs(pred - th) / th) < 0.1
+
+
+# ---------------------------------------------------------------------------
+# The cache inside PATH renders.
+
+
+def nrc_scene(width=128, height=72):
+    return scenes.heightfield_blobs_scene(instances=12, blob_level=3, hf_nx=96, hf_nz=48, width=width,
+                                          height=height)
+
+
+def render_film(sc, seed, frames=1, cache_cfg=None, read_cache=None):
+    with CudaTracer(0) as t:
+        t.initializeBuffers(sc, seed=seed)
+        t.initializeImageBuffers(sc.width, sc.height)
+        c = RadianceCache(t, **cache_cfg) if cache_cfg is not None else None
+        st = TracerState(scene=sc, filmWidth=sc.width, filmHeight=sc.height, pixelCount=sc.width * sc.height)
+        for _ in range(frames):
+            t.run(st)
+        film = t.read_film()
+        extra = read_cache(c) if (read_cache and c) else None
+    return film, extra
+
+
+def test_render_without_termination_equals_plain():
+    sc = nrc_scene()
+    plain, _ = render_film(sc, seed=3, frames=2)
+    # lookups never happen (segment 99) and 1 slot in 16 records a training path
+    late, _ = render_film(sc, seed=3, frames=2, cache_cfg=dict(terminate_segment=99, train_steps=2))
+    # every slot is a training path
+    full, _ = render_film(sc, seed=3, frames=2, cache_cfg=dict(train_stride=1, train_steps=1))
+    assert np.array_equal(plain, late)
+    assert np.array_equal(plain, full)
+
+
+def test_sky_radiance_reaches_the_film():
+    sc = nrc_scene(64, 36)
+    lit, _ = render_film(sc, seed=2)
+    sc.settings["miss_radiance"] = None
+    dark, _ = render_film(sc, seed=2)
+    assert lit[:, :3].mean() > 0.05
+    assert np.all(dark[:, :3] == 0.0)  # no emitters: the reference's miss returns black
+
+
+def test_training_targets_are_path_radiance():
+    """With every slot a training path, vertex 0's target is that pixel's plain
+    path value (the film at 1 sample per pixel)."""
+    sc = nrc_scene()
+    film, samples = render_film(sc, seed=4, cache_cfg=dict(train_stride=1, train_steps=0),
+                                read_cache=lambda c: c.samples())
+    vi, gi = RadianceCache.sample_tags(samples)
+    assert samples.shape[0] > film.shape[0] // 2
+    v0 = vi == 0
+    tgt = samples[v0, 12:15].astype(np.float64)
+    ref = film[gi[v0], :3].astype(np.float64)
+    np.testing.assert_allclose(tgt, ref, rtol=2e-5, atol=1e-7)
+    # queries lie on surfaces with unit directions and normals
+    np.testing.assert_allclose(np.linalg.norm(samples[:, 3:6], axis=1), 1.0, atol=1e-5)
+    np.testing.assert_allclose(np.linalg.norm(samples[:, 6:9], axis=1), 1.0, atol=1e-4)
+    assert np.all((samples[:, 9:12] >= 0.1 - 1e-6) & (samples[:, 9:12] <= 0.9 + 1e-6))
+    # at most max_path_length vertices per path, each counted once
+    assert vi.max() < sc.settings["max_path_length"]
+    assert len(set(zip(vi.tolist(), gi.tolist()))) == samples.shape[0]
+
+
+def test_trained_cache_beats_untrained_cache():
+    """At equal frames, the trained cache's image is much closer to the
+    float64 high-spp ground truth than the same renderer's with an untrained
+    cache (the gain of training), and its error keeps falling."""
+    sc = nrc_scene()
+    with CudaTracer(0) as t:
+        t.initializeBuffers(sc, seed=9)
+        t.initializeImageBuffers(sc.width, sc.height)
+        st = TracerState(scene=sc, filmWidth=sc.width, filmHeight=sc.height, pixelCount=sc.width * sc.height)
+        gt = GroundTruth(t)
+        for _ in range(256):
+            t.run(st)
+            gt.add_film(clear_film=True)
+        # the renders below restart the frame counter: a different seed keeps
+        # their samples independent of the ground truth's
+        t.set_general(general_record(sc, seed=10))
+
+        def rmse_after(frames, **cfg):
+            t.clear()
+            c = RadianceCache(t, **cfg)
+            for _ in range(frames):
+                t.run(st)
+            r = gt.rmse()
+            c.set_enabled(False)
+            return r
+
+        untrained = rmse_after(64, train_steps=0, seed=3)
+        trained = rmse_after(64, seed=3)
+        plain = None
+        t.clear()
+        for _ in range(64):
+            t.run(st)
+        plain = gt.rmse()
+    print(f"rmse after 64 frames: trained cache {trained:.4f}, untrained {untrained:.4f}, plain {plain:.4f}")
+    assert trained < 0.5 * untrained
