@@ -52,8 +52,13 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--order", choices=["nearest", "reference"], default="nearest")
-    ap.add_argument("--workload", choices=["raycast", "batch"], default="raycast",
-                    help="raycast: the 1080p heightfield frame (default); batch: 64 rooms in one graph launch")
+    ap.add_argument("--workload", choices=["raycast", "batch", "nrc"], default="raycast",
+                    help="raycast: the 1080p heightfield frame (default); batch: 64 rooms in one graph launch; "
+                         "nrc: time to display RMSE 0.01, radiance cache vs plain path tracing")
+    ap.add_argument("--gt-spp", type=int, default=4096, help="nrc: ground-truth samples per pixel")
+    ap.add_argument("--scale", type=float, default=1.0, help="nrc: film scale (1 = 1920x1080)")
+    ap.add_argument("--terminate-segment", type=int, default=2,
+                    help="nrc: paths end into the cache at the hit of this segment")
     return ap.parse_args()
 
 
@@ -445,11 +450,58 @@ def run_batch(args, rank, world):
     return 0
 
 
+def run_nrc(args, rank, world):
+    """Heightfield + 200 blob instances (5.1M tris), 1080p, 1 spp per frame,
+    depth 12, sky-lit: wall time until the display RMSE against a float64
+    4096-spp plain-tracer ground truth reaches 0.01, plain tracer vs the
+    radiance-cache tracer (paths end into the cache at the hit of segment 2;
+    1 slot in 16 trains; 4 Adam steps of 16384 samples per frame)."""
+    if rank != 0:
+        return 0
+    from raycer_gb300 import scenes
+    from raycer_gb300.nrc_eval import time_to_rmse
+
+    w, h = int(round(1920 * args.scale)), int(round(1080 * args.scale))
+    t0 = time.perf_counter()
+    sc = scenes.heightfield_blobs_scene(width=w, height=h)
+    build_s = time.perf_counter() - t0
+    res = time_to_rmse(sc, target=0.01, gt_spp=args.gt_spp, max_frames=4096, max_seconds=90.0,
+                       cache_config=dict(terminate_segment=args.terminate_segment),
+                       progress=lambda m: print(m, file=sys.stderr, flush=True))
+
+    def run_dict(r):
+        return {"frames": r.frames, "seconds": round(r.seconds, 3), "gpu_ms": round(r.gpu_ms, 1),
+                "rmse": round(r.rmse, 5), "reached": r.reached,
+                "mrays_per_s": round(r.rays / max(r.seconds, 1e-9) / 1e6, 1)}
+
+    line = {
+        "metric": "time-to-RMSE 0.01 (s), radiance cache", "value": round(res.cache.seconds, 3), "unit": "s",
+        "n_gpus": 1, "steps": res.cache.frames, "warmup": 0,
+        "ms_per_step": round(1e3 * res.cache.seconds / max(res.cache.frames, 1), 3),
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "bf16 (MLP) / f32 (paths)",
+        "data": "synthetic (seeded heightfield + blob instances)",
+        "config": {"workload": f"radiance cache: heightfield + 200 blobs, {sc.triangle_count} tris, {w}x{h}, "
+                               "1 spp/frame, depth 12, sky-lit",
+                   "gt_spp": res.gt_spp, "gt_seconds": round(res.gt_seconds, 1), "scene_build_s": round(build_s, 1),
+                   "terminate_segment": args.terminate_segment},
+        "plain": run_dict(res.plain), "cache": run_dict(res.cache),
+        "time_ratio_cache_over_plain": (round(res.cache.seconds / res.plain.seconds, 3)
+                                        if res.plain.reached and res.cache.reached else None),
+        "cache_stats": {k: (round(v, 4) if isinstance(v, float) else v) for k, v in res.cache_stats.items()},
+        "curves": {"plain": res.plain.curve[::max(1, len(res.plain.curve) // 24)],
+                   "cache": res.cache.curve[::max(1, len(res.cache.curve) // 24)]},
+    }
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     args = parse_args()
     rank, local_rank, world = dist_env()
     if args.workload == "batch":
         return run_batch(args, rank, world)
+    if args.workload == "nrc":
+        return run_nrc(args, rank, world)
     if args.impl == "reference":
         return run_reference(args, rank, world)
     return run_ours(args, rank, local_rank, world)

@@ -166,38 +166,59 @@ def test_training_targets_are_path_radiance():
     assert len(set(zip(vi.tolist(), gi.tolist()))) == samples.shape[0]
 
 
-def test_trained_cache_beats_untrained_cache():
-    """At equal frames, the trained cache's image is much closer to the
-    float64 high-spp ground truth than the same renderer's with an untrained
-    cache (the gain of training), and its error keeps falling."""
+def zero_cache_params() -> np.ndarray:
+    """Weights whose output is exp(-30) ~ 0 everywhere: one hidden unit carries
+    the constant input through the ReLU layers and the output layer scales
+    it by -30. A tracer with this cache ends its paths at the lookup with no
+    estimate of the rest: the method without the network."""
+    w = np.zeros(20992, np.float32)
+    w[0 * 128 + 102] = 1.0           # W1[0][102]: the constant feature
+    for off in (8192, 12288, 16384):  # W2..W4[0][0]
+        w[off] = 1.0
+    for c in range(3):               # W5[c][0]
+        w[20480 + c * 64] = -30.0
+    return w
+
+
+def test_trained_cache_gain():
+    """At equal frames, against a float64 high-spp ground truth: the trained
+    cache's image is far closer than the same tracer's with a zero cache
+    (paths cut at the lookup) and than with an untrained cache, and not
+    worse than plain path tracing beyond noise."""
     sc = nrc_scene()
     with CudaTracer(0) as t:
         t.initializeBuffers(sc, seed=9)
         t.initializeImageBuffers(sc.width, sc.height)
         st = TracerState(scene=sc, filmWidth=sc.width, filmHeight=sc.height, pixelCount=sc.width * sc.height)
         gt = GroundTruth(t)
-        for _ in range(256):
+        for _ in range(512):
             t.run(st)
             gt.add_film(clear_film=True)
         # the renders below restart the frame counter: a different seed keeps
         # their samples independent of the ground truth's
         t.set_general(general_record(sc, seed=10))
 
-        def rmse_after(frames, **cfg):
+        def rmse_after(frames, params=None, **cfg):
             t.clear()
             c = RadianceCache(t, **cfg)
+            if params is not None:
+                c.params = params
             for _ in range(frames):
                 t.run(st)
             r = gt.rmse()
             c.set_enabled(False)
             return r
 
-        untrained = rmse_after(64, train_steps=0, seed=3)
-        trained = rmse_after(64, seed=3)
-        plain = None
+        frames = 128
+        zero = rmse_after(frames, params=zero_cache_params(), train_steps=0)
+        untrained = rmse_after(frames, train_steps=0, seed=3)
+        trained = rmse_after(frames, seed=3)
         t.clear()
-        for _ in range(64):
+        for _ in range(frames):
             t.run(st)
         plain = gt.rmse()
-    print(f"rmse after 64 frames: trained cache {trained:.4f}, untrained {untrained:.4f}, plain {plain:.4f}")
-    assert trained < 0.5 * untrained
+    print(f"rmse after {frames} frames: trained cache {trained:.4f}, untrained {untrained:.4f}, "
+          f"zero cache {zero:.4f}, plain {plain:.4f}")
+    assert trained < 0.5 * zero
+    assert trained < untrained
+    assert trained < 1.15 * plain
