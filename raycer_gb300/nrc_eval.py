@@ -88,3 +88,39 @@ def time_to_rmse(scene, target: float = 0.01, gt_spp: int = 4096, max_frames: in
         if progress:
             progress(f"cache: {cached.frames} frames, {cached.seconds:.2f} s, rmse {cached.rmse:.4f}")
         return Result(target, gt_spp, gt_seconds, plain, cached, stats)
+
+
+def render_frames(scene, frames: int, cache_config: dict | None = None, seed: int = 1, device: int = 0) -> dict:
+    """Renders `frames` frames with the cache (no ground truth); for profiling."""
+    with CudaTracer(device) as t:
+        t.initializeBuffers(scene, seed=seed)
+        t.initializeImageBuffers(scene.width, scene.height)
+        st = TracerState(scene=scene, filmWidth=scene.width, filmHeight=scene.height,
+                         pixelCount=scene.width * scene.height)
+        cache = RadianceCache(t, **(cache_config or {}))
+        for _ in range(frames):
+            t.run(st)
+        return cache.stats()
+
+
+def main(argv=None) -> int:
+    import argparse
+    import json
+    import sys
+
+    from . import scenes
+
+    ap = argparse.ArgumentParser(description="radiance-cache frames on the heightfield + blobs scene")
+    ap.add_argument("--scale", type=float, default=0.5, help="film scale (1 = 1920x1080)")
+    ap.add_argument("--frames", type=int, default=4)
+    ap.add_argument("--instances", type=int, default=200)
+    args = ap.parse_args(argv)
+    w, h = int(round(1920 * args.scale)), int(round(1080 * args.scale))
+    sc = scenes.heightfield_blobs_scene(instances=args.instances, width=w, height=h)
+    print(json.dumps(render_frames(sc, args.frames)))
+    sys.stdout.flush()
+    return 0
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())
