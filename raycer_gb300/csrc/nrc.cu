@@ -8,14 +8,14 @@
 // leave registers. Weights sit in shared memory with rows padded by 8
 // elements (no bank conflicts on the B-fragment loads).
 //
-// Training (k_nrc_train): per warp, a 16-sample tile runs forward with the
-// activations stored to its shared-memory scratch (BF16), then backward:
-// relative-L2 loss gradient, dH = dZ W (mma), dZ = dH * relu', and
-// dW = dZ^T H (mma over the 16 samples) added into a per-block FP32 gradient
-// array in shared memory. Each block writes its gradient sum to its own
-// partial buffer; k_nrc_adam sums the partials in a fixed order, so the
-// step is independent of block scheduling, and applies Adam to the FP32
-// master weights, refreshing the BF16 copy.
+// Training (k_nrc_train): a block of 8 warps takes 128 samples at a time;
+// forward and the backward chain dZ_{l-1} = (dZ_l W_l) * relu' run per warp
+// on its 16 rows (register chains, activations and gradients also stored to
+// shared memory as BF16), and dW_l = dZ_l^T H_{l-1} is a block-wide product
+// over the 128 samples with every warp owning fixed dW tiles in registers
+// (see the comment at k_nrc_train). Each block writes its gradient sum once
+// to its own partial buffer; k_nrc_adam sums the partials in a fixed order
+// and applies Adam to the FP32 master weights, refreshing the BF16 copy.
 
 #include <cuda_bf16.h>
 
@@ -42,18 +42,6 @@ constexpr int kS4 = kS3 + kNrcHidden * kLdH;   // 17920
 constexpr int kS5 = kS4 + kNrcHidden * kLdH;   // 22528
 constexpr int kSmemW = kS5 + kNrcOutPad * kLdH;  // 23104 elements = 46,208 B
 
-// per-warp training scratch (elements of BF16)
-constexpr int kLdT = 16 + 8;  // dZ5: 16 columns
-constexpr int kScH0 = 0;
-constexpr int kScH1 = kScH0 + 16 * kLd1;
-constexpr int kScH2 = kScH1 + 16 * kLdH;
-constexpr int kScH3 = kScH2 + 16 * kLdH;
-constexpr int kScH4 = kScH3 + 16 * kLdH;
-constexpr int kScZa = kScH4 + 16 * kLdH;
-constexpr int kScZb = kScZa + 16 * kLdH;
-constexpr int kScZ5 = kScZb + 16 * kLdH;
-constexpr int kScratch = kScZ5 + 16 * kLdT;  // per warp
-
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
 
 // Copies the packed [out][in] weights into the padded shared-memory layout.
@@ -77,11 +65,6 @@ __device__ void load_weights(__nv_bfloat16* s, const __nv_bfloat16* __restrict__
 }
 
 __device__ __forceinline__ uint32_t ld32(const __nv_bfloat16* p) { return *reinterpret_cast<const uint32_t*>(p); }
-
-__device__ __forceinline__ uint32_t pack_raw(__nv_bfloat16 lo, __nv_bfloat16 hi)
-{
-    return uint32_t(__bfloat16_as_ushort(lo)) | (uint32_t(__bfloat16_as_ushort(hi)) << 16);
-}
 
 // Encoded inputs of rows r0 (= gid) and r1 (= gid + 8) as A fragments.
 __device__ __forceinline__ void encode_fragments(const float* q0, const float* q1, const NrcBox& box,
@@ -236,41 +219,76 @@ __global__ void __launch_bounds__(kThreads) k_nrc_infer(NrcInferParams p)
 
 // ---------------------------------------------------------------------------
 // Training
+//
+// One block = 8 warps; it takes 128 samples at a time (16 rows per warp).
+//   F   each warp: forward of its rows (register chain), H0..H4 and the
+//       output-layer gradient dZ5 stored to shared memory (BF16)
+//   P5  block: dW5 += dZ5^T H4;  each warp: dZ4 = (dZ5 W5) * [H4 > 0] (own rows)
+//   P4  block: dW4 += dZ4^T H3;  each warp: dZ3 = (dZ4 W4) * [H3 > 0]
+//   P3, P2 likewise; P1 block: dW1 += dZ1^T H0
+// with a block barrier between phases (dZ alternates between two buffers).
+// The weight gradient is a sum over samples, K = 128 per chunk: every warp
+// owns a fixed set of 16x8 output tiles of dW (21 tiles, 84 FP32
+// accumulators per lane) that stay in registers across all the block's
+// chunks; the transposed operands come from shared memory through
+// ldmatrix.trans. Each block writes its dW once (no atomics), so a block's
+// sum has a fixed order.
 
-// A fragment of a row-major [16][ld] matrix at columns col0..col0+15.
-__device__ __forceinline__ void frag_a(const __nv_bfloat16* M, int ld, int col0, uint32_t (&a)[4])
+constexpr int kTWarps = 8;
+constexpr int kTThreads = kTWarps * 32;
+constexpr int kChunk = 16 * kTWarps;            // 128 samples
+constexpr int kLdT = 16 + 8;                     // dZ5 row stride: 16 columns used
+constexpr int kTW = 0;                           // weights (W5 padded to 16 rows)
+constexpr int kTH0 = kSmemW + 8 * kLdH;          // 23,680
+constexpr int kTH1 = kTH0 + kChunk * kLd1;
+constexpr int kTH2 = kTH1 + kChunk * kLdH;
+constexpr int kTH3 = kTH2 + kChunk * kLdH;
+constexpr int kTH4 = kTH3 + kChunk * kLdH;
+constexpr int kTZA = kTH4 + kChunk * kLdH;
+constexpr int kTZB = kTZA + kChunk * kLdH;
+constexpr int kTZ5 = kTZB + kChunk * kLdH;
+constexpr int kTEnd = kTZ5 + kChunk * kLdT;      // 99,456 elements = 198,912 B
+static_assert(kTH0 % 8 == 0 && kTH1 % 8 == 0 && kTZ5 % 8 == 0, "ldmatrix rows need 16-byte alignment");
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p)
 {
-    const int gid = int(lane_id() >> 2), tig = int(lane_id() & 3u);
-    a[0] = ld32(M + gid * ld + col0 + tig * 2);
-    a[1] = ld32(M + (gid + 8) * ld + col0 + tig * 2);
-    a[2] = ld32(M + gid * ld + col0 + 8 + tig * 2);
-    a[3] = ld32(M + (gid + 8) * ld + col0 + 8 + tig * 2);
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }
 
-// A fragment of M^T (A[m][k] = M[k][m]) for m in m0.., k in 0..15; M = [16][ld].
-__device__ __forceinline__ void frag_a_t(const __nv_bfloat16* M, int ld, int m0, uint32_t (&a)[4])
+// Four 8x8 BF16 matrices, transposed; lane l gives the row address of
+// matrix l / 8, row l % 8.
+__device__ __forceinline__ void ldsm_x4_t(uint32_t (&r)[4], const __nv_bfloat16* p)
 {
-    const int gid = int(lane_id() >> 2), tig = int(lane_id() & 3u);
-    const int k = tig * 2;
-    a[0] = pack_raw(M[k * ld + m0 + gid], M[(k + 1) * ld + m0 + gid]);
-    a[1] = pack_raw(M[k * ld + m0 + gid + 8], M[(k + 1) * ld + m0 + gid + 8]);
-    a[2] = pack_raw(M[(k + 8) * ld + m0 + gid], M[(k + 9) * ld + m0 + gid]);
-    a[3] = pack_raw(M[(k + 8) * ld + m0 + gid + 8], M[(k + 9) * ld + m0 + gid + 8]);
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(smem_addr(p)));
 }
 
-// B fragment with B[k][n] = M[k][n] (M row-major [rows][ld]) for k in k0..k0+15
-// (rows >= kRows read as 0), n in n0..n0+7.
-__device__ __forceinline__ void frag_b_kn(const __nv_bfloat16* M, int ld, int kRows, int k0, int n0, uint32_t (&b)[2])
+__device__ __forceinline__ void ldsm_x2_t(uint32_t (&r)[2], const __nv_bfloat16* p)
 {
-    const int gid = int(lane_id() >> 2), tig = int(lane_id() & 3u);
-    const __nv_bfloat16 z = __float2bfloat16(0.0f);
-    int k = k0 + tig * 2;
-    b[0] = pack_raw(k < kRows ? M[k * ld + n0 + gid] : z, k + 1 < kRows ? M[(k + 1) * ld + n0 + gid] : z);
-    k += 8;
-    b[1] = pack_raw(k < kRows ? M[k * ld + n0 + gid] : z, k + 1 < kRows ? M[(k + 1) * ld + n0 + gid] : z);
+    asm volatile("ldmatrix.sync.aligned.m8n8.x2.trans.shared.b16 {%0,%1}, [%2];\n"
+                 : "=r"(r[0]), "=r"(r[1])
+                 : "r"(smem_addr(p)));
 }
 
-// Stores a [16 x 64] accumulator (8 n-tiles) as BF16 rows into M[16][ld], with ReLU.
+// Row address for an A fragment of M^T (A[m][k] = M[k][m], M row-major):
+// matrices (k0-7, m0-7), (k0-7, m8-15), (k8-15, m0-7), (k8-15, m8-15).
+__device__ __forceinline__ const __nv_bfloat16* a_trans_row(const __nv_bfloat16* M, int ld, int k0, int m0)
+{
+    const int l = int(lane_id());
+    return M + (k0 + (l & 7) + ((l >> 4) & 1) * 8) * ld + m0 + ((l >> 3) & 1) * 8;
+}
+
+// Row address for the B fragments of two n-tiles of a row-major [k][n]
+// matrix: (k0-7, n0-7), (k8-15, n0-7), (k0-7, n8-15), (k8-15, n8-15) ->
+// {b0, b1} of tile n0 and of tile n0 + 8.
+__device__ __forceinline__ const __nv_bfloat16* b_pair_row(const __nv_bfloat16* M, int ld, int k0, int n0)
+{
+    const int l = int(lane_id());
+    return M + (k0 + (l & 7) + ((l >> 3) & 1) * 8) * ld + n0 + ((l >> 4) & 1) * 8;
+}
+
+// Stores a 16 x 64 accumulator of the warp's rows with ReLU, as BF16.
 __device__ __forceinline__ void store_relu(const float (&C)[8][4], __nv_bfloat16* M, int ld)
 {
     const int gid = int(lane_id() >> 2), tig = int(lane_id() & 3u);
@@ -284,63 +302,98 @@ __device__ __forceinline__ void store_relu(const float (&C)[8][4], __nv_bfloat16
     }
 }
 
-// dW[o][i] += sum over the 16 samples of dZ[s][o] * H[s][i]: outputs o in
-// [0, outRows), inputs i in [0, inCols); added into the FP32 gradient g
-// ([out][in], row stride inCols).
-__device__ __forceinline__ void weight_grad(const __nv_bfloat16* dZ, int ldZ, int outRows, const __nv_bfloat16* H,
-                                            int ldHh, int inCols, float* g)
+// 1 where a stored BF16 activation is > 0 (ReLU outputs are >= 0).
+__device__ __forceinline__ float active(uint32_t bits16) { return (bits16 & 0x7fffu) ? 1.0f : 0.0f; }
+
+// One backward step for the warp's 16 rows: D = (A x W) * [Hprev > 0], W a
+// row-major [16 KT][64] shared-memory matrix (rows = this layer's outputs),
+// D stored as BF16 rows and returned as the next step's A fragments.
+template <int KT>
+__device__ __forceinline__ void chain_step(const uint32_t (&A)[KT][4], const __nv_bfloat16* W, const __nv_bfloat16* Hprev,
+                                           __nv_bfloat16* D, uint32_t (&An)[4][4])
 {
     const int gid = int(lane_id() >> 2), tig = int(lane_id() & 3u);
-    for (int m0 = 0; m0 < outRows; m0 += 16)
+    float C[8][4];
+#pragma unroll
+    for (int j = 0; j < 8; ++j)
+        C[j][0] = C[j][1] = C[j][2] = C[j][3] = 0.0f;
+#pragma unroll
+    for (int t = 0; t < KT; ++t)
+    {
+#pragma unroll
+        for (int jp = 0; jp < 4; ++jp)
+        {
+            uint32_t b[4];
+            ldsm_x4_t(b, b_pair_row(W, kLdH, 16 * t, 16 * jp));
+            uint32_t b0[2] = { b[0], b[1] }, b1[2] = { b[2], b[3] };
+            mma_bf16(C[2 * jp], A[t], b0);
+            mma_bf16(C[2 * jp + 1], A[t], b1);
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < 8; ++j)
+    {
+        const int col = 8 * j + tig * 2;
+        const uint32_t h01 = ld32(Hprev + gid * kLdH + col);
+        const uint32_t h23 = ld32(Hprev + (gid + 8) * kLdH + col);
+        const uint32_t p01 = pack_bf16(C[j][0] * active(h01), C[j][1] * active(h01 >> 16));
+        const uint32_t p23 = pack_bf16(C[j][2] * active(h23), C[j][3] * active(h23 >> 16));
+        *reinterpret_cast<uint32_t*>(D + gid * kLdH + col) = p01;
+        *reinterpret_cast<uint32_t*>(D + (gid + 8) * kLdH + col) = p23;
+        An[j >> 1][(j & 1) * 2 + 0] = p01;
+        An[j >> 1][(j & 1) * 2 + 1] = p23;
+    }
+}
+
+// acc[NT] (16 x 8 tiles of dW at rows m0.., columns n0 + 8 j) += Z^T H over
+// the chunk's 128 samples; Z = [128][ldZ] gradients, H = [128][ldH] inputs.
+template <int NT>
+__device__ __forceinline__ void dw_tiles(float (&acc)[NT][4], const __nv_bfloat16* Z, int ldZ, int m0,
+                                         const __nv_bfloat16* H, int ldH, int n0)
+{
+#pragma unroll 2
+    for (int ks = 0; ks < kChunk / 16; ++ks)
     {
         uint32_t a[4];
-        frag_a_t(dZ, ldZ, m0, a);
-        for (int n0 = 0; n0 < inCols; n0 += 8)
+        ldsm_x4_t(a, a_trans_row(Z, ldZ, 16 * ks, m0));
+#pragma unroll
+        for (int jp = 0; jp < NT / 2; ++jp)
         {
-            uint32_t b[2];
-            frag_b_kn(H, ldHh, 16, 0, n0, b);
-            float c[4] = { 0.0f, 0.0f, 0.0f, 0.0f };
-            mma_bf16(c, a, b);
-            const int o0 = m0 + gid, o1 = o0 + 8, i = n0 + tig * 2;
-            if (o0 < outRows)
-            {
-                atomicAdd(g + o0 * inCols + i, c[0]);
-                atomicAdd(g + o0 * inCols + i + 1, c[1]);
-            }
-            if (o1 < outRows)
-            {
-                atomicAdd(g + o1 * inCols + i, c[2]);
-                atomicAdd(g + o1 * inCols + i + 1, c[3]);
-            }
+            uint32_t b[4];
+            ldsm_x4_t(b, b_pair_row(H, ldH, 16 * ks, n0 + 16 * jp));
+            uint32_t b0[2] = { b[0], b[1] }, b1[2] = { b[2], b[3] };
+            mma_bf16(acc[2 * jp], a, b0);
+            mma_bf16(acc[2 * jp + 1], a, b1);
         }
     }
 }
 
-// dZ_prev = (dZ x W) * (H_prev > 0), W = [out][ldW] padded shared weights with
-// `outRows` rows; dZ = [16][ldZ] with K = 16 * kTiles columns; result written
-// as BF16 into D[16][ldD] (64 columns).
-__device__ __forceinline__ void input_grad(const __nv_bfloat16* dZ, int ldZ, int kTiles, const __nv_bfloat16* W,
-                                           int ldW, int outRows, const __nv_bfloat16* Hprev, int ldHp,
-                                           __nv_bfloat16* D, int ldD)
+// The output layer's single tile per warp (rows 0-15 of dW5, columns n0..n0+7).
+__device__ __forceinline__ void dw_tile5(float (&acc)[4], const __nv_bfloat16* Z5, const __nv_bfloat16* H4, int n0)
+{
+    const int l = int(lane_id());
+#pragma unroll 2
+    for (int ks = 0; ks < kChunk / 16; ++ks)
+    {
+        uint32_t a[4], b[2];
+        ldsm_x4_t(a, a_trans_row(Z5, kLdT, 16 * ks, 0));
+        ldsm_x2_t(b, H4 + (16 * ks + (l & 7) + ((l >> 3) & 1) * 8) * kLdH + n0);
+        mma_bf16(acc, a, b);
+    }
+}
+
+// Writes a warp's dW tiles (rows m0 + gid, + 8; columns n0 + 8 j + 2 tig, + 1)
+// into the [out][in] gradient g.
+template <int NT>
+__device__ __forceinline__ void write_tiles(const float (&acc)[NT][4], float* g, int in, int m0, int n0)
 {
     const int gid = int(lane_id() >> 2), tig = int(lane_id() & 3u);
-    for (int j = 0; j < 8; ++j)
+#pragma unroll
+    for (int j = 0; j < NT; ++j)
     {
-        float c[4] = { 0.0f, 0.0f, 0.0f, 0.0f };
-        for (int t = 0; t < kTiles; ++t)
-        {
-            uint32_t a[4], b[2];
-            frag_a(dZ, ldZ, 16 * t, a);
-            frag_b_kn(W, ldW, outRows, 16 * t, 8 * j, b);
-            mma_bf16(c, a, b);
-        }
-        const int col = 8 * j + tig * 2;
-        float m0 = __bfloat162float(Hprev[gid * ldHp + col]) > 0.0f ? 1.0f : 0.0f;
-        float m1 = __bfloat162float(Hprev[gid * ldHp + col + 1]) > 0.0f ? 1.0f : 0.0f;
-        float m2 = __bfloat162float(Hprev[(gid + 8) * ldHp + col]) > 0.0f ? 1.0f : 0.0f;
-        float m3 = __bfloat162float(Hprev[(gid + 8) * ldHp + col + 1]) > 0.0f ? 1.0f : 0.0f;
-        *reinterpret_cast<uint32_t*>(D + gid * ldD + col) = pack_bf16(c[0] * m0, c[1] * m1);
-        *reinterpret_cast<uint32_t*>(D + (gid + 8) * ldD + col) = pack_bf16(c[2] * m2, c[3] * m3);
+        const int c = n0 + 8 * j + tig * 2;
+        *reinterpret_cast<float2*>(g + (m0 + gid) * in + c) = make_float2(acc[j][0], acc[j][1]);
+        *reinterpret_cast<float2*>(g + (m0 + gid + 8) * in + c) = make_float2(acc[j][2], acc[j][3]);
     }
 }
 
@@ -353,36 +406,54 @@ __device__ __forceinline__ int sample_index(const NrcTrainParams& p, unsigned to
     return p.index[h % total];
 }
 
-__global__ void __launch_bounds__(kThreads) k_nrc_train(NrcTrainParams p)
+__global__ void __launch_bounds__(kTThreads, 1) k_nrc_train(NrcTrainParams p)
 {
     extern __shared__ __align__(16) unsigned char smem[];
-    __nv_bfloat16* sW = reinterpret_cast<__nv_bfloat16*>(smem);
-    float* sG = reinterpret_cast<float*>(smem + kSmemW * 2);
-    __nv_bfloat16* scratchAll = reinterpret_cast<__nv_bfloat16*>(smem + kSmemW * 2 + kNrcParams * 4);
+    __nv_bfloat16* S = reinterpret_cast<__nv_bfloat16*>(smem);
+    __nv_bfloat16* sW = S + kTW;
     load_weights(sW, p.weights);
-    for (int i = threadIdx.x; i < kNrcParams; i += blockDim.x)
-        sG[i] = 0.0f;
+    // rows 8..15 of the output layer (read by the 16-row B fragments) are zero
+    for (int i = threadIdx.x; i < 8 * kLdH; i += blockDim.x)
+        sW[kS5 + 8 * kLdH + i] = __float2bfloat16(0.0f);
     __syncthreads();
 
     const int warp = int(threadIdx.x >> 5);
     const int gid = int(lane_id() >> 2), tig = int(lane_id() & 3u);
-    __nv_bfloat16* sc = scratchAll + warp * kScratch;
-    __nv_bfloat16* H0 = sc + kScH0;
-    __nv_bfloat16* H1 = sc + kScH1;
-    __nv_bfloat16* H2 = sc + kScH2;
-    __nv_bfloat16* H3 = sc + kScH3;
-    __nv_bfloat16* H4 = sc + kScH4;
-    __nv_bfloat16* Za = sc + kScZa;
-    __nv_bfloat16* Zb = sc + kScZb;
-    __nv_bfloat16* Z5 = sc + kScZ5;
-    float lossSum = 0.0f;
     const unsigned total = p.index ? *p.total : unsigned(p.batch);
     const int n = total == 0 ? 0 : p.batch;
-    const int tiles = (n + 15) / 16;
+    const int chunks = (n + kChunk - 1) / kChunk;
+    const float scale = 1.0f / (float(n > 0 ? n : 1) * 3.0f);
 
-    for (int tile = blockIdx.x * kWarps + warp; tile < tiles; tile += gridDim.x * kWarps)
+    // this warp's dW tiles
+    const int mt = warp >> 1;                   // 16-row block of the 64 hidden outputs
+    float acc1[8][4], acc2[4][4], acc3[4][4], acc4[4][4], acc5[4];
+#pragma unroll
+    for (int j = 0; j < 8; ++j)
+        acc1[j][0] = acc1[j][1] = acc1[j][2] = acc1[j][3] = 0.0f;
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
     {
-        const int r0 = tile * 16 + gid, r1 = r0 + 8;
+        acc2[j][0] = acc2[j][1] = acc2[j][2] = acc2[j][3] = 0.0f;
+        acc3[j][0] = acc3[j][1] = acc3[j][2] = acc3[j][3] = 0.0f;
+        acc4[j][0] = acc4[j][1] = acc4[j][2] = acc4[j][3] = 0.0f;
+    }
+    acc5[0] = acc5[1] = acc5[2] = acc5[3] = 0.0f;
+    float lossSum = 0.0f;
+
+    __nv_bfloat16* H0 = S + kTH0;
+    __nv_bfloat16* H1 = S + kTH1;
+    __nv_bfloat16* H2 = S + kTH2;
+    __nv_bfloat16* H3 = S + kTH3;
+    __nv_bfloat16* H4 = S + kTH4;
+    __nv_bfloat16* ZA = S + kTZA;
+    __nv_bfloat16* ZB = S + kTZB;
+    __nv_bfloat16* Z5 = S + kTZ5;
+    const int rowBase = 16 * warp;  // this warp's rows in the chunk
+
+    for (int chunk = blockIdx.x; chunk < chunks; chunk += gridDim.x)
+    {
+        // ---- F: forward of the warp's rows
+        const int r0 = chunk * kChunk + rowBase + gid, r1 = r0 + 8;
         const bool v0 = r0 < n, v1 = r1 < n;
         const int i0 = v0 ? sample_index(p, total, r0) : 0;
         const int i1 = v1 ? sample_index(p, total, r1) : 0;
@@ -397,96 +468,108 @@ __global__ void __launch_bounds__(kThreads) k_nrc_train(NrcTrainParams p)
             zero_query(q1);
         uint32_t A0[8][4];
         encode_fragments(q0, q1, p.box, A0);
-        // H0: the encoded inputs
-#pragma unroll
-        for (int t = 0; t < 8; ++t)
         {
-            *reinterpret_cast<uint32_t*>(H0 + gid * kLd1 + 16 * t + tig * 2) = A0[t][0];
-            *reinterpret_cast<uint32_t*>(H0 + (gid + 8) * kLd1 + 16 * t + tig * 2) = A0[t][1];
-            *reinterpret_cast<uint32_t*>(H0 + gid * kLd1 + 16 * t + 8 + tig * 2) = A0[t][2];
-            *reinterpret_cast<uint32_t*>(H0 + (gid + 8) * kLd1 + 16 * t + 8 + tig * 2) = A0[t][3];
+            __nv_bfloat16* h0 = H0 + rowBase * kLd1;
+#pragma unroll
+            for (int t = 0; t < 8; ++t)
+            {
+                *reinterpret_cast<uint32_t*>(h0 + gid * kLd1 + 16 * t + tig * 2) = A0[t][0];
+                *reinterpret_cast<uint32_t*>(h0 + (gid + 8) * kLd1 + 16 * t + tig * 2) = A0[t][1];
+                *reinterpret_cast<uint32_t*>(h0 + gid * kLd1 + 16 * t + 8 + tig * 2) = A0[t][2];
+                *reinterpret_cast<uint32_t*>(h0 + (gid + 8) * kLd1 + 16 * t + 8 + tig * 2) = A0[t][3];
+            }
         }
-        float C[8][4];
         uint32_t A[4][4];
-        layer_mma<8>(A0, sW + kS1, kLd1, C);
-        store_relu(C, H1, kLdH);
-        relu_pack(C, A);
-        layer_mma<4>(A, sW + kS2, kLdH, C);
-        store_relu(C, H2, kLdH);
-        relu_pack(C, A);
-        layer_mma<4>(A, sW + kS3, kLdH, C);
-        store_relu(C, H3, kLdH);
-        relu_pack(C, A);
-        layer_mma<4>(A, sW + kS4, kLdH, C);
-        store_relu(C, H4, kLdH);
-        relu_pack(C, A);
+        {
+            float C[8][4];
+            layer_mma<8>(A0, sW + kS1, kLd1, C);
+            store_relu(C, H1 + rowBase * kLdH, kLdH);
+            relu_pack(C, A);
+            layer_mma<4>(A, sW + kS2, kLdH, C);
+            store_relu(C, H2 + rowBase * kLdH, kLdH);
+            relu_pack(C, A);
+            layer_mma<4>(A, sW + kS3, kLdH, C);
+            store_relu(C, H3 + rowBase * kLdH, kLdH);
+            relu_pack(C, A);
+            layer_mma<4>(A, sW + kS4, kLdH, C);
+            store_relu(C, H4 + rowBase * kLdH, kLdH);
+            relu_pack(C, A);
+        }
         float o[4];
         output_mma(A, sW + kS5, o);
 
         // Relative L2 loss (p - y)^2 / (p^2 + 0.01), mean over batch x 3;
-        // the denominator is held constant for the gradient.
-        for (int k = lane_id(); k < 16 * kLdT; k += 32)
-            Z5[k] = __float2bfloat16(0.0f);
-        __syncwarp();
-        if (tig < 2)
+        // the denominator is held constant for the gradient. Output columns
+        // (2 tig, 2 tig + 1) of rows gid and gid + 8; only columns 0..2 exist.
+        float d[4] = { 0.0f, 0.0f, 0.0f, 0.0f };
+#pragma unroll
+        for (int e = 0; e < 4; ++e)
         {
-            const int col = tig * 2;
-            const float scale = 1.0f / (float(n) * 3.0f);
-            for (int h = 0; h < 2; ++h)
-            {
-                const bool valid = h == 0 ? v0 : v1;
-                const int idx = h == 0 ? i0 : i1;
-                const int row = h == 0 ? gid : gid + 8;
-                for (int e = 0; e < 2; ++e)
-                {
-                    const int c = col + e;
-                    if (!valid || c >= 3)
-                        continue;
-                    float pr = __expf(o[2 * h + e]);
-                    float y = reinterpret_cast<const float*>(&p.rec[idx].d)[c];
-                    float den = pr * pr + 0.01f;
-                    float diff = pr - y;
-                    lossSum += diff * diff / den * scale;
-                    float g = 2.0f * diff / den * scale * pr;  // d/dz of exp(z)
-                    Z5[row * kLdT + c] = __float2bfloat16(g);
-                }
-            }
+            const int c = tig * 2 + (e & 1);
+            const bool valid = (e < 2 ? v0 : v1) && c < 3;
+            if (!valid)
+                continue;
+            const int idx = e < 2 ? i0 : i1;
+            const float pr = __expf(o[e]);
+            const float y = reinterpret_cast<const float*>(&p.rec[idx].d)[c];
+            const float den = pr * pr + 0.01f;
+            const float diff = pr - y;
+            lossSum += diff * diff / den * scale;
+            d[e] = 2.0f * diff / den * scale * pr;  // d/dz of exp(z)
         }
-        __syncwarp();
+        uint32_t A5[1][4];
+        A5[0][0] = pack_bf16(d[0], d[1]);
+        A5[0][1] = pack_bf16(d[2], d[3]);
+        A5[0][2] = 0u;  // columns 8..15
+        A5[0][3] = 0u;
+        {
+            __nv_bfloat16* z5 = Z5 + rowBase * kLdT;
+            *reinterpret_cast<uint32_t*>(z5 + gid * kLdT + tig * 2) = A5[0][0];
+            *reinterpret_cast<uint32_t*>(z5 + (gid + 8) * kLdT + tig * 2) = A5[0][1];
+            *reinterpret_cast<uint32_t*>(z5 + gid * kLdT + 8 + tig * 2) = 0u;
+            *reinterpret_cast<uint32_t*>(z5 + (gid + 8) * kLdT + 8 + tig * 2) = 0u;
+        }
+        __syncthreads();
 
-        // layer 5: dW5, dZ4
-        weight_grad(Z5, kLdT, kNrcOut, H4, kLdH, kNrcHidden, sG + kNrcW5);
-        input_grad(Z5, kLdT, 1, sW + kS5, kLdH, kNrcOutPad, H4, kLdH, Za, kLdH);
-        __syncwarp();
-        // layer 4
-        weight_grad(Za, kLdH, kNrcHidden, H3, kLdH, kNrcHidden, sG + kNrcW4);
-        input_grad(Za, kLdH, 4, sW + kS4, kLdH, kNrcHidden, H3, kLdH, Zb, kLdH);
-        __syncwarp();
-        // layer 3
-        weight_grad(Zb, kLdH, kNrcHidden, H2, kLdH, kNrcHidden, sG + kNrcW3);
-        input_grad(Zb, kLdH, 4, sW + kS3, kLdH, kNrcHidden, H2, kLdH, Za, kLdH);
-        __syncwarp();
-        // layer 2
-        weight_grad(Za, kLdH, kNrcHidden, H1, kLdH, kNrcHidden, sG + kNrcW2);
-        input_grad(Za, kLdH, 4, sW + kS2, kLdH, kNrcHidden, H1, kLdH, Zb, kLdH);
-        __syncwarp();
-        // layer 1
-        weight_grad(Zb, kLdH, kNrcHidden, H0, kLd1, kNrcIn, sG + kNrcW1);
-        __syncwarp();
+        // ---- P5
+        dw_tile5(acc5, Z5, H4, 8 * warp);
+        chain_step<1>(A5, sW + kS5, H4 + rowBase * kLdH, ZA + rowBase * kLdH, A);
+        __syncthreads();
+        // ---- P4
+        dw_tiles<4>(acc4, ZA, kLdH, 16 * mt, H3, kLdH, (warp & 1) * 32);
+        chain_step<4>(A, sW + kS4, H3 + rowBase * kLdH, ZB + rowBase * kLdH, A);
+        __syncthreads();
+        // ---- P3
+        dw_tiles<4>(acc3, ZB, kLdH, 16 * mt, H2, kLdH, (warp & 1) * 32);
+        chain_step<4>(A, sW + kS3, H2 + rowBase * kLdH, ZA + rowBase * kLdH, A);
+        __syncthreads();
+        // ---- P2
+        dw_tiles<4>(acc2, ZA, kLdH, 16 * mt, H1, kLdH, (warp & 1) * 32);
+        chain_step<4>(A, sW + kS2, H1 + rowBase * kLdH, ZB + rowBase * kLdH, A);
+        __syncthreads();
+        // ---- P1
+        dw_tiles<8>(acc1, ZB, kLdH, 16 * mt, H0, kLd1, (warp & 1) * 64);
+        __syncthreads();
     }
+
+    float* part = p.partials + size_t(blockIdx.x) * kNrcParams;
+    write_tiles<8>(acc1, part + kNrcW1, kNrcIn, 16 * mt, (warp & 1) * 64);
+    write_tiles<4>(acc2, part + kNrcW2, kNrcHidden, 16 * mt, (warp & 1) * 32);
+    write_tiles<4>(acc3, part + kNrcW3, kNrcHidden, 16 * mt, (warp & 1) * 32);
+    write_tiles<4>(acc4, part + kNrcW4, kNrcHidden, 16 * mt, (warp & 1) * 32);
+    // dW5: rows 0..7 of the padded output layer (rows 3..7 are zero)
+    *reinterpret_cast<float2*>(part + kNrcW5 + gid * kNrcHidden + 8 * warp + tig * 2) = make_float2(acc5[0], acc5[1]);
+
     for (int off = 16; off > 0; off >>= 1)
         lossSum += __shfl_down_sync(0xffffffffu, lossSum, off);
-    __shared__ float sLoss[kWarps];
+    __shared__ float sLoss[kTWarps];
     if (lane_id() == 0)
         sLoss[warp] = lossSum;
     __syncthreads();
-    float* part = p.partials + size_t(blockIdx.x) * kNrcParams;
-    for (int i = threadIdx.x; i < kNrcParams; i += blockDim.x)
-        part[i] = sG[i];
     if (threadIdx.x == 0)
     {
         float l = 0.0f;
-        for (int w = 0; w < kWarps; ++w)
+        for (int w = 0; w < kTWarps; ++w)
             l += sLoss[w];
         p.lossPartials[blockIdx.x] = l;
     }
@@ -546,7 +629,7 @@ size_t nrc_infer_smem() { return size_t(kSmemW) * 2; }
 
 }  // namespace
 
-size_t nrc_train_smem() { return size_t(kSmemW) * 2 + size_t(kNrcParams) * 4 + size_t(kWarps * kScratch) * 2; }
+size_t nrc_train_smem() { return size_t(kTEnd) * 2; }
 
 int nrc_train_blocks(int numSMs) { return numSMs; }
 
@@ -578,7 +661,7 @@ cudaError_t launch_nrc_train(const NrcTrainParams& p, int blocks, cudaStream_t s
             return e;
         configured = true;
     }
-    k_nrc_train<<<blocks, kThreads, nrc_train_smem(), stream>>>(p);
+    k_nrc_train<<<blocks, kTThreads, nrc_train_smem(), stream>>>(p);
     return cudaGetLastError();
 }
 
