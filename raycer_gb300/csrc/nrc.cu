@@ -30,7 +30,7 @@ namespace rcx
 namespace
 {
 
-constexpr int kWarps = 4;
+constexpr int kWarps = 8;  // inference block
 constexpr int kThreads = kWarps * 32;
 // padded row strides (elements) of the shared-memory weight copies
 constexpr int kLd1 = kNrcIn + 8;       // 136
@@ -44,11 +44,16 @@ constexpr int kSmemW = kS5 + kNrcOutPad * kLdH;  // 23104 elements = 46,208 B
 
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
 
-// Copies the packed [out][in] weights into the padded shared-memory layout.
+// Copies the packed [out][in] weights into the padded shared-memory layout,
+// 8 elements (16 bytes) per load: every row length is a multiple of 8.
 __device__ void load_weights(__nv_bfloat16* s, const __nv_bfloat16* __restrict__ w)
 {
-    for (int i = threadIdx.x; i < kNrcParams; i += blockDim.x)
+    constexpr int kVec = kNrcParams / 8;
+    const uint4* __restrict__ src = reinterpret_cast<const uint4*>(w);
+#pragma unroll 4
+    for (int v = threadIdx.x; v < kVec; v += blockDim.x)
     {
+        const int i = v * 8;
         int dst;
         if (i < kNrcW2)
             dst = kS1 + (i / kNrcIn) * kLd1 + (i % kNrcIn);
@@ -60,7 +65,7 @@ __device__ void load_weights(__nv_bfloat16* s, const __nv_bfloat16* __restrict__
         }
         else
             dst = kS5 + ((i - kNrcW5) / kNrcHidden) * kLdH + ((i - kNrcW5) % kNrcHidden);
-        s[dst] = w[i];
+        *reinterpret_cast<uint4*>(s + dst) = __ldg(src + v);
     }
 }
 
@@ -589,9 +594,18 @@ __global__ void k_nrc_adam(NrcAdamParams p)
     }
     if (i >= kNrcParams)
         return;
-    float g = 0.0f;
-    for (int b = 0; b < p.numPartials; ++b)
-        g += p.partials[size_t(b) * kNrcParams + i];
+    // eight independent running sums (more loads in flight), combined in a fixed order
+    float acc[8] = { 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f };
+    int b = 0;
+    for (; b + 8 <= p.numPartials; b += 8)
+    {
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+            acc[k] += __ldg(p.partials + size_t(b + k) * kNrcParams + i);
+    }
+    for (; b < p.numPartials; ++b)
+        acc[0] += __ldg(p.partials + size_t(b) * kNrcParams + i);
+    const float g = ((acc[0] + acc[1]) + (acc[2] + acc[3])) + ((acc[4] + acc[5]) + (acc[6] + acc[7]));
     if (p.gradOut)
         p.gradOut[i] = g;
     if (!p.adam || (p.total && *p.total == 0))
@@ -635,17 +649,20 @@ int nrc_train_blocks(int numSMs) { return numSMs; }
 
 cudaError_t launch_nrc_infer(const NrcInferParams& p, int maxRecords, cudaStream_t stream, int numSMs)
 {
-    static bool configured = false;
-    if (!configured)
+    static int perSM = 0;
+    if (perSM == 0)
     {
         cudaError_t e =
             cudaFuncSetAttribute(k_nrc_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, int(nrc_infer_smem()));
         if (e != cudaSuccess)
             return e;
-        configured = true;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_nrc_infer, kThreads, nrc_infer_smem()) !=
+                cudaSuccess ||
+            perSM < 1)
+            perSM = 1;
     }
     int tiles = (maxRecords + 15) / 16;
-    int grid = std::max(1, std::min((tiles + kWarps - 1) / kWarps, numSMs * 4));
+    int grid = std::max(1, std::min((tiles + kWarps - 1) / kWarps, numSMs * perSM));
     k_nrc_infer<<<grid, kThreads, nrc_infer_smem(), stream>>>(p);
     return cudaGetLastError();
 }
