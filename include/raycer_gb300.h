@@ -85,7 +85,15 @@ typedef enum rc_tracer_type { RC_TRACER_RAY = 0, RC_TRACER_PATH = 1 } rc_tracer_
 /* Values follow the reference's enums (Rendering/Samplers/Sampler.h:24,
  * Rendering/Filters/Filter.h:10, Rendering/ToneMappers/ToneMapper.h:15). */
 typedef enum rc_sampler_type { RC_SAMPLER_CENTER = 0, RC_SAMPLER_RANDOM = 1, RC_SAMPLER_CMJ = 4 } rc_sampler_type;
-typedef enum rc_filter_type { RC_FILTER_BOX = 0 } rc_filter_type;
+typedef enum rc_filter_type
+{
+    RC_FILTER_BOX = 0,
+    RC_FILTER_TENT = 1,
+    RC_FILTER_BELL = 2,
+    RC_FILTER_GAUSSIAN = 3,
+    RC_FILTER_MITCHELL = 4,
+    RC_FILTER_LANCZOS_SINC = 5
+} rc_filter_type;
 typedef enum rc_tonemapper_type { RC_TONEMAP_PASSTHROUGH = 0, RC_TONEMAP_REINHARD = 3 } rc_tonemapper_type;
 
 /* Scene::General fields on the hot path (src/Raytracing/Scene.h:89-131)
@@ -98,7 +106,9 @@ typedef struct rc_general
     int32_t multi_sample_count_sqrt; /* multiSampleCountSqrt: n x n film samples    */
     int32_t multi_sampler_type;      /* rc_sampler_type (multiSamplerType)          */
     int32_t filter_type;             /* rc_filter_type (multiSamplerFilterType)     */
-    float filter_radius[2];          /* BoxFilter radius (BoxFilter.h:16: 0.5, 0.5) */
+    float filter_radius[2];          /* BOX radius (BoxFilter.h:16: 0.5, 0.5); the  */
+                                     /* others use their constructors' defaults as  */
+                                     /* the reference's Tracer does (Tracer.cpp:50) */
     float ray_start_offset;          /* rayStartOffset (Scene.h:95: 1e-5)           */
     float background[3];             /* backgroundColor (RAY tracer, miss)          */
     int32_t russian_roulette_depth;  /* 0 = off (reference); else first RR segment  */
@@ -261,7 +271,8 @@ rc_status rc_camera_from_euler(const double position[3], double pitch, double ya
                                uint64_t width, uint64_t height, rc_camera* out);
 
 /* Default General / ToneMapper records (the reference's defaults,
- * Scene.h:89-159, with box filter and the given tracer type). */
+ * Scene.h:89-159 — MITCHELL film filter, CMJ sampler — with the given
+ * tracer type). */
 void rc_general_defaults(rc_general* out, int32_t tracer_type);
 void rc_tonemapper_defaults(rc_tonemapper* out);
 

@@ -43,6 +43,9 @@ def _setup(lib: C.CDLL, protos: dict) -> C.CDLL:
 
 
 _ORACLE_PROTOS = {
+    "or32_filter_weight": (None, [C.c_int, i64, P, P, P]),
+    "or64_filter_weight": (None, [C.c_int, i64, P, P, P]),
+    "or32_filter_exp": (None, [i64, P, P]),
     "or_nrc_features": (None, [P, i64, P, P, C.c_int, P]),
     "or_nrc_forward": (None, [P, P, i64, P, P, C.c_int, P]),
     "or_nrc_loss": (f64, [P, P, P, i64, P, P, C.c_int, P]),
@@ -58,14 +61,14 @@ _ORACLE_PROTOS = {
     "or64_tri": (C.c_int, [P, i64, P, C.POINTER(f64), C.POINTER(f64), C.POINTER(f64)]),
     "or64_raycast": (f64, [P, P, u64, u64, u64, P, f64, P, P, P, C.c_int, C.POINTER(u64)]),
     "or64_render_path": (f64, [P, P, u64, u64, u64, u64, u64, u64, C.c_int, f64, f64, f64, u32, C.c_int, P,
-                               C.POINTER(u64)]),
+                               C.POINTER(u64), C.c_int]),
     "or64_tonemap": (None, [i64, P, f64, f64, C.c_int, C.c_int, P]),
     "or64_fastpow": (f64, [f64, f64]),
     "or32_cast": (None, [P, i64, P, C.c_int, C.c_int, P, P, P, P, P, C.c_int]),
     "or32_raycast": (None, [P, P, u64, u64, u64, P, f32, C.c_int, P, P, C.c_int]),
     "or32_camera_rays": (None, [P, u64, u64, u64, P]),
     "or32_render_path": (None, [P, P, u64, u64, u64, C.c_int, C.c_int, C.c_int, f32, f32, f32, C.c_int, C.c_int,
-                                C.c_int, u64, u32, P, P, C.c_int]),
+                                C.c_int, u64, u32, P, P, C.c_int, C.c_int]),
     "or32_sincos_turn": (None, [i64, P, P, P]),
     "or64_cmj": (None, [u64, u64, u64, u64, f64, f64, P]),
     "or32_cmj_permute": (u64, [u64, u64, u64]),
@@ -95,6 +98,7 @@ _REF_PROTOS = {
     "ref_fastpow": (f64, [f64, f64]),
     "ref_value_noise": (None, [u32, i64, P, u64, f64, f64, P]),
     "ref_cmj_pattern": (None, [u64, u64, u32, P, P]),
+    "ref_filter_weight": (None, [C.c_int, i64, P, P, P]),
 }
 
 _oracle = None
@@ -226,13 +230,13 @@ class Oracle:
 
     def render_path64(self, cam64: np.ndarray, width: int, count: int, max_path_length: int, path_samples: int,
                       ms_sqrt: int, sampler: int = 4, radius=(0.5, 0.5), offset: float = 1e-5, seed: int = 1,
-                      threads: int = 0, pixel_start: int = 0):
+                      threads: int = 0, pixel_start: int = 0, filter_type: int = 0):
         cam = np.ascontiguousarray(cam64, np.float64)
         film = np.zeros((count, 4), np.float64)
         rays = u64(0)
         sec = self.lib.or64_render_path(self.h, _ptr(cam), width, pixel_start, count, max_path_length, path_samples,
                                         ms_sqrt, sampler, radius[0], radius[1], offset, seed, threads, _ptr(film),
-                                        C.byref(rays))
+                                        C.byref(rays), int(filter_type))
         return film, rays.value, sec
 
     # float32 twin of the device
@@ -260,12 +264,14 @@ class Oracle:
 
     def render_path32(self, cam: np.ndarray, width: int, count: int, n: int, P: int, sampler: int, radius,
                       offset: float, max_path_length: int, rr_depth: int, order: int, seed: int, frame: int,
-                      film: np.ndarray | None = None, threads: int = 0, pixel_start: int = 0):
+                      film: np.ndarray | None = None, threads: int = 0, pixel_start: int = 0,
+                      filter_type: int = 0):
         c = np.ascontiguousarray(cam, np.float32)
         f = np.zeros((count, 4), np.float32) if film is None else np.ascontiguousarray(film, np.float32).copy()
         cnt = np.zeros(4, np.uint64)
         self.lib.or32_render_path(self.h, _ptr(c), width, pixel_start, count, n, P, sampler, radius[0], radius[1],
-                                  offset, max_path_length, rr_depth, order, seed, frame, _ptr(f), _ptr(cnt), threads)
+                                  offset, max_path_length, rr_depth, order, seed, frame, _ptr(f), _ptr(cnt), threads,
+                                  int(filter_type))
         return f, cnt
 
 
@@ -437,3 +443,38 @@ def nrc_adam(master, m, v, grad, t: int, lr=1e-2, b1=0.9, b2=0.99, eps=1e-8):
     g = np.ascontiguousarray(grad, np.float32)
     oracle_lib().or_nrc_adam(_ptr(w), _ptr(mm), _ptr(vv), _ptr(g), int(t), lr, b1, b2, eps)
     return w, mm, vv
+
+
+# ---------------------------------------------------------------------------
+# Film filters: one axis's weight at offsets x.
+
+def filter_weight32(filter_type: int, x) -> tuple[np.ndarray, float]:
+    xs = np.ascontiguousarray(x, np.float32)
+    out = np.empty_like(xs)
+    r = f32(0)
+    oracle_lib().or32_filter_weight(int(filter_type), xs.size, _ptr(xs), _ptr(out), C.byref(r))
+    return out, r.value
+
+
+def filter_weight64(filter_type: int, x) -> tuple[np.ndarray, float]:
+    xs = np.ascontiguousarray(x, np.float64)
+    out = np.empty_like(xs)
+    r = f64(0)
+    oracle_lib().or64_filter_weight(int(filter_type), xs.size, _ptr(xs), _ptr(out), C.byref(r))
+    return out, r.value
+
+
+def filter_exp32(t) -> np.ndarray:
+    ts = np.ascontiguousarray(t, np.float32)
+    out = np.empty_like(ts)
+    oracle_lib().or32_filter_exp(ts.size, _ptr(ts), _ptr(out))
+    return out
+
+
+def ref_filter_weight(filter_type: int, x) -> tuple[np.ndarray, float]:
+    """The reference's own Filter::getWeightX (needs oracle/_ref)."""
+    xs = np.ascontiguousarray(x, np.float64)
+    out = np.empty_like(xs)
+    r = f64(0)
+    ref_lib().ref_filter_weight(int(filter_type), xs.size, _ptr(xs), _ptr(out), C.byref(r))
+    return out, r.value

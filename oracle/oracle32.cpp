@@ -464,6 +464,124 @@ void cast32(const Scene32& s, int64_t n, const float* rays8, int anyHit, int ord
     }
 }
 
+// Film filters (the device's filters.cuh restated: same constants, same
+// operation order, std::fma where the device fuses).
+Filter32 filter32(int type, float boxRx, float boxRy)
+{
+    Filter32 f{};
+    f.type = type;
+    switch (type)
+    {
+    case 0:
+        f.rx = boxRx;
+        f.ry = boxRy;
+        f.ax = 1.0f / (2.0f * f.rx);
+        f.ay = 1.0f / (2.0f * f.ry);
+        break;
+    case 1:
+        f.rx = f.ry = 1.0f;
+        f.ax = f.ay = 1.0f;
+        break;
+    case 2:
+        f.rx = f.ry = 1.5f;
+        break;
+    case 3:
+        f.ax = f.ay = float(1.0 / std::sqrt(2.0 * 3.14159265358979323846));
+        f.bx = f.by = -0.5f;
+        f.rx = f.ry = float(7.43384 / 2.0);
+        break;
+    case 4:
+    {
+        const double B = 1.0 / 3.0, C = 1.0 / 3.0;
+        const double k[8] = { (12.0 - 9.0 * B - 6.0 * C) / 6.0, (-18.0 + 12.0 * B + 6.0 * C) / 6.0, 0.0,
+                              (6.0 - 2.0 * B) / 6.0, (-B - 6.0 * C) / 6.0, (6.0 * B + 30.0 * C) / 6.0,
+                              (-12.0 * B - 48.0 * C) / 6.0, (8.0 * B + 24.0 * C) / 6.0 };
+        for (int i = 0; i < 8; ++i)
+            f.cubic[i] = float(k[i]);
+        f.rx = f.ry = 2.0f;
+        break;
+    }
+    default:
+        f.rx = f.ry = 2.0f;
+        break;
+    }
+    return f;
+}
+
+float filter_exp32(float t)
+{
+    const float y = t * 1.44269504088896341f;
+    const float n = std::floor(y + 0.5f);
+    float f = std::fma(-n, 0.693145751953125f, t);
+    f = std::fma(-n, 1.42860682030941723e-6f, f);
+    float p = std::fma(f, 1.98412698412698413e-4f, 1.38888888888888889e-3f);
+    p = std::fma(f, p, 8.33333333333333333e-3f);
+    p = std::fma(f, p, 4.16666666666666667e-2f);
+    p = std::fma(f, p, 1.66666666666666667e-1f);
+    p = std::fma(f, p, 0.5f);
+    p = std::fma(f, p, 1.0f);
+    p = std::fma(f, p, 1.0f);
+    const int e = int(n);
+    if (e < -126)
+        return 0.0f;
+    uint32_t bits = uint32_t(e + 127) << 23;
+    float scale;
+    std::memcpy(&scale, &bits, 4);
+    return p * scale;
+}
+
+static float filter_sinc32(float s)
+{
+    float sv, cv;
+    sincos_turn(s * 0.5f, sv, cv);
+    return sv / (3.14159265358979324f * s);
+}
+
+float filter_weight32(const Filter32& f, float x, float r, float a, float b)
+{
+    switch (f.type)
+    {
+    case 0:
+        return (x >= -r && x < r) ? a : 0.0f;
+    case 1:
+    {
+        const float s = std::fabs(x * a);
+        return s < 1.0f ? (1.0f - s) * a : 0.0f;
+    }
+    case 2:
+    {
+        const float s = std::fabs(x);
+        if (s < 0.5f)
+            return 0.75f - s * s;
+        if (s <= 1.5f)
+        {
+            const float t = s - 1.5f;
+            return 0.5f * (t * t);
+        }
+        return 0.0f;
+    }
+    case 3:
+        return a * filter_exp32((x * x) * b);
+    case 4:
+    {
+        const float s = std::fabs(x);
+        const float* c = s <= 1.0f ? f.cubic : f.cubic + 4;
+        if (s > 2.0f)
+            return 0.0f;
+        return std::fma(std::fma(std::fma(c[0], s, c[1]), s, c[2]), s, c[3]);
+    }
+    default:
+    {
+        const float s = std::fabs(x);
+        if (s == 0.0f)
+            return 1.0f;
+        if (s > r)
+            return 0.0f;
+        return filter_sinc32(s) * filter_sinc32(s / r);
+    }
+    }
+}
+
 // The device's PATH render (pathtrace.cu) path by path: generate, then
 // extend/shade per segment, then accumulate per pixel in sample order.
 void render_path32(const Scene32& s, const Camera32& cam, const PathSettings32& ps, uint64_t width,
@@ -473,8 +591,7 @@ void render_path32(const Scene32& s, const Camera32& cam, const PathSettings32& 
         omp_set_num_threads(threads);
     const int n = ps.n, P = ps.P;
     const int nn = n * n;
-    const float wx = 1.0f / (2.0f * ps.rx);
-    const float wy = 1.0f / (2.0f * ps.ry);
+    const Filter32 flt = filter32(ps.filterType, ps.rx, ps.ry);
     uint64_t totalRays = 0;
     #pragma omp parallel for schedule(dynamic, 64) reduction(+ : totalRays)
     for (int64_t pl = 0; pl < int64_t(count); ++pl)
@@ -514,11 +631,9 @@ void render_path32(const Scene32& s, const Camera32& cam, const PathSettings32& 
                     sx = 0.5f;
                     sy = 0.5f;
                 }
-                float ox = ((sx - 0.5f) * 2.0f) * ps.rx;
-                float oy = ((sy - 0.5f) * 2.0f) * ps.ry;
-                float bw = (ox >= -ps.rx && ox < ps.rx) ? wx : 0.0f;
-                float bh = (oy >= -ps.ry && oy < ps.ry) ? wy : 0.0f;
-                w = bw * bh;
+                float ox = ((sx - 0.5f) * 2.0f) * flt.rx;
+                float oy = ((sy - 0.5f) * 2.0f) * flt.ry;
+                w = filter_weight32(flt, ox, flt.rx, flt.ax, flt.bx) * filter_weight32(flt, oy, flt.ry, flt.ay, flt.by);
                 px = px + ox;
                 py = py + oy;
             }

@@ -40,6 +40,7 @@ struct PathSettings32
     int n = 1;          // multiSampleCountSqrt
     int P = 1;          // pathSampleCount
     int samplerType = 4;
+    int filterType = 0;  // rc_filter_type; rx, ry = BOX radius
     float rx = 0.5f, ry = 0.5f;
     float rayStartOffset = 0.00001f;
     int maxPathLength = 4;
@@ -60,6 +61,16 @@ void cast32(const Scene32& s, int64_t n, const float* rays8, int anyHit, int ord
 void render_path32(const Scene32& s, const Camera32& cam, const PathSettings32& ps, uint64_t width,
                    uint64_t pixelStart, uint64_t count, float* film, uint64_t* counters, int threads);
 void sincos_turn(float x, float& s, float& c);
+// Film filter of the device (filters.cuh): radius and per-axis weight.
+struct Filter32
+{
+    int type;
+    float rx, ry, ax, ay, bx, by;
+    float cubic[8];
+};
+Filter32 filter32(int type, float boxRx, float boxRy);
+float filter_weight32(const Filter32& f, float x, float r, float a, float b);
+float filter_exp32(float t);
 uint32_t stream_key(uint64_t seed, uint32_t frame, uint64_t pixel, uint32_t sample);
 float stream_float(uint32_t key, uint32_t counter);
 uint64_t cmj_permute32(uint64_t i, uint64_t l, uint64_t p);

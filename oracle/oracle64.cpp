@@ -434,6 +434,79 @@ double cmj_component(uint64_t x, uint64_t y, uint64_t n, uint64_t permutation, d
 
 // Tracer::run (Tracer.cpp:58-113) + generateMultiSamples (:115-144) +
 // PathTracer::trace / traceRecursive (PathTracer.cpp:13-75) + Film::addSample.
+void filter_radius64(int type, const double* boxRadius, double* radius)
+{
+    switch (type)
+    {
+    case 0: radius[0] = boxRadius[0]; radius[1] = boxRadius[1]; break;   // BoxFilter(0.5, 0.5) or as set
+    case 1: radius[0] = radius[1] = 1.0; break;                          // TentFilter(1, 1)
+    case 2: radius[0] = radius[1] = 1.5; break;                          // BellFilter
+    case 3: radius[0] = radius[1] = (7.43384 * 1.0) / 2.0; break;        // GaussianFilter(1, 1)
+    default: radius[0] = radius[1] = 2.0; break;                         // Mitchell, LanczosSinc(2, 2)
+    }
+}
+
+// One axis of the filter at offset x; boxRadius points at that axis's BOX radius.
+double filter_weight64(int type, const double* boxRadius, double x)
+{
+    const double pi = 3.14159265358979323846;
+    switch (type)
+    {
+    case 0:
+    {
+        const double r = boxRadius[0];
+        return (x >= -r && x < r) ? 1.0 / (2.0 * r) : 0.0;
+    }
+    case 1:
+    {
+        const double inv = 1.0 / 1.0;
+        const double s = std::abs(x * inv);
+        return (s < 1.0 ? 1.0 - s : 0.0) * inv;
+    }
+    case 2:
+    {
+        const double s = std::abs(x);
+        if (s < 0.5)
+            return 0.75 - s * s;
+        if (s <= 1.5)
+            return 0.5 * std::pow(s - 1.5, 2.0);
+        return 0.0;
+    }
+    case 3:
+    {
+        const double sd = 1.0;
+        const double alpha = 1.0 / (std::sqrt(2.0 * pi) * sd);
+        const double beta = -1.0 / (2.0 * sd * sd);
+        return alpha * std::exp(x * x * beta);
+    }
+    case 4:
+    {
+        const double B = 1.0 / 3.0, C = 1.0 / 3.0;
+        const double s = std::abs(x);
+        if (s <= 1.0)
+            return ((12.0 - 9.0 * B - 6.0 * C) * (s * s * s) + (-18.0 + 12.0 * B + 6.0 * C) * (s * s) +
+                    (6.0 - 2.0 * B)) *
+                   (1.0 / 6.0);
+        if (s <= 2.0)
+            return ((-B - 6.0 * C) * (s * s * s) + (6.0 * B + 30.0 * C) * (s * s) + (-12.0 * B - 48.0 * C) * s +
+                    (8.0 * B + 24.0 * C)) *
+                   (1.0 / 6.0);
+        return 0.0;
+    }
+    default:
+    {
+        const double size = 2.0;
+        const double s = std::abs(x);
+        if (s == 0.0)
+            return 1.0;
+        if (s > size)
+            return 0.0;
+        auto sinc = [pi](double v) { return std::sin(pi * v) / (pi * v); };
+        return sinc(s) * sinc(s / size);
+    }
+    }
+}
+
 void render_path64(const Scene64& s, const Camera64& cam, const PathSettings64& ps, uint64_t width, uint64_t pixelStart,
                    uint64_t pixelCount, double* film, int threads, uint32_t seed, uint64_t* raysOut)
 {
@@ -481,8 +554,8 @@ void render_path64(const Scene64& s, const Camera64& cam, const PathSettings64& 
         uint64_t permutation = randomPermutation(gen);
         uint64_t n = ps.multiSampleCountSqrt;
         std::uniform_real_distribution<double> uni(0.0, 1.0);
-        double wx = 1.0 / (2.0 * ps.filterRadius[0]);
-        double wy = 1.0 / (2.0 * ps.filterRadius[1]);
+        double rad[2];
+        filter_radius64(ps.filterType, ps.filterRadius, rad);
         for (uint64_t sy = 0; sy < n; ++sy)
         {
             for (uint64_t sx = 0; sx < n; ++sx)
@@ -505,11 +578,11 @@ void render_path64(const Scene64& s, const Camera64& cam, const PathSettings64& 
                     smx = 0.5;
                     smy = 0.5;
                 }
-                double ox = (smx - 0.5) * 2.0 * ps.filterRadius[0];
-                double oy = (smy - 0.5) * 2.0 * ps.filterRadius[1];
+                double ox = (smx - 0.5) * 2.0 * rad[0];
+                double oy = (smy - 0.5) * 2.0 * rad[1];
                 RGB c = trace(x + ox, y + oy);
-                double w = ((ox >= -ps.filterRadius[0] && ox < ps.filterRadius[0]) ? wx : 0.0) *
-                           ((oy >= -ps.filterRadius[1] && oy < ps.filterRadius[1]) ? wy : 0.0);
+                double w = filter_weight64(ps.filterType, ps.filterRadius, ox) *
+                           filter_weight64(ps.filterType, ps.filterRadius + 1, oy);
                 fp[0] += c.r * w;
                 fp[1] += c.g * w;
                 fp[2] += c.b * w;

@@ -60,9 +60,15 @@ struct PathSettings64
     uint64_t pathSampleCount = 1;
     uint64_t multiSampleCountSqrt = 1;
     int samplerType = 4;
-    double filterRadius[2] = { 0.5, 0.5 };
+    int filterType = 0;                     // FilterType (Filter.h:10)
+    double filterRadius[2] = { 0.5, 0.5 };  // BOX only; the others use their defaults
     double rayStartOffset = 0.00001;
 };
+
+// The reference's film filters in float64 (Rendering/Filters/*.cpp, default
+// constructors as Tracer.cpp:50-55 makes them): radius and per-axis weight.
+void filter_radius64(int type, const double* boxRadius, double* radius);
+double filter_weight64(int type, const double* boxRadius, double x);
 
 Ray64 make_ray64(V3d o, V3d d);
 Ray64 camera_ray64(const Camera64& c, double px, double py);

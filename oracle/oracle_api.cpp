@@ -194,9 +194,11 @@ double or64_raycast(void* hp, const double* cam, uint64_t width, uint64_t pixelS
 
 double or64_render_path(void* hp, const double* cam, uint64_t width, uint64_t pixelStart, uint64_t count,
                         uint64_t maxPathLength, uint64_t pathSampleCount, uint64_t msSqrt, int samplerType, double rx,
-                        double ry, double rayStartOffset, uint32_t seed, int threads, double* film, uint64_t* rays)
+                        double ry, double rayStartOffset, uint32_t seed, int threads, double* film, uint64_t* rays,
+                        int filterType)
 {
     PathSettings64 ps;
+    ps.filterType = filterType;
     ps.maxPathLength = maxPathLength;
     ps.pathSampleCount = pathSampleCount;
     ps.multiSampleCountSqrt = msSqrt;
@@ -246,9 +248,11 @@ void or32_camera_rays(const float* cam, uint64_t width, uint64_t pixelStart, uin
 
 void or32_render_path(void* hp, const float* cam, uint64_t width, uint64_t pixelStart, uint64_t count, int n, int P,
                       int samplerType, float rx, float ry, float rayStartOffset, int maxPathLength, int rrDepth,
-                      int order, uint64_t seed, uint32_t frame, float* film, uint64_t* counters, int threads)
+                      int order, uint64_t seed, uint32_t frame, float* film, uint64_t* counters, int threads,
+                      int filterType)
 {
     PathSettings32 ps;
+    ps.filterType = filterType;
     ps.n = n;
     ps.P = P;
     ps.samplerType = samplerType;
@@ -271,6 +275,32 @@ void or64_cmj(uint64_t x, uint64_t y, uint64_t n, uint64_t permutation, double j
 }
 
 uint64_t or32_cmj_permute(uint64_t i, uint64_t l, uint64_t p) { return cmj_permute32(i, l, p); }
+
+// Film filter weights of one axis at offsets x (BOX radius 0.5 for type 0):
+// float32 twin of the device and float64 port of the reference.
+void or32_filter_weight(int type, int64_t n, const float* x, float* out, float* radius)
+{
+    Filter32 f = filter32(type, 0.5f, 0.5f);
+    for (int64_t i = 0; i < n; ++i)
+        out[i] = filter_weight32(f, x[i], f.rx, f.ax, f.bx);
+    *radius = f.rx;
+}
+
+void or64_filter_weight(int type, int64_t n, const double* x, double* out, double* radius)
+{
+    const double box[2] = { 0.5, 0.5 };
+    double rad[2];
+    filter_radius64(type, box, rad);
+    for (int64_t i = 0; i < n; ++i)
+        out[i] = filter_weight64(type, box, x[i]);
+    *radius = rad[0];
+}
+
+void or32_filter_exp(int64_t n, const float* t, float* out)
+{
+    for (int64_t i = 0; i < n; ++i)
+        out[i] = filter_exp32(t[i]);
+}
 
 void or32_sincos_turn(int64_t n, const float* x, float* s, float* c)
 {

@@ -39,6 +39,7 @@
 #include "Rendering/Film.h"
 #include "Rendering/Image.h"
 #include "Rendering/Samplers/CMJSampler.h"
+#include "Rendering/Filters/Filter.h"
 #include "Rendering/ToneMappers/ReinhardToneMapper.h"
 #include "Math/MathUtils.h"
 #include "Math/Vector2.h"
@@ -549,6 +550,16 @@ void ref_cmj_pattern(uint64_t n, uint64_t permutation, uint32_t seed, double* ou
             out[(y * n + x) * 2 + 0] = s.x;
             out[(y * n + x) * 2 + 1] = s.y;
         }
+}
+
+// The reference's film filter (Filter::getFilter, default constructors as
+// the Tracer makes them, Tracer.cpp:50-55): weight of one axis at offsets x.
+void ref_filter_weight(int type, int64_t n, const double* x, double* out, double* radius)
+{
+    std::unique_ptr<Filter> f = Filter::getFilter(FilterType(type));
+    for (int64_t i = 0; i < n; ++i)
+        out[i] = f->getWeightX(x[i]);
+    *radius = f->getRadiusX();
 }
 
 }

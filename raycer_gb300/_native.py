@@ -35,6 +35,11 @@ RC_SAMPLER_CENTER = 0
 RC_SAMPLER_RANDOM = 1
 RC_SAMPLER_CMJ = 4
 RC_FILTER_BOX = 0
+RC_FILTER_TENT = 1
+RC_FILTER_BELL = 2
+RC_FILTER_GAUSSIAN = 3
+RC_FILTER_MITCHELL = 4
+RC_FILTER_LANCZOS_SINC = 5
 RC_TONEMAP_PASSTHROUGH = 0
 RC_TONEMAP_REINHARD = 3
 RC_ORDER_REFERENCE = 0

@@ -93,6 +93,7 @@ inline SceneArrays sceneArraysFrom(const Raycer::Scene& scene)
     a.general.path_sample_count = int32_t(g.pathSampleCount);
     a.general.multi_sample_count_sqrt = int32_t(g.multiSampleCountSqrt);
     a.general.multi_sampler_type = int32_t(g.multiSamplerType);
+    a.general.filter_type = int32_t(g.multiSamplerFilterType);  // same enum order (Filter.h:10)
     a.general.ray_start_offset = float(g.rayStartOffset);
     a.general.background[0] = float(g.backgroundColor.r);
     a.general.background[1] = float(g.backgroundColor.g);

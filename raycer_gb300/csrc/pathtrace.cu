@@ -27,6 +27,7 @@
 
 #include <cfloat>
 
+#include "filters.cuh"
 #include "pathtrace.h"
 #include "sampling.cuh"
 #include "traverse.cuh"
@@ -97,12 +98,6 @@ __device__ __forceinline__ SlotInfo slot_info(const PathChunk& ch, const PathSce
     return si;
 }
 
-__device__ __forceinline__ float box_weight(float x, float r, float w)
-{
-    // BoxFilter::getWeightX (BoxFilter.cpp:23-29)
-    return (x >= -r && x < r) ? w : 0.0f;
-}
-
 __global__ void __launch_bounds__(256) k_generate(PassParams p)
 {
     uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -159,9 +154,9 @@ __global__ void __launch_bounds__(256) k_generate(PassParams p)
             sy = 0.5f;
         }
         // sampleOffset = (sample - 0.5) * 2 * radius (Tracer.cpp:138)
-        float ox = __fmul_rn(__fmul_rn(__fsub_rn(sx, 0.5f), 2.0f), sc.rx);
-        float oy = __fmul_rn(__fmul_rn(__fsub_rn(sy, 0.5f), 2.0f), sc.ry);
-        w = __fmul_rn(box_weight(ox, sc.rx, sc.wx), box_weight(oy, sc.ry, sc.wy));
+        float ox = __fmul_rn(__fmul_rn(__fsub_rn(sx, 0.5f), 2.0f), sc.filter.rx);
+        float oy = __fmul_rn(__fmul_rn(__fsub_rn(sy, 0.5f), 2.0f), sc.filter.ry);
+        w = filter_weight(sc.filter, ox, oy);
         px = __fadd_rn(px, ox);
         py = __fadd_rn(py, oy);
     }

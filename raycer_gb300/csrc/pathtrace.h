@@ -18,6 +18,16 @@
 namespace rcx
 {
 
+// Film reconstruction filter (filters.cuh) with its per-axis constants.
+struct FilterSpec
+{
+    int type;        // rc_filter_type
+    float rx, ry;    // radius: camera samples are offset within [-r, r)
+    float ax, ay;    // BOX 1/(2r), TENT 1/r, GAUSSIAN alpha
+    float bx, by;    // GAUSSIAN beta
+    float cubic[8];  // MITCHELL: |x| <= 1 and 1 < |x| <= 2 cubics, highest power first
+};
+
 // Everything a slot of one scene needs (device memory, one per scene).
 struct PathScene
 {
@@ -30,8 +40,7 @@ struct PathScene
     int P;                // pathSampleCount
     int spp;              // n * n * P slots per pixel
     int samplerType;
-    float rx, ry;         // box filter radius
-    float wx, wy;         // box filter weight per axis: 1 / (2 r)
+    FilterSpec filter;
     float rayStartOffset;
     int maxPathLength;
     int rrDepth;          // 0 = no Russian roulette
@@ -123,6 +132,9 @@ cudaError_t launch_nrc_targets(const PassParams& p, cudaStream_t stream);
 // Reinhard / passthrough resolve of the film into out (float4 per pixel).
 // partials needs tone_partials_bytes(pixels) bytes.
 size_t tone_partials_bytes(uint64_t pixels);
+// The filter record of a General record (the reference's filter constructors'
+// defaults; BOX takes filter_radius).
+FilterSpec filter_spec(const rc_general& g);
 cudaError_t launch_tonemap(const float4* film, uint64_t pixels, int type, int applyGamma, int shouldClamp,
                            double gamma, double key, void* partials, float4* out, cudaStream_t stream, int numSMs);
 cudaError_t launch_linear(const float4* film, uint64_t pixels, float4* out, cudaStream_t stream);

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -89,6 +90,57 @@ void release_render_buffers(rc_tracer* h)
     h->pathSlots = 0;
 }
 
+FilterSpec filter_spec(const rc_general& g)
+{
+    FilterSpec f{};
+    f.type = g.filter_type;
+    switch (g.filter_type)
+    {
+    case RC_FILTER_BOX:
+        // BoxFilter::setRadius (BoxFilter.cpp:15-21): weight = 1 / (2 r)
+        f.rx = g.filter_radius[0];
+        f.ry = g.filter_radius[1];
+        f.ax = 1.0f / (2.0f * f.rx);
+        f.ay = 1.0f / (2.0f * f.ry);
+        break;
+    case RC_FILTER_TENT:
+        // TentFilter() radius 1 (TentFilter.h:16)
+        f.rx = f.ry = 1.0f;
+        f.ax = f.ay = 1.0f;
+        break;
+    case RC_FILTER_BELL:
+        f.rx = f.ry = 1.5f;  // BellFilter.cpp:23-27
+        break;
+    case RC_FILTER_GAUSSIAN:
+    {
+        // GaussianFilter(1, 1): alpha = 1 / (sqrt(2 pi) sd), beta = -1 / (2 sd^2),
+        // radius = 7.43384 sd / 2 (GaussianFilter.cpp:12-21)
+        const double sd = 1.0;
+        f.ax = f.ay = float(1.0 / (std::sqrt(2.0 * 3.14159265358979323846) * sd));
+        f.bx = f.by = float(-1.0 / (2.0 * sd * sd));
+        f.rx = f.ry = float((7.43384 * sd) / 2.0);
+        break;
+    }
+    case RC_FILTER_MITCHELL:
+    {
+        // MitchellFilter(1/3, 1/3), radius 2 (MitchellFilter.h:16, .cpp:8-36):
+        // the two cubics with the 1/6 folded in
+        const double B = 1.0 / 3.0, C = 1.0 / 3.0;
+        const double k[8] = { (12.0 - 9.0 * B - 6.0 * C) / 6.0, (-18.0 + 12.0 * B + 6.0 * C) / 6.0, 0.0,
+                              (6.0 - 2.0 * B) / 6.0, (-B - 6.0 * C) / 6.0, (6.0 * B + 30.0 * C) / 6.0,
+                              (-12.0 * B - 48.0 * C) / 6.0, (8.0 * B + 24.0 * C) / 6.0 };
+        for (int i = 0; i < 8; ++i)
+            f.cubic[i] = float(k[i]);
+        f.rx = f.ry = 2.0f;
+        break;
+    }
+    default:
+        f.rx = f.ry = 2.0f;  // LanczosSincFilter(2, 2)
+        break;
+    }
+    return f;
+}
+
 // Fills the per-scene record the pass kernels read (pathtrace.h).
 PathScene path_scene(const rc_tracer* h, uint64_t pixelStart)
 {
@@ -119,11 +171,7 @@ PathScene path_scene(const rc_tracer* h, uint64_t pixelStart)
     ps.P = g.path_sample_count;
     ps.spp = g.multi_sample_count_sqrt * g.multi_sample_count_sqrt * g.path_sample_count;
     ps.samplerType = g.multi_sampler_type;
-    ps.rx = g.filter_radius[0];
-    ps.ry = g.filter_radius[1];
-    // BoxFilter::setRadius (BoxFilter.cpp:15-21): weight = 1 / (2 r).
-    ps.wx = 1.0f / (2.0f * g.filter_radius[0]);
-    ps.wy = 1.0f / (2.0f * g.filter_radius[1]);
+    ps.filter = filter_spec(g);
     ps.rayStartOffset = g.ray_start_offset;
     ps.maxPathLength = g.max_path_length;
     ps.rrDepth = g.russian_roulette_depth;

@@ -687,10 +687,10 @@ rc_status rc_set_general(rc_tracer* h, const rc_general* g)
     if (g->multi_sampler_type != RC_SAMPLER_CMJ && g->multi_sampler_type != RC_SAMPLER_RANDOM &&
         g->multi_sampler_type != RC_SAMPLER_CENTER)
         return fail(h, RC_UNSUPPORTED, "set_general: multi sampler must be CENTER, RANDOM or CMJ");
-    if (g->filter_type != RC_FILTER_BOX)
-        return fail(h, RC_UNSUPPORTED, "set_general: only the box filter is supported");
-    if (!(g->filter_radius[0] > 0.0f) || !(g->filter_radius[1] > 0.0f))
-        return fail(h, RC_INVALID_ARG, "set_general: filter radius must be > 0");
+    if (g->filter_type < RC_FILTER_BOX || g->filter_type > RC_FILTER_LANCZOS_SINC)
+        return fail(h, RC_INVALID_ARG, "set_general: unknown filter type");
+    if (g->filter_type == RC_FILTER_BOX && (!(g->filter_radius[0] > 0.0f) || !(g->filter_radius[1] > 0.0f)))
+        return fail(h, RC_INVALID_ARG, "set_general: box filter radius must be > 0");
     if (g->russian_roulette_depth < 0 || (g->flags & ~int32_t(RC_GENERAL_SKY)) != 0)
         return fail(h, RC_INVALID_ARG, "set_general: invalid russian_roulette_depth / flags");
     h->general = *g;
@@ -730,14 +730,13 @@ void rc_general_defaults(rc_general* g, int32_t tracer_type)
     if (!g)
         return;
     std::memset(g, 0, sizeof(*g));
-    // Scene::General defaults (Scene.h:89-108); the film filter is BOX here
-    // (the reference defaults to MITCHELL, which this build does not have).
+    // Scene::General defaults (Scene.h:89-108).
     g->tracer_type = tracer_type;
     g->max_path_length = 3;
     g->path_sample_count = 1;
     g->multi_sample_count_sqrt = 1;
     g->multi_sampler_type = RC_SAMPLER_CMJ;
-    g->filter_type = RC_FILTER_BOX;
+    g->filter_type = RC_FILTER_MITCHELL;
     g->filter_radius[0] = 0.5f;
     g->filter_radius[1] = 0.5f;
     g->ray_start_offset = 0.00001f;

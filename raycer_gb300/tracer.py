@@ -74,6 +74,10 @@ def camera_record(desc: SceneDesc, width: int | None = None, height: int | None 
     return cam
 
 
+FILTERS = {"box": N.RC_FILTER_BOX, "tent": N.RC_FILTER_TENT, "bell": N.RC_FILTER_BELL,
+           "gaussian": N.RC_FILTER_GAUSSIAN, "mitchell": N.RC_FILTER_MITCHELL, "lanczos": N.RC_FILTER_LANCZOS_SINC}
+
+
 def general_record(desc: SceneDesc, seed: int = 1) -> N.rc_general:
     s = desc.settings
     g = N.rc_general()
@@ -86,6 +90,11 @@ def general_record(desc: SceneDesc, seed: int = 1) -> N.rc_general:
     g.multi_sampler_type = {"cmj": N.RC_SAMPLER_CMJ, "random": N.RC_SAMPLER_RANDOM,
                             "center": N.RC_SAMPLER_CENTER}[s.get("sampler", "cmj")]
     g.russian_roulette_depth = int(s.get("russian_roulette_depth", 0))
+    # the scene descriptions of this package default to the box filter; the
+    # C records' default (rc_general_defaults) is the reference's MITCHELL
+    g.filter_type = FILTERS[s.get("filter", "box")]
+    if "filter_radius" in s:
+        g.filter_radius[:] = [float(x) for x in s["filter_radius"]]
     if s.get("miss_radiance") is not None:
         # GPU extension: escaping paths see a uniform sky of this radiance
         g.flags |= N.RC_GENERAL_SKY

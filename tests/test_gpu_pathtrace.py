@@ -29,3 +29,24 @@ def test_film_bit_exact(ms, P, depth, sampler):
     ref, _ = orc.render_path32(cam, sc.width, sc.width * sc.height, ms, P, sampler, (0.5, 0.5), 1e-5, depth, 0, 1,
                                11, 0)
     assert np.array_equal(film, ref), f"{(film != ref).any(axis=1).sum()} pixels differ"
+
+
+@pytest.mark.parametrize("filt,ftype", [("tent", 1), ("bell", 2), ("gaussian", 3), ("mitchell", 4), ("lanczos", 5)])
+@pytest.mark.parametrize("ms,sampler", [(2, 4), (3, 1)])
+def test_film_bit_exact_filters(filt, ftype, ms, sampler):
+    sc = small_room(width=40, height=30)
+    sc.settings.update(multi_sample_count_sqrt=ms, path_sample_count=1, max_path_length=4, filter=filt,
+                       sampler={4: "cmj", 1: "random"}[sampler])
+    with CudaTracer(0) as t:
+        t.initializeBuffers(sc, seed=12)
+        t.initializeImageBuffers(sc.width, sc.height)
+        st = TracerState(scene=sc, filmWidth=sc.width, filmHeight=sc.height, pixelCount=sc.width * sc.height)
+        t.run(st)
+        film = t.read_film()
+        cam = camera_floats(camera_record(sc))
+    orc = oracle.Oracle(sc)
+    ref, _ = orc.render_path32(cam, sc.width, sc.width * sc.height, ms, 1, sampler, (0.5, 0.5), 1e-5, 4, 0, 1,
+                               12, 0, filter_type=ftype)
+    assert np.array_equal(film, ref), f"{(film != ref).any(axis=1).sum()} pixels differ"
+    if ftype in (4, 5):
+        assert (film[:, 3] != film[0, 3]).any()  # weights vary with the sample offsets
