@@ -45,7 +45,8 @@ typedef enum rc_status
     RC_TIMEOUT = 5,      /* a kernel's iteration budget ran out            */
     RC_NOT_READY = 6,    /* call order: e.g. render before upload/resize   */
     RC_UNSUPPORTED = 7,  /* valid in the reference, not in this build      */
-    RC_DEVICE_ERROR = 8  /* a kernel reported an error status (e.g. stack) */
+    RC_DEVICE_ERROR = 8, /* a kernel reported an error status (e.g. stack) */
+    RC_IO = 9            /* a file could not be read / written or is invalid */
 } rc_status;
 
 typedef struct rc_tracer rc_tracer; /* opaque handle: one tracer on one GPU */
@@ -422,6 +423,38 @@ rc_status rc_get_stats(const rc_tracer* h, rc_stats* out);
 /* The handle's CUDA stream (cudaStream_t) as an opaque pointer. */
 void* rc_stream(rc_tracer* h);
 rc_status rc_sync(rc_tracer* h);
+
+/* ------------------------------------------------------------------------ */
+/* Binary scene + BVH cache files (replace Scene::saveToFile / loadFromFile, */
+/* Scene.cpp:67-183, and FlatBVH's serialised nodes restored by              */
+/* FlatBVH::restore, FlatBVH.h:98-105, for this path; the format is this     */
+/* build's own, not cereal's). A file holds the flat BVH in the reference's */
+/* form, the primitive order and the device triangle / shading / material   */
+/* records: loading builds nothing. Every load validates the file (magic,   */
+/* version, sizes, a 64-bit checksum, the BVH's structure and depth, the    */
+/* triangle records) before it allocates device memory; RC_IO + message on  */
+/* failure.                                                                  */
+
+typedef struct rc_scene_file_info
+{
+    uint64_t triangles;
+    uint64_t materials;
+    uint64_t bvh_nodes;   /* flat (reference-form) nodes */
+    uint64_t bvh_depth;
+    double bounds[6];     /* root box: min xyz, max xyz */
+} rc_scene_file_info;
+
+/* Writes the uploaded scene of a handle. */
+rc_status rc_save_scene(rc_tracer* h, const char* path);
+/* Replaces the handle's scene with the file's (as rc_upload_scene would). */
+rc_status rc_load_scene(rc_tracer* h, const char* path);
+/* Host only (no GPU): builds the scene rc_upload_scene would upload and
+ * writes it. error (optional) receives a message on failure. */
+rc_status rc_write_scene_file(const double* vertices, const uint32_t* material_index, int64_t n,
+                              const rc_material* materials, int32_t material_count, uint32_t max_leaf_size,
+                              const char* path, char* error, int64_t error_capacity);
+/* Host only: validates a file and reports its contents. */
+rc_status rc_inspect_scene_file(const char* path, rc_scene_file_info* out, char* error, int64_t error_capacity);
 
 /* ------------------------------------------------------------------------ */
 /* Neural radiance cache (GPU-only extension; no counterpart in the          */

@@ -22,11 +22,12 @@ RC_TIMEOUT = 5
 RC_NOT_READY = 6
 RC_UNSUPPORTED = 7
 RC_DEVICE_ERROR = 8
+RC_IO = 9
 
 STATUS_NAMES = {
     RC_OK: "RC_OK", RC_INVALID_ARG: "RC_INVALID_ARG", RC_OOM: "RC_OOM", RC_CUDA: "RC_CUDA",
     RC_CANCELLED: "RC_CANCELLED", RC_TIMEOUT: "RC_TIMEOUT", RC_NOT_READY: "RC_NOT_READY",
-    RC_UNSUPPORTED: "RC_UNSUPPORTED", RC_DEVICE_ERROR: "RC_DEVICE_ERROR",
+    RC_UNSUPPORTED: "RC_UNSUPPORTED", RC_DEVICE_ERROR: "RC_DEVICE_ERROR", RC_IO: "RC_IO",
 }
 
 RC_TRACER_RAY = 0
@@ -121,6 +122,11 @@ class rc_nrc_stats(C.Structure):
                 ("last_loss", C.c_float), ("reserved", C.c_float), ("train_ms", C.c_double)]
 
 
+class rc_scene_file_info(C.Structure):
+    _fields_ = [("triangles", C.c_uint64), ("materials", C.c_uint64), ("bvh_nodes", C.c_uint64),
+                ("bvh_depth", C.c_uint64), ("bounds", C.c_double * 6)]
+
+
 RC_GENERAL_SKY = 1
 RC_NRC_PARAMS = 20992
 RC_NRC_QUERY_FLOATS = 12
@@ -189,6 +195,10 @@ PROTOTYPES = {
     "rc_nrc_read_samples": (i32, [P, P, i64, C.POINTER(i64)]),
     "rc_nrc_get_stats": (i32, [P, C.POINTER(rc_nrc_stats)]),
     "rc_film_accumulate_f64": (i32, [P, P, i32]),
+    "rc_save_scene": (i32, [P, C.c_char_p]),
+    "rc_load_scene": (i32, [P, C.c_char_p]),
+    "rc_write_scene_file": (i32, [P, P, i64, P, i32, u32, C.c_char_p, C.c_char_p, i64]),
+    "rc_inspect_scene_file": (i32, [C.c_char_p, C.POINTER(rc_scene_file_info), C.c_char_p, i64]),
     "rc_film_rmse_f64": (i32, [P, P, C.POINTER(C.c_double)]),
 }
 

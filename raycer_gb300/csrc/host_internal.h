@@ -16,6 +16,19 @@
 namespace rcx
 {
 
+// Device-layout records of one scene built on the host: the reference-form
+// flat BVH and primitive order, triangles and shading records in BVH order,
+// materials. The device nodes are derived from `flat` at upload.
+struct HostScene
+{
+    std::vector<BuildNode> flat;
+    std::vector<uint32_t> order;
+    std::vector<DevTri> tris;
+    std::vector<DevShade> shade;
+    std::vector<DevMat> mats;
+    uint32_t depth = 0;
+};
+
 // Neural radiance cache state of a handle (nrc_host.cpp).
 struct NrcState
 {
@@ -138,6 +151,11 @@ rc_status raycast_into(rc_tracer* h, const rc_ray* dRays, uint64_t pixelStart, u
 rc_status render_raycast(rc_tracer* h, uint64_t pixelStart, uint64_t count, const rc_ray* dRays);
 rc_status render_path(rc_tracer* h, uint64_t pixelStart, uint64_t count, const volatile int32_t* cancel);
 void release_render_buffers(rc_tracer* h);
+// Scene construction (tracer_host.cpp), shared with the scene files (scene_file.cpp).
+void build_host_scene(const double* v, const uint32_t* matIdx, int64_t n, const rc_material* mats, int32_t matCount,
+                      std::vector<BuildNode>&& nodes, std::vector<uint32_t>&& order, uint32_t depth, HostScene& hs);
+rc_status upload_host_scene(rc_tracer* h, HostScene&& hs);
+bool validate_flat_bvh(const std::vector<BuildNode>& nodes, uint64_t n, uint32_t& depth, std::string& err);
 // Grow-only device buffer (frees the old one); counts into deviceBytes.
 rc_status device_grow(rc_tracer* h, void** ptr, size_t* cap, size_t bytes, const char* what);
 

@@ -217,29 +217,26 @@ bool validate_flat(const std::vector<BuildNode>& nodes, uint64_t n, uint32_t& de
     return true;
 }
 
-// Flattens the reference-form BVH to the device layout and uploads it.
-rc_status upload_common(rc_tracer* h, const double* v, const uint32_t* matIdx, int64_t n, const rc_material* mats,
-                        int32_t matCount, std::vector<BuildNode>&& nodes, std::vector<uint32_t>&& order,
-                        uint32_t depth)
-{
-    if (depth > uint32_t(kMaxStack))
-        return fail(h, RC_UNSUPPORTED, "BVH depth " + std::to_string(depth) + " exceeds the traversal stack (" +
-                                           std::to_string(kMaxStack) + ")");
+}  // namespace
 
-    // Inner nodes get compact indices in preorder.
+namespace rcx
+{
+
+// Device nodes from a validated reference-form flat BVH: inner nodes get
+// compact indices in preorder, leaves fold into their parents' links.
+void device_nodes(const std::vector<BuildNode>& nodes, std::vector<DevNode>& dn, int32_t& rootLink, uint64_t& inner)
+{
     std::vector<int32_t> innerIndex(nodes.size(), -1);
-    int32_t inner = 0;
+    int32_t count = 0;
     for (size_t i = 0; i < nodes.size(); ++i)
         if (nodes[i].rightOffset != 0)
-            innerIndex[i] = inner++;
-
+            innerIndex[i] = count++;
     auto link = [&](size_t i) -> int32_t {
         if (nodes[i].rightOffset != 0)
             return innerIndex[i];
         return ~int32_t((nodes[i].start << kLeafCountBits) | nodes[i].count);
     };
-
-    std::vector<DevNode> dn(size_t(std::max(inner, 1)));
+    dn.assign(size_t(std::max(count, 1)), DevNode{});
     for (size_t i = 0; i < nodes.size(); ++i)
     {
         if (nodes[i].rightOffset == 0)
@@ -254,9 +251,18 @@ rc_status upload_common(rc_tracer* h, const double* v, const uint32_t* matIdx, i
         d.z01 = make_float4(float(L.bmin[2]), float(L.bmax[2]), float(R.bmin[2]), float(R.bmax[2]));
         d.link = make_int4(link(l), link(r), 0, 0);
     }
+    rootLink = nodes[0].rightOffset != 0 ? 0 : link(0);
+    inner = uint64_t(count);
+}
 
-    std::vector<DevTri> dt(static_cast<size_t>(n));
-    std::vector<DevShade> ds(static_cast<size_t>(n));
+// Triangle, shading and material records of a scene in BVH order.
+void build_host_scene(const double* v, const uint32_t* matIdx, int64_t n, const rc_material* mats, int32_t matCount,
+                      std::vector<BuildNode>&& nodes, std::vector<uint32_t>&& order, uint32_t depth, HostScene& hs)
+{
+    std::vector<DevTri>& dt = hs.tris;
+    std::vector<DevShade>& ds = hs.shade;
+    dt.resize(static_cast<size_t>(n));
+    ds.resize(static_cast<size_t>(n));
     for (int64_t s = 0; s < n; ++s)
     {
         uint32_t p = order[size_t(s)];
@@ -290,7 +296,7 @@ rc_status upload_common(rc_tracer* h, const double* v, const uint32_t* matIdx, i
         sh.bt = make_float4(float(bit.x), float(bit.y), float(bit.z), 0.0f);
     }
 
-    std::vector<DevMat> dm(static_cast<size_t>(matCount));
+    hs.mats.resize(static_cast<size_t>(matCount));
     for (int32_t i = 0; i < matCount; ++i)
     {
         const rc_material& m = mats[i];
@@ -298,40 +304,78 @@ rc_status upload_common(rc_tracer* h, const double* v, const uint32_t* matIdx, i
                          (m.invert_normal ? kMatInvertNormal : 0u);
         float ff;
         std::memcpy(&ff, &flags, 4);
-        dm[size_t(i)].diffuse = make_float4(m.diffuse[0], m.diffuse[1], m.diffuse[2], 0.0f);
-        dm[size_t(i)].emittance = make_float4(m.emittance[0], m.emittance[1], m.emittance[2], ff);
+        hs.mats[size_t(i)].diffuse = make_float4(m.diffuse[0], m.diffuse[1], m.diffuse[2], 0.0f);
+        hs.mats[size_t(i)].emittance = make_float4(m.emittance[0], m.emittance[1], m.emittance[2], ff);
     }
+    hs.depth = depth;
+    hs.flat = std::move(nodes);
+    hs.order = std::move(order);
+}
+
+// Uploads a host scene (its flat BVH already validated, depth within the stack).
+rc_status upload_host_scene(rc_tracer* h, HostScene&& hs)
+{
+    if (hs.depth > uint32_t(kMaxStack))
+        return fail(h, RC_UNSUPPORTED, "BVH depth " + std::to_string(hs.depth) + " exceeds the traversal stack (" +
+                                           std::to_string(kMaxStack) + ")");
+    std::vector<DevNode> dn;
+    int32_t rootLink = 0;
+    uint64_t inner = 0;
+    device_nodes(hs.flat, dn, rootLink, inner);
 
     release_scene(h);
     rc_status s;
     if ((s = dev_alloc(h, &h->dNodes, dn.size(), "allocate BVH nodes")) != RC_OK ||
-        (s = dev_alloc(h, &h->dTris, dt.size(), "allocate triangles")) != RC_OK ||
-        (s = dev_alloc(h, &h->dShade, ds.size(), "allocate shading records")) != RC_OK ||
-        (s = dev_alloc(h, &h->dMats, dm.size(), "allocate materials")) != RC_OK)
+        (s = dev_alloc(h, &h->dTris, hs.tris.size(), "allocate triangles")) != RC_OK ||
+        (s = dev_alloc(h, &h->dShade, hs.shade.size(), "allocate shading records")) != RC_OK ||
+        (s = dev_alloc(h, &h->dMats, hs.mats.size(), "allocate materials")) != RC_OK)
     {
         release_scene(h);
         return s;
     }
     h->innerCount = dn.size();
-    h->nTris = n;
-    h->nMats = matCount;
+    h->nTris = int64_t(hs.tris.size());
+    h->nMats = int32_t(hs.mats.size());
     RC_CUDA_TRY(h, cudaMemcpy(h->dNodes, dn.data(), dn.size() * sizeof(DevNode), cudaMemcpyHostToDevice),
                 "upload BVH nodes");
-    RC_CUDA_TRY(h, cudaMemcpy(h->dTris, dt.data(), dt.size() * sizeof(DevTri), cudaMemcpyHostToDevice),
+    RC_CUDA_TRY(h, cudaMemcpy(h->dTris, hs.tris.data(), hs.tris.size() * sizeof(DevTri), cudaMemcpyHostToDevice),
                 "upload triangles");
-    RC_CUDA_TRY(h, cudaMemcpy(h->dShade, ds.data(), ds.size() * sizeof(DevShade), cudaMemcpyHostToDevice),
+    RC_CUDA_TRY(h, cudaMemcpy(h->dShade, hs.shade.data(), hs.shade.size() * sizeof(DevShade), cudaMemcpyHostToDevice),
                 "upload shading records");
-    RC_CUDA_TRY(h, cudaMemcpy(h->dMats, dm.data(), dm.size() * sizeof(DevMat), cudaMemcpyHostToDevice),
+    RC_CUDA_TRY(h, cudaMemcpy(h->dMats, hs.mats.data(), hs.mats.size() * sizeof(DevMat), cudaMemcpyHostToDevice),
                 "upload materials");
 
-    h->rootLink = nodes[0].rightOffset != 0 ? 0 : ~int32_t((nodes[0].start << kLeafCountBits) | nodes[0].count);
-    h->bvhDepth = depth;
-    h->bvhInner = uint64_t(inner);
-    h->hostNodes = std::move(nodes);
-    h->hostOrder = std::move(order);
+    h->rootLink = rootLink;
+    h->bvhDepth = hs.depth;
+    h->bvhInner = inner;
+    h->hostNodes = std::move(hs.flat);
+    h->hostOrder = std::move(hs.order);
     h->sceneReady = true;
     return RC_OK;
 }
+
+bool validate_flat_bvh(const std::vector<BuildNode>& nodes, uint64_t n, uint32_t& depth, std::string& err)
+{
+    return validate_flat(nodes, n, depth, err);
+}
+
+// Flattens the reference-form BVH to the device layout and uploads it.
+rc_status upload_common(rc_tracer* h, const double* v, const uint32_t* matIdx, int64_t n, const rc_material* mats,
+                        int32_t matCount, std::vector<BuildNode>&& nodes, std::vector<uint32_t>&& order,
+                        uint32_t depth)
+{
+    if (depth > uint32_t(kMaxStack))
+        return fail(h, RC_UNSUPPORTED, "BVH depth " + std::to_string(depth) + " exceeds the traversal stack (" +
+                                           std::to_string(kMaxStack) + ")");
+    HostScene hs;
+    build_host_scene(v, matIdx, n, mats, matCount, std::move(nodes), std::move(order), depth, hs);
+    return upload_host_scene(h, std::move(hs));
+}
+
+}  // namespace rcx
+
+namespace
+{
 
 rc_status check_scene_args(rc_tracer* h, const double* v, const uint32_t* matIdx, int64_t n, const rc_material* mats,
                            int32_t matCount)

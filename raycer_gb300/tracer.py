@@ -159,6 +159,29 @@ class Film:
         return self.toneMappedImage
 
 
+def write_scene_file(scene: SceneDesc, path) -> None:
+    """Host-only: builds the scene's BVH and device records and writes a scene file."""
+    v = np.ascontiguousarray(scene.vertices, np.float64)
+    m = np.ascontiguousarray(scene.material_index, np.uint32)
+    mats = materials_array(scene.materials)
+    err = C.create_string_buffer(512)
+    st = N.lib().rc_write_scene_file(_ptr(v), _ptr(m), v.shape[0], mats, len(scene.materials),
+                                      int(scene.max_leaf_size), str(path).encode(), err, 512)
+    if st != N.RC_OK:
+        raise RaycerError(st, f"write_scene_file: {err.value.decode()}")
+
+
+def inspect_scene_file(path) -> dict:
+    """Validates a scene file (host only) and returns its counts and bounds."""
+    info = N.rc_scene_file_info()
+    err = C.create_string_buffer(512)
+    st = N.lib().rc_inspect_scene_file(str(path).encode(), C.byref(info), err, 512)
+    if st != N.RC_OK:
+        raise RaycerError(st, err.value.decode())
+    return {"triangles": info.triangles, "materials": info.materials, "bvh_nodes": info.bvh_nodes,
+            "bvh_depth": info.bvh_depth, "bounds": list(info.bounds)}
+
+
 class CudaTracer:
     """GPU tracer with the method shape of CLTracer (CLTracer.h:23-41)."""
 
@@ -213,8 +236,23 @@ class CudaTracer:
     def releaseImageBuffers(self) -> None:
         """Film buffers are released with the handle or replaced by the next resize."""
 
-    def initializeBuffers(self, scene: SceneDesc, seed: int = 1, prebuilt=None) -> None:
-        """CLTracer::initializeBuffers + CLScene::readSceneFull (CLTracer.cpp:173, CLScene.cpp:72)."""
+    def initializeBuffers(self, scene: SceneDesc, seed: int = 1, prebuilt=None, cache=None) -> None:
+        """CLTracer::initializeBuffers + CLScene::readSceneFull (CLTracer.cpp:173, CLScene.cpp:72).
+        cache: a scene file path; loaded when it holds a scene of this size, else
+        written after the upload."""
+        if cache is not None and prebuilt is None:
+            import os
+            if os.path.exists(cache):
+                try:
+                    info = inspect_scene_file(cache)
+                except RaycerError:
+                    info = None
+                if info and info["triangles"] == scene.triangle_count and info["materials"] == len(scene.materials):
+                    self.load_scene(cache, scene, seed)
+                    return
+            self.initializeBuffers(scene, seed)
+            self.save_scene(cache)
+            return
         v = np.ascontiguousarray(scene.vertices, np.float64)
         m = np.ascontiguousarray(scene.material_index, np.uint32)
         mats = materials_array(scene.materials)
@@ -228,6 +266,19 @@ class CudaTracer:
             st = self._lib.rc_upload_scene_prebuilt(self._h, _ptr(v), _ptr(m), v.shape[0], mats,
                                                     len(scene.materials), _ptr(nodes), nodes.shape[0], _ptr(order))
         self._check(st, "initializeBuffers")
+        self._scene = scene
+        self._seed = seed
+        self._set_general(scene)
+        self._set_tonemapper(scene)
+        self._set_lights(scene)
+
+    def save_scene(self, path) -> None:
+        """Writes the uploaded scene as a binary scene + BVH file."""
+        self._check(self._lib.rc_save_scene(self._h, str(path).encode()), "save_scene")
+
+    def load_scene(self, path, scene: SceneDesc, seed: int = 1) -> None:
+        """Loads a scene file; `scene` supplies the camera and render settings."""
+        self._check(self._lib.rc_load_scene(self._h, str(path).encode()), "load_scene")
         self._scene = scene
         self._seed = seed
         self._set_general(scene)
