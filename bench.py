@@ -52,7 +52,7 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--order", choices=["nearest", "reference"], default="nearest")
-    ap.add_argument("--workload", choices=["raycast", "batch", "nrc"], default="raycast",
+    ap.add_argument("--workload", choices=["raycast", "batch", "nrc", "build"], default="raycast",
                     help="raycast: the 1080p heightfield frame (default); batch: 64 rooms in one graph launch; "
                          "nrc: time to display RMSE 0.01, radiance cache vs plain path tracing")
     ap.add_argument("--gt-spp", type=int, default=4096, help="nrc: ground-truth samples per pixel")
@@ -495,6 +495,59 @@ def run_nrc(args, rank, world):
     return 0
 
 
+def run_build(args, rank, world):
+    """BVH build + upload time of the reference SAH builder (host) and the
+    GPU linear-BVH builder on the 1,045,506-triangle heightfield and the
+    5,141,506-triangle heightfield + blobs scene, with the RAY frame's
+    device time (1080p primary + shadow) on each tree."""
+    if rank != 0:
+        return 0
+    from raycer_gb300 import _native as N
+    from raycer_gb300 import scenes
+    from raycer_gb300.tracer import CudaTracer, TracerState
+
+    out = {}
+    for name, make in (("heightfield_1M", scenes.heightfield_scene), ("heightfield_blobs_5M",
+                                                                     scenes.heightfield_blobs_scene)):
+        sc = make()
+        sc.settings["tracer"] = "ray"
+        if sc.light_direction is None:
+            sc.light_direction = (-0.3, -1.0, -0.2)
+        row = {"triangles": sc.triangle_count}
+        for label, b in (("sah_host", N.RC_BUILDER_REFERENCE_SAH), ("lbvh_gpu", N.RC_BUILDER_GPU_LBVH)):
+            with CudaTracer(0) as t:
+                assert N.lib().rc_set_bvh_builder(t.handle, b) == N.RC_OK
+                builds = []
+                for _ in range(max(1, min(args.steps, 3))):
+                    t.initializeBuffers(sc)
+                    builds.append(t.stats()["build_ms"])
+                st = t.stats()
+                t.initializeImageBuffers(sc.width, sc.height)
+                state = TracerState(scene=sc, filmWidth=sc.width, filmHeight=sc.height,
+                                    pixelCount=sc.width * sc.height)
+                t.set_counting(True)
+                t.run(state)
+                counted = t.stats()
+                t.set_counting(False)
+                for _ in range(3):
+                    t.run(state)
+                ms, rays = [], []
+                for _ in range(10):
+                    t.run(state)
+                    s2 = t.stats()
+                    ms.append(s2["last_ms"])
+                    rays.append(s2["rays_traced"])
+                row[label] = {"build_ms": round(min(builds), 1), "bvh_inner_nodes": st["bvh_inner_nodes"],
+                              "bvh_depth": st["bvh_depth"],
+                              "frame_mrays_per_s": round(sum(rays) / (sum(ms) / 1e3) / 1e6, 1),
+                              "node_visits_per_ray": round(counted["node_visits"] / max(counted["rays_traced"], 1), 2),
+                              "tri_tests_per_ray": round(counted["tri_tests"] / max(counted["rays_traced"], 1), 2)}
+        out[name] = row
+    print(json.dumps({"metric": "BVH build ms", "workload": "build", "unit": "ms", "higher_is_better": False,
+                      "n_gpus": 1, "results": out}))
+    return 0
+
+
 def main():
     args = parse_args()
     rank, local_rank, world = dist_env()
@@ -502,6 +555,8 @@ def main():
         return run_batch(args, rank, world)
     if args.workload == "nrc":
         return run_nrc(args, rank, world)
+    if args.workload == "build":
+        return run_build(args, rank, world)
     if args.impl == "reference":
         return run_reference(args, rank, world)
     return run_ours(args, rank, local_rank, world)

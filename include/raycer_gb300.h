@@ -211,6 +211,7 @@ typedef struct rc_stats
     uint64_t stage_nodes[2];   /* when counting is on */
     uint64_t stage_tris[2];    /* when counting is on */
     double stage_ms[2];        /* device time from CUDA events around the stage's launches */
+    double build_ms;           /* host wall time of the last scene build + upload */
 } rc_stats;
 
 /* ------------------------------------------------------------------------ */
@@ -246,6 +247,15 @@ rc_status rc_upload_scene_prebuilt(rc_tracer* h, const double* vertices, const u
  * checks and for caching; nodes: node_count entries, ordered_index: n). */
 rc_status rc_get_bvh(const rc_tracer* h, rc_bvh_node* nodes, int64_t node_capacity, int64_t* node_count,
                      uint64_t* ordered_index, int64_t index_capacity);
+
+/* BVH builder of the next rc_upload_scene (no counterpart in the reference;
+ * GPU-only extension). RC_BUILDER_REFERENCE_SAH (default): FlatBVH::build's
+ * SAH tree on the host, identical to the reference's. RC_BUILDER_GPU_LBVH:
+ * a linear BVH built on the device (Morton order, Karras 2012), leaves of up
+ * to max_leaf_size triangles; much faster to build, not the reference's
+ * tree (closest hits equal except at equal-distance ties). */
+typedef enum rc_bvh_builder { RC_BUILDER_REFERENCE_SAH = 0, RC_BUILDER_GPU_LBVH = 1 } rc_bvh_builder;
+rc_status rc_set_bvh_builder(rc_tracer* h, int32_t builder);
 
 /* Host-only SAH build (no device memory, no GPU needed): the BVH
  * rc_upload_scene would build, returned in the reference's FlatBVHNode form

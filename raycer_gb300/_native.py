@@ -97,7 +97,7 @@ class rc_stats(C.Structure):
     _fields_ = [("rays_traced", C.c_uint64), ("node_visits", C.c_uint64), ("tri_tests", C.c_uint64),
                 ("last_ms", C.c_double), ("bvh_inner_nodes", C.c_uint64), ("bvh_depth", C.c_uint64),
                 ("device_bytes", C.c_uint64), ("stage_rays", C.c_uint64 * 2), ("stage_nodes", C.c_uint64 * 2),
-                ("stage_tris", C.c_uint64 * 2), ("stage_ms", C.c_double * 2)]
+                ("stage_tris", C.c_uint64 * 2), ("stage_ms", C.c_double * 2), ("build_ms", C.c_double)]
 
 
 class rc_batch_stats(C.Structure):
@@ -128,6 +128,8 @@ class rc_scene_file_info(C.Structure):
 
 
 RC_GENERAL_SKY = 1
+RC_BUILDER_REFERENCE_SAH = 0
+RC_BUILDER_GPU_LBVH = 1
 RC_NRC_PARAMS = 20992
 RC_NRC_QUERY_FLOATS = 12
 RC_NRC_INPUTS = 128
@@ -195,6 +197,7 @@ PROTOTYPES = {
     "rc_nrc_read_samples": (i32, [P, P, i64, C.POINTER(i64)]),
     "rc_nrc_get_stats": (i32, [P, C.POINTER(rc_nrc_stats)]),
     "rc_film_accumulate_f64": (i32, [P, P, i32]),
+    "rc_set_bvh_builder": (i32, [P, i32]),
     "rc_save_scene": (i32, [P, C.c_char_p]),
     "rc_load_scene": (i32, [P, C.c_char_p]),
     "rc_write_scene_file": (i32, [P, P, i64, P, i32, u32, C.c_char_p, C.c_char_p, i64]),

@@ -101,6 +101,7 @@ struct rc_tracer
     std::vector<rc_directional_light> lights;
     int order = RC_ORDER_NEAREST;
     int counting = 0;
+    int builder = RC_BUILDER_REFERENCE_SAH;
     uint32_t frameIndex = 0;  // advances per PATH render, reset by rc_clear
 
     // Film: r, g, b, filter-weight sum per pixel (float32), and the RAY
@@ -155,6 +156,10 @@ void release_render_buffers(rc_tracer* h);
 void build_host_scene(const double* v, const uint32_t* matIdx, int64_t n, const rc_material* mats, int32_t matCount,
                       std::vector<BuildNode>&& nodes, std::vector<uint32_t>&& order, uint32_t depth, HostScene& hs);
 rc_status upload_host_scene(rc_tracer* h, HostScene&& hs);
+void release_scene_data(rc_tracer* h);
+// Upload through the GPU BVH builder (gpu_build_host.cpp).
+rc_status upload_gpu_built(rc_tracer* h, const double* v, const uint32_t* matIdx, int64_t n, const rc_material* mats,
+                           int32_t matCount, uint32_t maxLeafSize);
 bool validate_flat_bvh(const std::vector<BuildNode>& nodes, uint64_t n, uint32_t& depth, std::string& err);
 // Grow-only device buffer (frees the old one); counts into deviceBytes.
 rc_status device_grow(rc_tracer* h, void** ptr, size_t* cap, size_t bytes, const char* what);

@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cfloat>
 #include <cmath>
 #include <cstring>
@@ -354,6 +355,8 @@ rc_status upload_host_scene(rc_tracer* h, HostScene&& hs)
     return RC_OK;
 }
 
+void release_scene_data(rc_tracer* h) { release_scene(h); }
+
 bool validate_flat_bvh(const std::vector<BuildNode>& nodes, uint64_t n, uint32_t& depth, std::string& err)
 {
     return validate_flat(nodes, n, depth, err);
@@ -572,12 +575,27 @@ rc_status rc_upload_scene(rc_tracer* h, const double* vertices, const uint32_t* 
     if (max_leaf_size < 1 || max_leaf_size > 15)
         return fail(h, RC_UNSUPPORTED, "upload: max_leaf_size must be in 1..15");
     cudaSetDevice(h->device);
+    if (h->builder == RC_BUILDER_GPU_LBVH)
+        return upload_gpu_built(h, vertices, material_index, n, materials, material_count, max_leaf_size);
+    const auto t0 = std::chrono::steady_clock::now();
     BuildResult br;
     std::string err;
     if (!buildFlatBVH(vertices, n, max_leaf_size, 0, br, err))
         return fail(h, RC_INVALID_ARG, err);
-    return upload_common(h, vertices, material_index, n, materials, material_count, std::move(br.nodes),
-                         std::move(br.order), br.depth);
+    s = upload_common(h, vertices, material_index, n, materials, material_count, std::move(br.nodes),
+                      std::move(br.order), br.depth);
+    h->stats.build_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return s;
+}
+
+rc_status rc_set_bvh_builder(rc_tracer* h, int32_t builder)
+{
+    if (!h)
+        return RC_INVALID_ARG;
+    if (builder != RC_BUILDER_REFERENCE_SAH && builder != RC_BUILDER_GPU_LBVH)
+        return fail(h, RC_INVALID_ARG, "set_bvh_builder: unknown builder");
+    h->builder = builder;
+    return RC_OK;
 }
 
 rc_status rc_upload_scene_prebuilt(rc_tracer* h, const double* vertices, const uint32_t* material_index, int64_t n,
