@@ -64,7 +64,9 @@ typedef struct rc_material
     int32_t is_emissive;  /* isEmissive                                  */
     int32_t non_shadowing;/* nonShadowing: skipped by shadow rays        */
     int32_t invert_normal;/* invertNormal                                */
-    int32_t reserved;     /* must be 0                                   */
+    int32_t dielectric;   /* GPU extension: 1 = smooth dielectric (PATH   */
+                          /* tracer: Fresnel reflection / refraction)    */
+    float ior;            /* its index of refraction (> 0); 0 otherwise  */
 } rc_material;
 
 /* Float32 camera record, the fields CLScene::readSceneCamera copies
@@ -433,6 +435,37 @@ rc_status rc_get_stats(const rc_tracer* h, rc_stats* out);
 /* The handle's CUDA stream (cudaStream_t) as an opaque pointer. */
 void* rc_stream(rc_tracer* h);
 rc_status rc_sync(rc_tracer* h);
+
+/* ------------------------------------------------------------------------ */
+/* Instanced (two-level) scenes — Instance (Instance.cpp:17-116) placing a  */
+/* PrimitiveGroup with its own BVH (PrimitiveGroup.cpp:13-62). Each mesh    */
+/* gets the reference's SAH BVH; each instance the reference's transform   */
+/* T(c + translate) * R_x(pitch) R_y(yaw) R_z(roll) * S(scale) * T(-c), c  */
+/* the mesh's box centre; a BVH over the instances' world boxes finds them. */
+/* Geometry that is not instanced is a mesh with an identity instance.     */
+/* Traced by rc_cast / rc_cast_device (hit prim = the flattened index:     */
+/* the triangles of instance 0, then of instance 1, ...) and PATH renders; */
+/* the RAY frame kernels and scene files take single-level scenes only.    */
+
+typedef struct rc_mesh
+{
+    const double* vertices;          /* triangle_count * 9 */
+    const uint32_t* material_index;  /* triangle_count */
+    int64_t triangle_count;
+} rc_mesh;
+
+typedef struct rc_instance
+{
+    int32_t mesh;         /* index into the mesh array                           */
+    int32_t material;     /* material for all its triangles (changePrimitive), or -1 */
+    double scale[3];      /* Instance::scale                                      */
+    double rotate[3];     /* Instance::rotate: pitch, yaw, roll (degrees)          */
+    double translate[3];  /* Instance::translate                                  */
+} rc_instance;
+
+rc_status rc_upload_instanced(rc_tracer* h, const rc_mesh* meshes, int32_t mesh_count, const rc_instance* instances,
+                              int64_t instance_count, const rc_material* materials, int32_t material_count,
+                              uint32_t max_leaf_size);
 
 /* ------------------------------------------------------------------------ */
 /* Binary scene + BVH cache files (replace Scene::saveToFile / loadFromFile, */

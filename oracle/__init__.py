@@ -43,6 +43,7 @@ def _setup(lib: C.CDLL, protos: dict) -> C.CDLL:
 
 
 _ORACLE_PROTOS = {
+    "or_scene_set_ior": (None, [P, P, i32]),
     "or32_filter_weight": (None, [C.c_int, i64, P, P, P]),
     "or64_filter_weight": (None, [C.c_int, i64, P, P, P]),
     "or32_filter_exp": (None, [i64, P, P]),
@@ -99,6 +100,7 @@ _REF_PROTOS = {
     "ref_value_noise": (None, [u32, i64, P, u64, f64, f64, P]),
     "ref_cmj_pattern": (None, [u64, u64, u32, P, P]),
     "ref_filter_weight": (None, [C.c_int, i64, P, P, P]),
+    "ref_scene_add_instanced_mesh": (None, [P, i64, P, P, u64, u64, i64, P, u64]),
 }
 
 _oracle = None
@@ -137,7 +139,7 @@ def _mat_arrays(materials):
     diffuse = np.array([mm.diffuse for mm in materials], np.float32).reshape(m, 3)
     emit = np.array([mm.emittance for mm in materials], np.float32).reshape(m, 3)
     flags = np.array([(1 if mm.is_emissive else 0) | (2 if mm.non_shadowing else 0) | (4 if mm.invert_normal else 0)
-                      for mm in materials], np.int32)
+                      | (8 if getattr(mm, "dielectric", False) else 0) for mm in materials], np.int32)
     return diffuse, emit, flags
 
 
@@ -153,6 +155,8 @@ class Oracle:
         self._keep = (v, m, d, e, f)
         self.h = self.lib.or_scene_new(_ptr(v), _ptr(m), v.shape[0], _ptr(d), _ptr(e), _ptr(f), len(scene.materials),
                                        int(scene.max_leaf_size), 1 if (build and prebuilt is None) else 0)
+        ior = np.array([float(getattr(mm, "ior", 0.0)) for mm in scene.materials], np.float32)
+        self.lib.or_scene_set_ior(self.h, _ptr(ior), len(scene.materials))
         if prebuilt is not None:
             self.set_bvh(*prebuilt)
 
@@ -302,9 +306,12 @@ class RefScene:
             e = np.array(m.emittance, np.float64)
             self.lib.ref_scene_add_material(self.h, i + 1, _ptr(d), _ptr(e), int(m.is_emissive),
                                             int(m.non_shadowing))
-        v = np.ascontiguousarray(scene.vertices, np.float64)
-        mids = np.ascontiguousarray(scene.material_index.astype(np.uint64) + 1)
-        self.lib.ref_scene_add_triangles(self.h, v.shape[0], _ptr(v), _ptr(mids), 1)
+        if hasattr(scene, "meshes"):
+            self._add_instanced(scene)
+        else:
+            v = np.ascontiguousarray(scene.vertices, np.float64)
+            mids = np.ascontiguousarray(scene.material_index.astype(np.uint64) + 1)
+            self.lib.ref_scene_add_triangles(self.h, v.shape[0], _ptr(v), _ptr(mids), 1)
         c = scene.camera
         pos = np.array(c.position, np.float64)
         self.lib.ref_scene_set_camera(self.h, _ptr(pos), c.pitch, c.yaw, c.roll, c.fov)
@@ -314,6 +321,21 @@ class RefScene:
             self.lib.ref_scene_add_directional_light(self.h, _ptr(d), _ptr(col), 1.0)
         if init:
             self.initialize()
+
+    # Instanced scenes: mesh m's triangle j has id MESH_ID * m + 1 + j.
+    MESH_ID = 10_000_000
+
+    def _add_instanced(self, scene):
+        for m, (v, mi) in enumerate(scene.meshes):
+            ks = [k for k, d in enumerate(scene.instances) if d.mesh == m]
+            if not ks:
+                continue
+            srt = np.array([[*scene.instances[k].scale, *scene.instances[k].rotate, *scene.instances[k].translate]
+                            for k in ks], np.float64)
+            v = np.ascontiguousarray(v, np.float64)
+            mids = np.ascontiguousarray(np.asarray(mi).astype(np.uint64) + 1)
+            self.lib.ref_scene_add_instanced_mesh(self.h, v.shape[0], _ptr(v), _ptr(mids), self.MESH_ID * m + 1,
+                                                  900_000_000 + m, len(ks), _ptr(srt), 950_000_000 + 10_000 * m)
 
     def initialize(self):
         if self.lib.ref_scene_initialize(self.h, int(self.scene.max_leaf_size)) != 0:

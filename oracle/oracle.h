@@ -34,7 +34,8 @@ struct Material
 {
     float diffuse[3];
     float emittance[3];
-    int32_t flags;  // bit0 emissive, bit1 nonShadowing, bit2 invertNormal
+    int32_t flags;  // bit0 emissive, bit1 nonShadowing, bit2 invertNormal, bit3 dielectric
+    float ior = 0.0f;
 };
 
 struct Scene64

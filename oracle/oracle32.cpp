@@ -332,6 +332,35 @@ void sincos_turn(float x, float& s, float& c)
     }
 }
 
+// The device's dielectric_bounce (pathtrace.cu): Schlick Fresnel choice,
+// mirror reflection or refraction, same operations.
+static V3f dielectric32(V3f d, V3f n, float ior, float xi)
+{
+    const float c = dot3(d, n);
+    const bool outside = c < 0.0f;
+    const float n1 = outside ? 1.0f : ior;
+    const float n2 = outside ? ior : 1.0f;
+    const V3f N = outside ? n : V3f{ -n.x, -n.y, -n.z };
+    const float ci = std::fabs(c);
+    float r0 = (n2 - n1) / (n2 + n1);
+    r0 = r0 * r0;
+    const float m = 1.0f - ci;
+    const float m2 = m * m;
+    const float m5 = (m2 * m2) * m;
+    const float R = r0 + (1.0f - r0) * m5;
+    const float eta = n1 / n2;
+    const float k = 1.0f - (eta * eta) * (1.0f - ci * ci);
+    if (k <= 0.0f || xi < R)
+    {
+        const float s2 = 2.0f * ci;
+        return V3f{ std::fmaf(N.x, s2, d.x), std::fmaf(N.y, s2, d.y), std::fmaf(N.z, s2, d.z) };
+    }
+    const float a = eta * ci - std::sqrt(k);
+    V3f r{ std::fmaf(N.x, a, d.x * eta), std::fmaf(N.y, a, d.y * eta), std::fmaf(N.z, a, d.z * eta) };
+    const float len = std::sqrt(dot3(r, r));
+    return V3f{ r.x / len, r.y / len, r.z / len };
+}
+
 V3f hemisphere32(V3f U, V3f V, V3f W, float x, float y)
 {
     float sp, cp;
@@ -682,12 +711,16 @@ void render_path32(const Scene32& s, const Camera32& cam, const PathSettings32& 
                         nrm = V3f{ -nrm.x, -nrm.y, -nrm.z };
                     float xr = stream_float(key, 2u * uint32_t(seg));
                     float yr = stream_float(key, 2u * uint32_t(seg) + 1u);
-                    V3f dir = hemisphere32(V3f{ sh[3], sh[4], sh[5] }, V3f{ sh[6], sh[7], sh[8] }, nrm, xr, yr);
+                    const bool dielectric = (m.flags & 8) != 0;
+                    V3f dir = dielectric ? dielectric32(d, nrm, m.ior, xr)
+                                         : hemisphere32(V3f{ sh[3], sh[4], sh[5] }, V3f{ sh[6], sh[7], sh[8] }, nrm, xr, yr);
                     V3f ip{ std::fmaf(d.x, h.t, o.x), std::fmaf(d.y, h.t, o.y), std::fmaf(d.z, h.t, o.z) };
                     o = V3f{ std::fmaf(dir.x, ps.rayStartOffset, ip.x), std::fmaf(dir.y, ps.rayStartOffset, ip.y),
                              std::fmaf(dir.z, ps.rayStartOffset, ip.z) };
                     d = dir;
                     from = h.slot;
+                    if (dielectric)
+                        continue;
                     float alpha = std::fabs(dot3(dir, nrm));
                     thr[0] = thr[0] * ((2.0f * m.diffuse[0]) * alpha);
                     thr[1] = thr[1] * ((2.0f * m.diffuse[1]) * alpha);

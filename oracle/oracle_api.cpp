@@ -64,6 +64,13 @@ extern "C" {
 // flags) x m. prebuiltNodes/order: optional reference-form BVH (10 doubles
 // per node: min xyz, max xyz, rightOffset, start, count as doubles... see
 // or_scene_set_bvh); when absent the BVH is built (FlatBVH::build).
+void or_scene_set_ior(void* hp, const float* ior, int32_t m)
+{
+    auto* h = static_cast<Handle*>(hp);
+    for (int32_t i = 0; i < m && size_t(i) < h->s64.mats.size(); ++i)
+        h->s64.mats[size_t(i)].ior = ior[i];
+}
+
 void* or_scene_new(const double* v, const uint32_t* mat, int64_t n, const float* diffuse, const float* emittance,
                    const int32_t* flags, int32_t m, uint32_t maxLeafSize, int build)
 {

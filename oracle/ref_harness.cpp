@@ -34,6 +34,8 @@
 #include "Raytracing/Intersection.h"
 #include "Raytracing/Primitives/FlatBVH.h"
 #include "Raytracing/Primitives/Triangle.h"
+#include "Raytracing/Primitives/PrimitiveGroup.h"
+#include "Raytracing/Primitives/Instance.h"
 #include "Raytracing/Tracers/Tracer.h"
 #include "Raytracing/Tracers/TracerState.h"
 #include "Rendering/Film.h"
@@ -192,6 +194,50 @@ void ref_scene_add_triangles(void* h, int64_t n, const double* v, const uint64_t
             t.normals[k] = Vector3(0.0, 0.0, 0.0);
         }
         scene.primitives.triangles.push_back(t);
+    }
+}
+
+// A mesh placed by instances: its triangles (ids firstTriId + i) are
+// invisible and grouped in a PrimitiveGroup with its own BVH (id groupId);
+// each instance k (id firstInstanceId + k) references the group with
+// srt[k] = scale xyz, rotate pitch/yaw/roll (degrees), translate xyz. With
+// changePrimitive off, hits report the mesh triangle (Instance.cpp:93).
+void ref_scene_add_instanced_mesh(void* h, int64_t n, const double* v, const uint64_t* materialIds,
+                                  uint64_t firstTriId, uint64_t groupId, int64_t instances, const double* srt,
+                                  uint64_t firstInstanceId)
+{
+    Scene& scene = S(h)->scene;
+    PrimitiveGroup group;
+    group.id = groupId;
+    group.invisible = true;
+    group.enableBVH = true;
+    for (int64_t i = 0; i < n; ++i)
+    {
+        Triangle t;
+        t.id = firstTriId + uint64_t(i);
+        t.materialId = materialIds[i];
+        t.invisible = true;
+        for (int k = 0; k < 3; ++k)
+        {
+            t.vertices[k] = Vector3(v[i * 9 + k * 3 + 0], v[i * 9 + k * 3 + 1], v[i * 9 + k * 3 + 2]);
+            t.normals[k] = Vector3(0.0, 0.0, 0.0);
+        }
+        scene.primitives.triangles.push_back(t);
+        group.primitiveIds.push_back(t.id);
+    }
+    scene.primitives.primitiveGroups.push_back(group);
+    for (int64_t k = 0; k < instances; ++k)
+    {
+        const double* p = srt + k * 9;
+        Instance in;
+        in.id = firstInstanceId + uint64_t(k);
+        in.primitiveId = groupId;
+        in.materialId = materialIds[0];
+        in.scale = Vector3(p[0], p[1], p[2]);
+        in.rotate = EulerAngle(p[3], p[4], p[5]);
+        in.translate = Vector3(p[6], p[7], p[8]);
+        in.changePrimitive = false;
+        scene.primitives.instances.push_back(in);
     }
 }
 

@@ -49,7 +49,8 @@ RC_ORDER_NEAREST = 1
 
 class rc_material(C.Structure):
     _fields_ = [("diffuse", C.c_float * 3), ("emittance", C.c_float * 3), ("is_emissive", C.c_int32),
-                ("non_shadowing", C.c_int32), ("invert_normal", C.c_int32), ("reserved", C.c_int32)]
+                ("non_shadowing", C.c_int32), ("invert_normal", C.c_int32), ("dielectric", C.c_int32),
+                ("ior", C.c_float)]
 
 
 class rc_camera(C.Structure):
@@ -120,6 +121,15 @@ class rc_nrc_config(C.Structure):
 class rc_nrc_stats(C.Structure):
     _fields_ = [("lookups", C.c_uint64), ("training_samples", C.c_uint64), ("steps", C.c_uint64),
                 ("last_loss", C.c_float), ("reserved", C.c_float), ("train_ms", C.c_double)]
+
+
+class rc_mesh(C.Structure):
+    _fields_ = [("vertices", C.c_void_p), ("material_index", C.c_void_p), ("triangle_count", C.c_int64)]
+
+
+class rc_instance(C.Structure):
+    _fields_ = [("mesh", C.c_int32), ("material", C.c_int32), ("scale", C.c_double * 3), ("rotate", C.c_double * 3),
+                ("translate", C.c_double * 3)]
 
 
 class rc_scene_file_info(C.Structure):
@@ -198,6 +208,7 @@ PROTOTYPES = {
     "rc_nrc_get_stats": (i32, [P, C.POINTER(rc_nrc_stats)]),
     "rc_film_accumulate_f64": (i32, [P, P, i32]),
     "rc_set_bvh_builder": (i32, [P, i32]),
+    "rc_upload_instanced": (i32, [P, C.POINTER(rc_mesh), i32, C.POINTER(rc_instance), i64, P, i32, u32]),
     "rc_save_scene": (i32, [P, C.c_char_p]),
     "rc_load_scene": (i32, [P, C.c_char_p]),
     "rc_write_scene_file": (i32, [P, P, i64, P, i32, u32, C.c_char_p, C.c_char_p, i64]),

@@ -64,11 +64,29 @@ constexpr uint32_t kMetaNonShadowing = 0x80000000u;
 constexpr uint32_t kMatEmissive = 1u;
 constexpr uint32_t kMatNonShadowing = 2u;
 constexpr uint32_t kMatInvertNormal = 4u;
+constexpr uint32_t kMatDielectric = 8u;  // DevMat.diffuse.w = index of refraction
 
 constexpr int kLeafCountBits = 4;
 constexpr int kMaxStack = 64;
 
-// Device scene handed to every kernel by value.
+// One placed copy of a mesh (two-level scenes): world -> object rows
+// (object = A world + b; r_i = (A_i0, A_i1, A_i2, b_i)), the mesh's BVH
+// root link (into the pooled node / triangle arrays), a material that
+// replaces the triangles' own (or -1), and the first flattened primitive
+// index of this instance (prim = primBase + the triangle's mesh-local index).
+struct __align__(16) DevInstance
+{
+    float4 r0, r1, r2;
+    int rootLink;
+    int material;
+    int primBase;
+    int identity;  // 1: A = I, b = 0 (no transform needed)
+};
+
+// Device scene handed to every kernel by value. Two-level scenes
+// (numInstances > 0) keep every mesh's BVH in `nodes` / `tris` / `shade`
+// (links already offset into the pools) and a top-level BVH over the
+// instances in `tlas` (leaf links index `instances`).
 struct DevScene
 {
     const DevNode* nodes;
@@ -79,6 +97,10 @@ struct DevScene
     int numTris;
     int numMats;
     int pad;
+    const DevNode* tlas;
+    const DevInstance* instances;
+    int tlasRoot;
+    int numInstances;  // 0: single-level scene
 };
 
 // Float32 camera record used by the kernels (same fields as rc_camera).

@@ -92,6 +92,12 @@ struct rc_tracer
     bool sceneReady = false;
     std::vector<rcx::BuildNode> hostNodes;
     std::vector<uint32_t> hostOrder;
+    // Two-level scenes (rc_upload_instanced): top-level BVH over instances.
+    rcx::DevNode* dTlas = nullptr;
+    size_t tlasCount = 0;
+    rcx::DevInstance* dInstances = nullptr;
+    int64_t nInstances = 0;
+    int32_t tlasRoot = 0;
 
     // Per-frame records.
     rc_camera camera{};
@@ -157,6 +163,7 @@ void build_host_scene(const double* v, const uint32_t* matIdx, int64_t n, const 
                       std::vector<BuildNode>&& nodes, std::vector<uint32_t>&& order, uint32_t depth, HostScene& hs);
 rc_status upload_host_scene(rc_tracer* h, HostScene&& hs);
 void release_scene_data(rc_tracer* h);
+void device_nodes(const std::vector<BuildNode>& nodes, std::vector<DevNode>& dn, int32_t& rootLink, uint64_t& inner);
 // Upload through the GPU BVH builder (gpu_build_host.cpp).
 rc_status upload_gpu_built(rc_tracer* h, const double* v, const uint32_t* matIdx, int64_t n, const rc_material* mats,
                            int32_t matCount, uint32_t maxLeafSize);

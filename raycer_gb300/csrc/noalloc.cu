@@ -71,6 +71,9 @@ extern "C" rc_status rc_cast_with_shadow_device_noalloc(rc_tracer* h, const rc_r
         return RC_INVALID_ARG;
     if (!h->sceneReady)
         return fail(h, RC_NOT_READY, "cast_with_shadow_device_noalloc: no scene uploaded");
+    if (h->nInstances > 0)
+        return fail(h, RC_UNSUPPORTED, "cast_with_shadow_device_noalloc: instanced scenes are traced by rc_cast "
+                                       "and PATH renders only");
     if (n <= 0 || !d_rays || !d_out)
         return fail(h, RC_INVALID_ARG, "cast_with_shadow_device_noalloc: bad ray count or null buffer");
     if (n > kNoAllocMaxRays)
@@ -97,7 +100,7 @@ extern "C" rc_status rc_cast_with_shadow_device_noalloc(rc_tracer* h, const rc_r
     if (castShadow)
         L = make_float3(-h->lights[0].direction[0], -h->lights[0].direction[1], -h->lights[0].direction[2]);
 
-    rcx::DevScene sc;
+    rcx::DevScene sc{};
     sc.nodes = h->dNodes;
     sc.tris = h->dTris;
     sc.shade = h->dShade;

@@ -162,7 +162,7 @@ __global__ void __launch_bounds__(256) k_generate(PassParams p)
     }
     V3 d = camera_dir(sc.cam, px, py);
     p.o[s] = make_float4(sc.cam.pos[0], sc.cam.pos[1], sc.cam.pos[2], __int_as_float(-1));
-    p.d[s] = make_float4(d.x, d.y, d.z, 0.0f);
+    p.d[s] = make_float4(d.x, d.y, d.z, __int_as_float(-1));  // w: instance the ray leaves from
     p.thr[s] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
     p.res[s] = make_float4(0.0f, 0.0f, 0.0f, w);
     p.qa[s] = int(s);
@@ -194,9 +194,12 @@ __global__ void __launch_bounds__(BLOCK, (RC_TRACE_MIN_BLOCKS * 128) / BLOCK) k_
             float4 o = p.o[s];
             float4 d = p.d[s];
             RayF ray = make_ray(v3(o.x, o.y, o.z), v3(d.x, d.y, d.z), 0.0f, FLT_MAX);
-            HitF h{ -1, FLT_MAX, 0.0f, 0.0f };
-            bool found = traverse<false, ORDER, COUNT>(sc, ray, h, cnt, err, __float_as_int(o.w));
-            p.hit[s] = make_int4(found ? h.slot : -1, __float_as_int(h.t), __float_as_int(h.u), __float_as_int(h.v));
+            HitF h{ -1, FLT_MAX, 0.0f, 0.0f, -1 };
+            bool found = traverse_scene<false, ORDER, COUNT>(sc, ray, h, cnt, err, __float_as_int(o.w),
+                                                             __float_as_int(d.w));
+            // w: v, or the instance of a two-level scene's hit (shading uses neither u nor v)
+            p.hit[s] = make_int4(found ? h.slot : -1, __float_as_int(h.t), __float_as_int(h.u),
+                                 sc.numInstances > 0 ? h.inst : __float_as_int(h.v));
             done++;
         }
     }
@@ -218,6 +221,70 @@ __global__ void __launch_bounds__(BLOCK, (RC_TRACE_MIN_BLOCKS * 128) / BLOCK) k_
     }
     if (err)
         atomicOr(&p.ctl->error, 1);
+}
+
+// Shading frame of a hit: the triangle's normal, tangent and bitangent
+// (Triangle::initialize), the normal inverted for invertNormal materials;
+// in an instance, each transformed by A^T (the inverse transpose of the
+// instance transform) and normalised, as Instance transforms its ONB
+// (Instance.cpp:98-99, ONB.cpp:21-30).
+struct ShadeFrame
+{
+    V3 n, t, b;
+};
+
+__device__ __forceinline__ V3 inst_normal(const DevInstance& in, V3 v)
+{
+    V3 w = v3(__fmaf_rn(in.r0.x, v.x, __fmaf_rn(in.r1.x, v.y, __fmul_rn(in.r2.x, v.z))),
+              __fmaf_rn(in.r0.y, v.x, __fmaf_rn(in.r1.y, v.y, __fmul_rn(in.r2.y, v.z))),
+              __fmaf_rn(in.r0.z, v.x, __fmaf_rn(in.r1.z, v.y, __fmul_rn(in.r2.z, v.z))));
+    const float len = __fsqrt_rn(vdot(w, w));
+    return v3(__fdiv_rn(w.x, len), __fdiv_rn(w.y, len), __fdiv_rn(w.z, len));
+}
+
+__device__ __forceinline__ ShadeFrame shade_frame(const DevScene& sc, int slot, const DevInstance* in, uint32_t mflags)
+{
+    const float4* sp = reinterpret_cast<const float4*>(sc.shade + slot);
+    const float4 sn = __ldg(sp + 0), st = __ldg(sp + 1), sb = __ldg(sp + 2);
+    ShadeFrame f{ v3(sn.x, sn.y, sn.z), v3(st.x, st.y, st.z), v3(sb.x, sb.y, sb.z) };
+    if (in && !in->identity)
+    {
+        f.n = inst_normal(*in, f.n);
+        f.t = inst_normal(*in, f.t);
+        f.b = inst_normal(*in, f.b);
+    }
+    if (mflags & kMatInvertNormal)
+        f.n = v3(-f.n.x, -f.n.y, -f.n.z);
+    return f;
+}
+
+// Specular bounce off a dielectric (GPU extension: the reference's path
+// tracer is diffuse only). Fresnel reflectance by Schlick's approximation
+// as the reference's Whitted tracer computes it (Raytracer.cpp:126-143);
+// reflect with that probability (or on total internal reflection), else
+// refract (Raytracer.cpp:230-246 with the normal facing the ray). The
+// throughput is unchanged: the choice probability equals its weight.
+__device__ __forceinline__ V3 dielectric_bounce(V3 d, V3 n, float ior, float xi)
+{
+    const float c = vdot(d, n);
+    const bool outside = c < 0.0f;
+    const float n1 = outside ? 1.0f : ior;
+    const float n2 = outside ? ior : 1.0f;
+    const V3 N = outside ? n : v3(-n.x, -n.y, -n.z);
+    const float ci = fabsf(c);
+    float r0 = __fdiv_rn(__fsub_rn(n2, n1), __fadd_rn(n2, n1));
+    r0 = __fmul_rn(r0, r0);
+    const float m = __fsub_rn(1.0f, ci);
+    const float m2 = __fmul_rn(m, m);
+    const float m5 = __fmul_rn(__fmul_rn(m2, m2), m);
+    const float R = __fadd_rn(r0, __fmul_rn(__fsub_rn(1.0f, r0), m5));
+    const float eta = __fdiv_rn(n1, n2);
+    const float k = __fsub_rn(1.0f, __fmul_rn(__fmul_rn(eta, eta), __fsub_rn(1.0f, __fmul_rn(ci, ci))));
+    if (k <= 0.0f || xi < R)
+        return vfma(N, __fmul_rn(2.0f, ci), d);  // d - 2 (d.N) N, d.N = -ci
+    const V3 r = vfma(N, __fsub_rn(__fmul_rn(eta, ci), __fsqrt_rn(k)), vscale(d, eta));
+    const float len = __fsqrt_rn(vdot(r, r));
+    return v3(__fdiv_rn(r.x, len), __fdiv_rn(r.y, len), __fdiv_rn(r.z, len));
 }
 
 // Training-path choice of slot s: one random slot per run of trainStride.
@@ -302,9 +369,18 @@ __global__ void __launch_bounds__(BLOCK) k_shade(PassParams p, int segment)
                 const float4* tp = reinterpret_cast<const float4*>(sc.tris + h.x);
                 float4 tc = __ldg(tp + 2);
                 uint32_t mi = __float_as_uint(tc.y) & kMetaMaterialMask;
+                const int inst = sc.numInstances > 0 ? h.w : -1;
+                DevInstance in{};
+                if (inst >= 0)
+                {
+                    in = load_instance(sc.instances, inst);
+                    if (in.material >= 0)
+                        mi = uint32_t(in.material);  // Instance::changePrimitive (Instance.cpp:93)
+                }
                 float4 md = __ldg(&sc.mats[mi].diffuse);
                 float4 me = __ldg(&sc.mats[mi].emittance);
                 uint32_t mflags = __float_as_uint(me.w);
+                const bool dielectric = (mflags & kMatDielectric) != 0;
                 float4 thr = p.thr[s];
                 if (mflags & kMatEmissive)
                 {
@@ -317,17 +393,13 @@ __global__ void __launch_bounds__(BLOCK) k_shade(PassParams p, int segment)
                     if (train)
                         nrc_end(p.nrc, g, me.x, me.y, me.z, uint32_t(segment));
                 }
-                else if (NRC && !train && segment == p.nrc.termSegment)
+                else if (NRC && !train && !dielectric && segment >= p.nrc.termSegment)
                 {
-                    const float4* sp = reinterpret_cast<const float4*>(sc.shade + h.x);
-                    float4 sn = __ldg(sp + 0);
-                    V3 nrm = v3(sn.x, sn.y, sn.z);
-                    if (mflags & kMatInvertNormal)
-                        nrm = v3(-nrm.x, -nrm.y, -nrm.z);
+                    const ShadeFrame fr = shade_frame(sc, h.x, inst >= 0 ? &in : nullptr, mflags);
                     float4 o = p.o[s];
                     float4 d = p.d[s];
                     V3 ip = vfma(v3(d.x, d.y, d.z), __int_as_float(h.y), v3(o.x, o.y, o.z));
-                    lrec = nrc_record(ip, d, nrm, md, 0.0f, 0.0f, 0.0f, __int_as_float(s));
+                    lrec = nrc_record(ip, d, fr.n, md, 0.0f, 0.0f, 0.0f, __int_as_float(s));
                     lookup = true;
                 }
                 else if (segment + 1 < scn.maxPathLength)
@@ -350,59 +422,69 @@ __global__ void __launch_bounds__(BLOCK) k_shade(PassParams p, int segment)
                             thr.z = __fdiv_rn(thr.z, qs);
                         }
                     }
-                    const float4* sp = reinterpret_cast<const float4*>(sc.shade + h.x);
-                    float4 sn = __ldg(sp + 0);
-                    V3 nrm = v3(sn.x, sn.y, sn.z);
-                    if (mflags & kMatInvertNormal)
-                        nrm = v3(-nrm.x, -nrm.y, -nrm.z);
+                    const ShadeFrame frm = shade_frame(sc, h.x, inst >= 0 ? &in : nullptr, mflags);
+                    const V3 nrm = frm.n;
                     float4 o = p.o[s];
                     float4 d = p.d[s];
                     float t = __int_as_float(h.y);
                     V3 ip = vfma(v3(d.x, d.y, d.z), t, v3(o.x, o.y, o.z));
                     if (alive)
                     {
-                        float4 st = __ldg(sp + 1);
-                        float4 sb = __ldg(sp + 2);
                         float xr = stream_float(key, kCounterBounce + 2u * uint32_t(segment));
                         float yr = stream_float(key, kCounterBounce + 2u * uint32_t(segment) + 1u);
-                        V3 dir = hemisphere_cosine(v3(st.x, st.y, st.z), v3(sb.x, sb.y, sb.z), nrm, xr, yr);
+                        V3 dir;
+                        float fr, fg, fb;
+                        if (dielectric)
+                        {
+                            dir = dielectric_bounce(v3(d.x, d.y, d.z), nrm, md.w, xr);
+                            fr = fg = fb = 1.0f;
+                        }
+                        else
+                        {
+                            dir = hemisphere_cosine(frm.t, frm.b, nrm, xr, yr);
+                            float alpha = fabsf(vdot(dir, nrm));
+                            // brdf = 2 * reflectance * alpha (PathTracer.cpp:70-71)
+                            fr = __fmul_rn(__fmul_rn(2.0f, md.x), alpha);
+                            fg = __fmul_rn(__fmul_rn(2.0f, md.y), alpha);
+                            fb = __fmul_rn(__fmul_rn(2.0f, md.z), alpha);
+                            thr.x = __fmul_rn(thr.x, fr);
+                            thr.y = __fmul_rn(thr.y, fg);
+                            thr.z = __fmul_rn(thr.z, fb);
+                        }
                         V3 no = vfma(dir, scn.rayStartOffset, ip);
-                        float alpha = fabsf(vdot(dir, nrm));
-                        // brdf = 2 * reflectance * alpha (PathTracer.cpp:70-71)
-                        float fr = __fmul_rn(__fmul_rn(2.0f, md.x), alpha);
-                        float fg = __fmul_rn(__fmul_rn(2.0f, md.y), alpha);
-                        float fb = __fmul_rn(__fmul_rn(2.0f, md.z), alpha);
-                        thr.x = __fmul_rn(thr.x, fr);
-                        thr.y = __fmul_rn(thr.y, fg);
-                        thr.z = __fmul_rn(thr.z, fb);
                         p.o[s] = make_float4(no.x, no.y, no.z, __int_as_float(h.x));
-                        p.d[s] = make_float4(dir.x, dir.y, dir.z, 0.0f);
+                        p.d[s] = make_float4(dir.x, dir.y, dir.z, __int_as_float(inst));
                         p.thr[s] = thr;
                         cont = true;
                         if (train)
-                            p.nrc.vtx[size_t(segment) * size_t(p.nrc.groups) + g] =
-                                nrc_record(ip, d, nrm, md, fr / qs, fg / qs, fb / qs, 0.0f);
+                        {
+                            // specular vertices pass radiance on but are not training samples
+                            NrcRecord rec = nrc_record(ip, d, nrm, md, fr / qs, fg / qs, fb / qs, 0.0f);
+                            if (dielectric)
+                                rec.c.y = -1.0f;
+                            p.nrc.vtx[size_t(segment) * size_t(p.nrc.groups) + g] = rec;
+                        }
                     }
                     else if (train)
                     {
-                        p.nrc.vtx[size_t(segment) * size_t(p.nrc.groups) + g] =
-                            nrc_record(ip, d, nrm, md, 0.0f, 0.0f, 0.0f, 0.0f);
+                        NrcRecord rec = nrc_record(ip, d, nrm, md, 0.0f, 0.0f, 0.0f, 0.0f);
+                        if (dielectric)
+                            rec.c.y = -1.0f;
+                        p.nrc.vtx[size_t(segment) * size_t(p.nrc.groups) + g] = rec;
                         nrc_end(p.nrc, g, 0.0f, 0.0f, 0.0f, uint32_t(segment + 1));
                     }
                 }
                 else if (train)
                 {
                     // The depth limit cuts the path: its radiance from here on is 0.
-                    const float4* sp = reinterpret_cast<const float4*>(sc.shade + h.x);
-                    float4 sn = __ldg(sp + 0);
-                    V3 nrm = v3(sn.x, sn.y, sn.z);
-                    if (mflags & kMatInvertNormal)
-                        nrm = v3(-nrm.x, -nrm.y, -nrm.z);
+                    const ShadeFrame fr = shade_frame(sc, h.x, inst >= 0 ? &in : nullptr, mflags);
                     float4 o = p.o[s];
                     float4 d = p.d[s];
                     V3 ip = vfma(v3(d.x, d.y, d.z), __int_as_float(h.y), v3(o.x, o.y, o.z));
-                    p.nrc.vtx[size_t(segment) * size_t(p.nrc.groups) + g] =
-                        nrc_record(ip, d, nrm, md, 0.0f, 0.0f, 0.0f, 0.0f);
+                    NrcRecord rec = nrc_record(ip, d, fr.n, md, 0.0f, 0.0f, 0.0f, 0.0f);
+                    if (dielectric)
+                        rec.c.y = -1.0f;
+                    p.nrc.vtx[size_t(segment) * size_t(p.nrc.groups) + g] = rec;
                     nrc_end(p.nrc, g, 0.0f, 0.0f, 0.0f, uint32_t(segment + 1) | kNrcTermTruncated);
                 }
             }
@@ -538,9 +620,8 @@ __global__ void __launch_bounds__(256) k_nrc_targets(PassParams p)
     const bool truncated = (flags & kNrcTermTruncated) != 0;
     // a suffix cut by the depth limit counts only with minSuffix vertices
     const int last = truncated ? V - p.nrc.minSuffix : V - 1;
-    const int count = last >= 0 ? last + 1 : 0;
-    unsigned base = count > 0 ? atomicAdd(&p.nrc.counters[1], unsigned(count)) : 0u;
     float r = t.x, gg = t.y, b = t.z;
+    int count = 0;
     for (int i = V - 1; i >= 0; --i)
     {
         const size_t idx = size_t(i) * size_t(p.nrc.groups) + g;
@@ -550,8 +631,18 @@ __global__ void __launch_bounds__(256) k_nrc_targets(PassParams p)
         b = __fmul_rn(d.z, b);
         // tag: vertex index << 24 | training path (group) index
         p.nrc.vtx[idx].d = make_float4(r, gg, b, __uint_as_float((uint32_t(i) << 24) | g));
-        if (i <= last)
-            p.nrc.index[base + unsigned(last - i)] = int(idx);
+        // specular (dielectric) vertices carry albedo -1: not samples
+        if (i <= last && !(p.nrc.vtx[idx].c.y < 0.0f))
+            count++;
+    }
+    if (count == 0)
+        return;
+    unsigned k = atomicAdd(&p.nrc.counters[1], unsigned(count));
+    for (int i = last; i >= 0; --i)
+    {
+        const size_t idx = size_t(i) * size_t(p.nrc.groups) + g;
+        if (!(p.nrc.vtx[idx].c.y < 0.0f))
+            p.nrc.index[k++] = int(idx);
     }
 }
 

@@ -139,10 +139,10 @@ cudaError_t launch_tonemap(const float4* film, uint64_t pixels, int type, int ap
                            double gamma, double key, void* partials, float4* out, cudaStream_t stream, int numSMs);
 cudaError_t launch_linear(const float4* film, uint64_t pixels, float4* out, cudaStream_t stream);
 // acc += film (float64); clear != 0 zeroes the film afterwards.
-cudaError_t launch_film_accumulate_f64(float4* film, uint64_t pixels, double4* acc, int clear, cudaStream_t stream);
+cudaError_t launch_film_accumulate_f64(float4* film, uint64_t pixels, double4_32a* acc, int clear, cudaStream_t stream);
 // Display-space RMSE of film vs truth (float64), result in device memory.
 size_t rmse_scratch_bytes();
-cudaError_t launch_rmse_f64(const float4* film, const double4* truth, uint64_t pixels, int applyGamma, int shouldClamp,
+cudaError_t launch_rmse_f64(const float4* film, const double4_32a* truth, uint64_t pixels, int applyGamma, int shouldClamp,
                             double gamma, double key, void* scratch, double* result, cudaStream_t stream, int numSMs);
 
 }  // namespace rcx

@@ -153,6 +153,10 @@ PathScene path_scene(const rc_tracer* h, uint64_t pixelStart)
     ps.sc.rootLink = h->rootLink;
     ps.sc.numTris = int(h->nTris);
     ps.sc.numMats = int(h->nMats);
+    ps.sc.tlas = h->dTlas;
+    ps.sc.instances = h->dInstances;
+    ps.sc.tlasRoot = h->tlasRoot;
+    ps.sc.numInstances = int(h->nInstances);
     for (int k = 0; k < 3; ++k)
     {
         ps.cam.pos[k] = h->camera.position[k];
@@ -430,7 +434,7 @@ rc_status rc_film_accumulate_f64(rc_tracer* h, double* d_acc, int32_t clear_film
         return fail(h, RC_INVALID_ARG, "film_accumulate_f64: accumulator must be 32-byte aligned");
     cudaSetDevice(h->device);
     RC_CUDA_TRY(h,
-                launch_film_accumulate_f64(h->dFilm, h->filmPixels, reinterpret_cast<double4*>(d_acc), clear_film,
+                launch_film_accumulate_f64(h->dFilm, h->filmPixels, reinterpret_cast<double4_32a*>(d_acc), clear_film,
                                            h->stream),
                 "launch float64 accumulation");
     RC_CUDA_TRY(h, cudaStreamSynchronize(h->stream), "film_accumulate_f64");
@@ -453,7 +457,7 @@ rc_status rc_film_rmse_f64(rc_tracer* h, const double* d_truth, double* rmse)
     double* dResult = reinterpret_cast<double*>(static_cast<char*>(h->dRmse) + rmse_scratch_bytes());
     const rc_tonemapper& t = h->tonemapper;
     RC_CUDA_TRY(h,
-                launch_rmse_f64(h->dFilm, reinterpret_cast<const double4*>(d_truth), h->filmPixels, t.apply_gamma,
+                launch_rmse_f64(h->dFilm, reinterpret_cast<const double4_32a*>(d_truth), h->filmPixels, t.apply_gamma,
                                 t.should_clamp, t.gamma, t.key, h->dRmse, dResult, h->stream, h->numSMs),
                 "launch rmse");
     RC_CUDA_TRY(h, cudaMemcpyAsync(rmse, dResult, sizeof(double), cudaMemcpyDeviceToHost, h->stream), "read rmse");

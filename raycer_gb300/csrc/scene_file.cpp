@@ -349,6 +349,13 @@ rc_status rc_write_scene_file(const double* vertices, const uint32_t* material_i
             copy_error("write_scene_file: material index out of range", error, error_capacity);
             return RC_INVALID_ARG;
         }
+    for (int32_t i = 0; i < material_count; ++i)
+        if ((materials[i].dielectric != 0 && materials[i].dielectric != 1) ||
+            (materials[i].dielectric && !(materials[i].ior > 0.0f && std::isfinite(materials[i].ior))))
+        {
+            copy_error("write_scene_file: rc_material.dielectric must be 0 or 1 with ior > 0", error, error_capacity);
+            return RC_INVALID_ARG;
+        }
     for (int64_t i = 0; i < n * 9; ++i)
         if (!std::isfinite(vertices[i]))
         {
@@ -410,6 +417,8 @@ rc_status rc_save_scene(rc_tracer* h, const char* path)
         return fail(h, RC_INVALID_ARG, "save_scene: null path");
     if (!h->sceneReady)
         return fail(h, RC_NOT_READY, "save_scene: no scene uploaded");
+    if (h->nInstances > 0)
+        return fail(h, RC_UNSUPPORTED, "save_scene: instanced scenes are not stored in scene files");
     cudaSetDevice(h->device);
     HostScene hs;
     hs.flat = h->hostNodes;

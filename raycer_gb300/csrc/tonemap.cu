@@ -172,13 +172,13 @@ __global__ void k_linear(const float4* __restrict__ film, uint64_t pixels, float
 
 // ---- high-spp ground truth and display-space RMSE (float64) ----
 
-__global__ void k_film_acc64(float4* __restrict__ film, uint64_t pixels, double4* __restrict__ acc, int clear)
+__global__ void k_film_acc64(float4* __restrict__ film, uint64_t pixels, double4_32a* __restrict__ acc, int clear)
 {
     uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= pixels)
         return;
     float4 f = film[i];
-    double4 a = acc[i];
+    double4_32a a = acc[i];
     a.x += double(f.x);
     a.y += double(f.y);
     a.z += double(f.z);
@@ -188,12 +188,12 @@ __global__ void k_film_acc64(float4* __restrict__ film, uint64_t pixels, double4
         film[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 }
 
-__device__ __forceinline__ double3 truth_linear(double4 t)
+__device__ __forceinline__ double3 truth_linear(double4_32a t)
 {
     return make_double3(t.x / t.w, t.y / t.w, t.z / t.w);
 }
 
-__global__ void __launch_bounds__(kToneBlock) k_truth_reduce(const double4* __restrict__ truth, uint64_t pixels,
+__global__ void __launch_bounds__(kToneBlock) k_truth_reduce(const double4_32a* __restrict__ truth, uint64_t pixels,
                                                             double2* __restrict__ partial)
 {
     __shared__ double sSum[kToneBlock];
@@ -252,7 +252,7 @@ __device__ __forceinline__ double3 display(double r, double g, double b, const T
 }
 
 __global__ void __launch_bounds__(kToneBlock) k_rmse_apply(const float4* __restrict__ film,
-                                                          const double4* __restrict__ truth, uint64_t pixels,
+                                                          const double4_32a* __restrict__ truth, uint64_t pixels,
                                                           const ToneParams* __restrict__ tp, int applyGamma,
                                                           int shouldClamp, double invGamma,
                                                           double* __restrict__ partial)
@@ -325,7 +325,7 @@ cudaError_t launch_tonemap(const float4* film, uint64_t pixels, int type, int ap
     return cudaGetLastError();
 }
 
-cudaError_t launch_film_accumulate_f64(float4* film, uint64_t pixels, double4* acc, int clear, cudaStream_t stream)
+cudaError_t launch_film_accumulate_f64(float4* film, uint64_t pixels, double4_32a* acc, int clear, cudaStream_t stream)
 {
     k_film_acc64<<<unsigned((pixels + 255) / 256), 256, 0, stream>>>(film, pixels, acc, clear);
     return cudaGetLastError();
@@ -333,7 +333,7 @@ cudaError_t launch_film_accumulate_f64(float4* film, uint64_t pixels, double4* a
 
 size_t rmse_scratch_bytes() { return sizeof(double2) * 4096 + sizeof(ToneParams) + sizeof(double) * 4097; }
 
-cudaError_t launch_rmse_f64(const float4* film, const double4* truth, uint64_t pixels, int applyGamma, int shouldClamp,
+cudaError_t launch_rmse_f64(const float4* film, const double4_32a* truth, uint64_t pixels, int applyGamma, int shouldClamp,
                             double gamma, double key, void* scratch, double* result, cudaStream_t stream, int numSMs)
 {
     int blocks = reduce_blocks(pixels, numSMs);

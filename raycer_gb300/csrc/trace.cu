@@ -84,10 +84,11 @@ __global__ void __launch_bounds__(kBlock, RC_TRACE_MIN_BLOCKS) k_cast(DevScene s
             float4 r0 = __ldg(rp);
             float4 r1 = __ldg(rp + 1);
             RayF ray = make_ray(v3(r0.x, r0.y, r0.z), v3(r1.x, r1.y, r1.z), r0.w, r1.w);
-            HitF h{ -1, FLT_MAX, 0.0f, 0.0f };
-            bool found = traverse<ANY, ORDER, COUNT>(sc, ray, h, cnt, err);
+            HitF h{ -1, FLT_MAX, 0.0f, 0.0f, -1 };
+            bool found = traverse_scene<ANY, ORDER, COUNT>(sc, ray, h, cnt, err, -1, -1);
             int4 out;
-            out.x = found ? caller_index(sc, h.slot) : -1;
+            // two-level scenes: the flattened index (instance's first + mesh-local)
+            out.x = found ? caller_index(sc, h.slot) + (h.inst >= 0 ? __ldg(&sc.instances[h.inst].primBase) : 0) : -1;
             out.y = __float_as_int(found ? h.t : -1.0f);
             out.z = __float_as_int(found ? h.u : 0.0f);
             out.w = __float_as_int(found ? h.v : 0.0f);
@@ -149,7 +150,7 @@ __global__ void __launch_bounds__(kBlock, RC_TRACE_MIN_BLOCKS) k_raycast_primary
         if (valid)
         {
             RayF ray = primary_ray(cam, rays, pixelStart + uint64_t(i), i, width);
-            HitF h{ -1, FLT_MAX, 0.0f, 0.0f };
+            HitF h{ -1, FLT_MAX, 0.0f, 0.0f, -1 };
             bool found = traverse<false, ORDER, COUNT>(sc, ray, h, cnt, err);
             int4 o;
             o.x = found ? caller_index(sc, h.slot) : -1;
@@ -207,7 +208,7 @@ __global__ void __launch_bounds__(kBlock, RC_TRACE_MIN_BLOCKS) k_raycast_shadow(
             V3 ip = vfma(pr.d, t, pr.o);
             V3 dl = v3(L.x, L.y, L.z);
             RayF sr = make_ray(vfma(dl, rayStartOffset, ip), dl, 0.0f, FLT_MAX);
-            HitF h{ -1, FLT_MAX, 0.0f, 0.0f };
+            HitF h{ -1, FLT_MAX, 0.0f, 0.0f, -1 };
             bool occ = traverse<true, ORDER_REF, COUNT>(sc, sr, h, cnt, err, e.y);
             out[i].occluder = occ ? caller_index(sc, h.slot) : -1;
             out[i].flags = 1 | 2 | (occ ? 4 : 0);

@@ -107,6 +107,11 @@ void release_scene(rc_tracer* h)
     dev_free(h, &h->dTris, size_t(h->nTris));
     dev_free(h, &h->dShade, size_t(h->nTris));
     dev_free(h, &h->dMats, size_t(h->nMats));
+    dev_free(h, &h->dTlas, h->tlasCount);
+    dev_free(h, &h->dInstances, size_t(h->nInstances));
+    h->tlasCount = 0;
+    h->nInstances = 0;
+    h->tlasRoot = 0;
     h->sceneReady = false;
     h->nTris = 0;
     h->nMats = 0;
@@ -302,10 +307,11 @@ void build_host_scene(const double* v, const uint32_t* matIdx, int64_t n, const 
     {
         const rc_material& m = mats[i];
         uint32_t flags = (m.is_emissive ? kMatEmissive : 0u) | (m.non_shadowing ? kMatNonShadowing : 0u) |
-                         (m.invert_normal ? kMatInvertNormal : 0u);
+                         (m.invert_normal ? kMatInvertNormal : 0u) | (m.dielectric ? kMatDielectric : 0u);
         float ff;
         std::memcpy(&ff, &flags, 4);
-        hs.mats[size_t(i)].diffuse = make_float4(m.diffuse[0], m.diffuse[1], m.diffuse[2], 0.0f);
+        hs.mats[size_t(i)].diffuse =
+            make_float4(m.diffuse[0], m.diffuse[1], m.diffuse[2], m.dielectric ? m.ior : 0.0f);
         hs.mats[size_t(i)].emittance = make_float4(m.emittance[0], m.emittance[1], m.emittance[2], ff);
     }
     hs.depth = depth;
@@ -398,14 +404,15 @@ rc_status check_scene_args(rc_tracer* h, const double* v, const uint32_t* matIdx
         if (!std::isfinite(v[i]))
             return fail(h, RC_INVALID_ARG, "upload: non-finite vertex coordinate");
     for (int32_t i = 0; i < matCount; ++i)
-        if (mats[i].reserved != 0)
-            return fail(h, RC_INVALID_ARG, "upload: rc_material.reserved must be 0");
+        if ((mats[i].dielectric != 0 && mats[i].dielectric != 1) ||
+            (mats[i].dielectric && !(mats[i].ior > 0.0f && std::isfinite(mats[i].ior))))
+            return fail(h, RC_INVALID_ARG, "upload: rc_material.dielectric must be 0 or 1 with ior > 0");
     return RC_OK;
 }
 
 DevScene dev_scene(const rc_tracer* h)
 {
-    DevScene s;
+    DevScene s{};
     s.nodes = h->dNodes;
     s.tris = h->dTris;
     s.shade = h->dShade;
@@ -414,6 +421,10 @@ DevScene dev_scene(const rc_tracer* h)
     s.numTris = int(h->nTris);
     s.numMats = int(h->nMats);
     s.pad = 0;
+    s.tlas = h->dTlas;
+    s.instances = h->dInstances;
+    s.tlasRoot = h->tlasRoot;
+    s.numInstances = int(h->nInstances);
     return s;
 }
 
@@ -646,6 +657,8 @@ rc_status rc_get_bvh(const rc_tracer* hc, rc_bvh_node* nodes, int64_t node_capac
         return RC_INVALID_ARG;
     if (!h->sceneReady)
         return fail(h, RC_NOT_READY, "get_bvh: no scene uploaded");
+    if (h->nInstances > 0)
+        return fail(h, RC_UNSUPPORTED, "get_bvh: an instanced scene has one BVH per mesh and one over instances");
     if (node_count)
         *node_count = int64_t(h->hostNodes.size());
     if (nodes)
@@ -1078,6 +1091,9 @@ namespace rcx
 rc_status raycast_into(rc_tracer* h, const rc_ray* dRays, uint64_t pixelStart, uint64_t count, int order,
                        rc_cast_pixel* dOut, int* dQueue)
 {
+    if (h->nInstances > 0)
+        return fail(h, RC_UNSUPPORTED, "the RAY tracer's primary + shadow kernels trace single-level scenes; "
+                                       "instanced scenes are traced by rc_cast and PATH renders");
     float3 L = make_float3(0.0f, 0.0f, 0.0f);
     int castShadow = h->lights.empty() ? 0 : 1;
     if (castShadow)

@@ -46,6 +46,7 @@ struct HitF
     float t;
     float u;
     float v;
+    int inst;  // instance of the hit in a two-level scene, else -1
 };
 
 struct TravCount
@@ -198,6 +199,159 @@ __device__ __forceinline__ bool traverse(const DevScene& sc, const RayF& ray, Hi
             break;
         }
     }
+}
+
+// Ray in an instance's object space: o' = A o + b, d' = A d. d' is not
+// renormalised, so a hit's parameter t is the same in both spaces and the
+// levels share one closest distance. (The reference's Instance normalises
+// the direction and recomputes the world distance from the transformed hit
+// point, Instance.cpp:65-100: the same t in exact arithmetic.)
+__device__ __forceinline__ RayF instance_ray(const DevInstance& in, const RayF& r)
+{
+    if (in.identity)
+        return r;
+    V3 o = v3(__fmaf_rn(in.r0.x, r.o.x, __fmaf_rn(in.r0.y, r.o.y, __fmaf_rn(in.r0.z, r.o.z, in.r0.w))),
+              __fmaf_rn(in.r1.x, r.o.x, __fmaf_rn(in.r1.y, r.o.y, __fmaf_rn(in.r1.z, r.o.z, in.r1.w))),
+              __fmaf_rn(in.r2.x, r.o.x, __fmaf_rn(in.r2.y, r.o.y, __fmaf_rn(in.r2.z, r.o.z, in.r2.w))));
+    V3 d = v3(__fmaf_rn(in.r0.x, r.d.x, __fmaf_rn(in.r0.y, r.d.y, __fmul_rn(in.r0.z, r.d.z))),
+              __fmaf_rn(in.r1.x, r.d.x, __fmaf_rn(in.r1.y, r.d.y, __fmul_rn(in.r1.z, r.d.z))),
+              __fmaf_rn(in.r2.x, r.d.x, __fmaf_rn(in.r2.y, r.d.y, __fmul_rn(in.r2.z, r.d.z))));
+    return make_ray(o, d, r.tmin, r.tmax);
+}
+
+__device__ __forceinline__ DevInstance load_instance(const DevInstance* __restrict__ p, int k)
+{
+    const float4* q = reinterpret_cast<const float4*>(p + k);
+    DevInstance in;
+    in.r0 = __ldg(q + 0);
+    in.r1 = __ldg(q + 1);
+    in.r2 = __ldg(q + 2);
+    const int4 m = __ldg(reinterpret_cast<const int4*>(q + 3));
+    in.rootLink = m.x;
+    in.material = m.y;
+    in.primBase = m.z;
+    in.identity = m.w;
+    return in;
+}
+
+// Two-level traversal: the top-level BVH over instances (nearest child
+// first, culled by the closest hit), and inside each instance its mesh's
+// BVH with the object-space ray. `skip` / `skipInst` name the triangle (and
+// its instance) a secondary ray leaves from. Instance materials that are
+// nonShadowing are skipped by any-hit queries (Instance.cpp:25-26).
+template <bool ANY_HIT, bool COUNT>
+__device__ __noinline__ bool traverse_instanced(const DevScene& sc, const RayF& ray, HitF& hit, TravCount& cnt,
+                                                int& err, int skip, int skipInst)
+{
+    constexpr int kTopStack = 32;
+    int stack[kTopStack];
+    float sdist[kTopStack];
+    int sp = 0;
+    int cur = sc.tlasRoot;
+    bool found = false;
+    DevScene mesh = sc;
+    while (true)
+    {
+        if (cur >= 0)
+        {
+            float4 a, b, c;
+            int4 l;
+            load_node(sc.tlas, cur, a, b, c, l);
+            float e0, e1;
+            bool h0, h1;
+            if (ray.finite)
+            {
+                h0 = slab_finite(ray, a.x, a.y, a.z, a.w, c.x, c.y, e0);
+                h1 = slab_finite(ray, b.x, b.y, b.z, b.w, c.z, c.w, e1);
+            }
+            else
+            {
+                h0 = slab(ray, a.x, a.y, a.z, a.w, c.x, c.y, e0);
+                h1 = slab(ray, b.x, b.y, b.z, b.w, c.z, c.w, e1);
+            }
+            if (!ANY_HIT)
+            {
+                h0 = h0 && !(e0 > hit.t);
+                h1 = h1 && !(e1 > hit.t);
+            }
+            if (h0 && h1)
+            {
+                int nearC = l.x, farC = l.y;
+                float farD = e1;
+                if (!ANY_HIT && e1 < e0)
+                {
+                    nearC = l.y;
+                    farC = l.x;
+                    farD = e0;
+                }
+                if (sp >= kTopStack)
+                {
+                    err = 1;
+                    return found;
+                }
+                stack[sp] = farC;
+                sdist[sp] = farD;
+                sp++;
+                cur = nearC;
+                continue;
+            }
+            if (h0)
+            {
+                cur = l.x;
+                continue;
+            }
+            if (h1)
+            {
+                cur = l.y;
+                continue;
+            }
+        }
+        else
+        {
+            const int leaf = ~cur;
+            const int start = leaf >> kLeafCountBits;
+            const int count = leaf & ((1 << kLeafCountBits) - 1);
+            for (int i = 0; i < count; ++i)
+            {
+                const int k = start + i;
+                const DevInstance in = load_instance(sc.instances, k);
+                if (ANY_HIT && in.material >= 0 &&
+                    (__float_as_uint(__ldg(&sc.mats[in.material].emittance.w)) & kMatNonShadowing))
+                    continue;
+                const RayF r2 = instance_ray(in, ray);
+                mesh.rootLink = in.rootLink;
+                HitF h2 = hit;
+                if (traverse<ANY_HIT, ORDER_NEAREST, COUNT>(mesh, r2, h2, cnt, err, k == skipInst ? skip : -1))
+                {
+                    hit = h2;
+                    hit.inst = k;
+                    found = true;
+                    if (ANY_HIT)
+                        return true;
+                }
+            }
+        }
+        while (true)
+        {
+            if (sp == 0)
+                return found;
+            sp--;
+            cur = stack[sp];
+            if (!ANY_HIT && sdist[sp] > hit.t)
+                continue;
+            break;
+        }
+    }
+}
+
+// Either traversal, by the scene's kind.
+template <bool ANY_HIT, int ORDER, bool COUNT>
+__device__ __forceinline__ bool traverse_scene(const DevScene& sc, const RayF& ray, HitF& hit, TravCount& cnt,
+                                               int& err, int skip, int skipInst)
+{
+    if (sc.numInstances > 0)
+        return traverse_instanced<ANY_HIT, COUNT>(sc, ray, hit, cnt, err, skip, skipInst);
+    return traverse<ANY_HIT, ORDER, COUNT>(sc, ray, hit, cnt, err, skip);
 }
 
 }  // namespace rcx

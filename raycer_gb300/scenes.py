@@ -47,6 +47,8 @@ class Material:
     is_emissive: bool = False
     non_shadowing: bool = False
     invert_normal: bool = False
+    dielectric: bool = False   # GPU extension: smooth dielectric (Fresnel, refraction)
+    ior: float = 0.0
 
 
 @dataclass
@@ -431,3 +433,121 @@ def heightfield_blobs_scene(instances: int = 200, blob_level: int = 5, seed: int
         settings=dict(tracer="path", max_path_length=12, multi_sample_count_sqrt=1, path_sample_count=1,
                       sampler="cmj", miss_radiance=tuple(sky)),
     )
+
+
+# ---------------------------------------------------------------------------
+# Instanced (two-level) scenes.
+
+
+@dataclass
+class InstanceDesc:
+    """Instance (Instance.h:33-44): a placed copy of a mesh."""
+    mesh: int
+    material: int = -1                  # changePrimitive material, or -1: the mesh's own
+    scale: tuple = (1.0, 1.0, 1.0)
+    rotate: tuple = (0.0, 0.0, 0.0)     # pitch, yaw, roll in degrees (rotateXYZ)
+    translate: tuple = (0.0, 0.0, 0.0)
+
+
+@dataclass
+class InstancedScene:
+    name: str
+    meshes: list                        # [(vertices (n, 9) float64, material_index (n,) uint32)]
+    instances: list                     # [InstanceDesc]
+    materials: list                     # [Material]
+    camera: CameraDesc
+    width: int
+    height: int
+    light_direction: tuple | None = None
+    max_leaf_size: int = 4
+    settings: dict = field(default_factory=dict)
+
+    @property
+    def triangle_count(self) -> int:
+        """Triangles of the flattened scene."""
+        return int(sum(self.meshes[i.mesh][0].shape[0] for i in self.instances))
+
+    def flatten(self) -> SceneDesc:
+        """The same scene as world-space triangles, instance by instance
+        (the flattened primitive numbering of rc_upload_instanced)."""
+        verts, mats = [], []
+        for inst in self.instances:
+            v, m = self.meshes[inst.mesh]
+            M = instance_matrix(v, inst)
+            p = v.reshape(-1, 3) @ M[:3, :3].T + M[:3, 3]
+            verts.append(p.reshape(-1, 9))
+            mats.append(np.full(v.shape[0], inst.material, np.uint32) if inst.material >= 0 else m)
+        return SceneDesc(name=self.name + " (flattened)", vertices=np.concatenate(verts),
+                         material_index=np.concatenate(mats).astype(np.uint32), materials=self.materials,
+                         camera=self.camera, width=self.width, height=self.height,
+                         light_direction=self.light_direction, max_leaf_size=self.max_leaf_size,
+                         settings=dict(self.settings))
+
+
+def _rot(axis: int, deg: float) -> np.ndarray:
+    a = math.radians(deg)
+    s, c = math.sin(a), math.cos(a)
+    r = np.eye(4)
+    i, j = [(1, 2), (0, 2), (0, 1)][axis]
+    r[i, i] = c
+    r[j, j] = c
+    if axis == 1:   # rotateY: m[0][2] = s, m[2][0] = -s
+        r[i, j], r[j, i] = s, -s
+    else:           # rotateX / rotateZ: m[i][j] = -s, m[j][i] = s
+        r[i, j], r[j, i] = -s, s
+    return r
+
+
+def instance_matrix(mesh_vertices: np.ndarray, inst: InstanceDesc) -> np.ndarray:
+    """T(c + translate) * R_x R_y R_z * S(scale) * T(-c), c = the mesh box centre
+    (Instance::initialize, Instance.cpp:17-32)."""
+    p = mesh_vertices.reshape(-1, 3)
+    c = (p.min(axis=0) + p.max(axis=0)) * 0.5
+    t1 = np.eye(4)
+    t1[:3, 3] = -c
+    t2 = np.eye(4)
+    t2[:3, 3] = c + np.asarray(inst.translate, np.float64)
+    s = np.diag([*inst.scale, 1.0])
+    r = _rot(0, inst.rotate[0]) @ _rot(1, inst.rotate[1]) @ _rot(2, inst.rotate[2])
+    return t2 @ r @ s @ t1
+
+
+def heightfield_blobs_instanced(instances: int = 200, blob_level: int = 5, seed: int = 4, hf_nx: int = 1024,
+                                hf_nz: int = 512, width: int = 1920, height: int = 1080, sky=(1.0, 1.0, 1.0),
+                                dielectric_fraction: float = 0.0) -> InstancedScene:
+    """The heightfield (an identity instance of its own mesh) plus `instances`
+    placed copies of one random blob: uniform positions over the terrain,
+    Euler rotations U(0, 360)^3, uniform scale U(0.25, 0.6), each copy its
+    own material (albedo U(0.1, 0.9)^3; a fraction of them dielectric with
+    IOR U(1.3, 1.7))."""
+    hf = heightfield_scene(seed=2, nx=hf_nx, nz=hf_nz, width=width, height=height)
+    blob = blob_mesh(seed=seed, level=blob_level)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    px = -9.0 + 18.0 * rng.random(instances)
+    pz = -4.5 + 9.0 * rng.random(instances)
+    scale = 0.25 + 0.35 * rng.random(instances)
+    rot = 360.0 * rng.random((instances, 3))
+    albedo = (0.1 + 0.8 * rng.random((instances, 3))).astype(np.float32).astype(np.float64)
+    glass = rng.random(instances) < dielectric_fraction
+    ior = 1.3 + 0.4 * rng.random(instances)
+    g = hf.vertices.reshape(hf_nz - 1, hf_nx - 1, 2, 9)[:, :, 0, 0:3]
+    ix = np.clip(((px + 10.0) / 20.0 * (hf_nx - 1)).astype(int), 0, hf_nx - 2)
+    iz = np.clip(((pz + 5.0) / 10.0 * (hf_nz - 1)).astype(int), 0, hf_nz - 2)
+    py = g[iz, ix, 1] + scale * 0.6
+    bp = blob.reshape(-1, 3)
+    c = (bp.min(axis=0) + bp.max(axis=0)) * 0.5
+    mats = [Material(diffuse=(0.6, 0.6, 0.6))]
+    insts = [InstanceDesc(mesh=0)]
+    for k in range(instances):
+        mats.append(Material(diffuse=tuple(float(x) for x in albedo[k]), dielectric=bool(glass[k]),
+                             ior=float(np.float32(ior[k])) if glass[k] else 0.0))
+        insts.append(InstanceDesc(mesh=1, material=k + 1, scale=(float(scale[k]),) * 3,
+                                  rotate=tuple(float(x) for x in rot[k]),
+                                  translate=(float(px[k] - c[0]), float(py[k] - c[1]), float(pz[k] - c[2]))))
+    return InstancedScene(
+        name=f"heightfield + {instances} blob instances",
+        meshes=[(hf.vertices, hf.material_index), (blob, np.zeros(blob.shape[0], np.uint32))],
+        instances=insts, materials=mats, camera=hf.camera, width=width, height=height,
+        light_direction=None, max_leaf_size=4,
+        settings=dict(tracer="path", max_path_length=12, multi_sample_count_sqrt=1, path_sample_count=1,
+                      sampler="cmj", miss_radiance=tuple(sky)))

@@ -59,7 +59,8 @@ def materials_array(mats) -> C.Array:
         arr[i].is_emissive = int(m.is_emissive)
         arr[i].non_shadowing = int(m.non_shadowing)
         arr[i].invert_normal = int(m.invert_normal)
-        arr[i].reserved = 0
+        arr[i].dielectric = int(getattr(m, "dielectric", False))
+        arr[i].ior = float(getattr(m, "ior", 0.0)) if arr[i].dielectric else 0.0
     return arr
 
 
@@ -266,6 +267,35 @@ class CudaTracer:
             st = self._lib.rc_upload_scene_prebuilt(self._h, _ptr(v), _ptr(m), v.shape[0], mats,
                                                     len(scene.materials), _ptr(nodes), nodes.shape[0], _ptr(order))
         self._check(st, "initializeBuffers")
+        self._scene = scene
+        self._seed = seed
+        self._set_general(scene)
+        self._set_tonemapper(scene)
+        self._set_lights(scene)
+
+    def initializeInstanced(self, scene, seed: int = 1) -> None:
+        """Uploads a two-level scene (scenes.InstancedScene) with rc_upload_instanced."""
+        meshes = (N.rc_mesh * len(scene.meshes))()
+        keep = []
+        for i, (v, m) in enumerate(scene.meshes):
+            v = np.ascontiguousarray(v, np.float64)
+            m = np.ascontiguousarray(m, np.uint32)
+            keep += [v, m]
+            meshes[i].vertices = v.ctypes.data
+            meshes[i].material_index = m.ctypes.data
+            meshes[i].triangle_count = v.shape[0]
+        insts = (N.rc_instance * len(scene.instances))()
+        for i, d in enumerate(scene.instances):
+            insts[i].mesh = int(d.mesh)
+            insts[i].material = int(d.material)
+            insts[i].scale[:] = [float(x) for x in d.scale]
+            insts[i].rotate[:] = [float(x) for x in d.rotate]
+            insts[i].translate[:] = [float(x) for x in d.translate]
+        mats = materials_array(scene.materials)
+        self._check(self._lib.rc_upload_instanced(self._h, meshes, len(scene.meshes), insts, len(scene.instances),
+                                                  mats, len(scene.materials), int(scene.max_leaf_size)),
+                    "upload_instanced")
+        del keep
         self._scene = scene
         self._seed = seed
         self._set_general(scene)

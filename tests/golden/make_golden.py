@@ -188,5 +188,31 @@ def main() -> None:
     print("golden fixtures written:", sorted(p.name for p in OUT.iterdir()))
 
 
+INSTANCED = dict(instances=24, blob_level=3, hf_nx=128, hf_nz=64, width=160, height=90, seed=4)
+
+
+def instanced_golden() -> None:
+    """The reference's own Instance / PrimitiveGroup traversal (Instance.cpp,
+    PrimitiveGroup.cpp) on a small heightfield + blob-instances scene: mesh
+    and mesh-local triangle of every camera ray's closest hit, and its
+    distance. The scene is regenerated from its seeds by the tests."""
+    sc = scenes.heightfield_blobs_instanced(**INSTANCED)
+    ref = oracle.RefScene(sc)
+    state = ref.camera_state(sc.width, sc.height)
+    pix, rays = camera_ray_set(state, sc.width, sc.height, 1)
+    r32 = np.ascontiguousarray(rays).view(np.float32).reshape(-1, 8)
+    rays6 = np.concatenate([r32[:, 0:3], r32[:, 4:7]], axis=1).astype(np.float64)
+    prim, t = ref.intersect(rays6)
+    mesh = np.where(prim >= 0, prim // oracle.RefScene.MESH_ID, -1)
+    local = np.where(prim >= 0, prim % oracle.RefScene.MESH_ID, -1)
+    np.savez_compressed(OUT / "instanced.npz", camera_state=state, rays=r32, mesh=mesh.astype(np.int32),
+                        local=local.astype(np.int32), t=t)
+    print("instanced fixture written:", int((prim >= 0).sum()), "hits of", prim.size)
+
+
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["instanced"]:
+        instanced_golden()
+    else:
+        main()
+        instanced_golden()

@@ -1,0 +1,105 @@
+"""Instanced scenes and dielectrics on the GPU: closest hits of the
+two-level traversal against the reference's Instance traversal (committed
+fixture), renders against the flattened scene, dielectric films bit-exact
+against the float32 twin."""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import oracle
+from raycer_gb300 import scenes
+from raycer_gb300.tracer import RAY_DTYPE, CudaTracer, RaycerError, TracerState, camera_record
+
+from helpers import camera_floats, small_room
+from test_instancing import FIX, PARAMS, flat_to_mesh
+
+pytestmark = pytest.mark.gpu
+
+
+def test_hits_match_reference_instances():
+    sc = scenes.heightfield_blobs_instanced(**PARAMS)
+    rays = np.ascontiguousarray(FIX["rays"]).view(RAY_DTYPE).reshape(-1)
+    with CudaTracer(0) as t:
+        t.initializeInstanced(sc)
+        hits = t.cast(rays)
+    mesh, local = flat_to_mesh(sc, hits["prim"].astype(np.int64))
+    same = (mesh == FIX["mesh"]) & (local == FIX["local"])
+    assert same.mean() > 0.995, same.mean()
+    hit = same & (hits["prim"] >= 0)
+    np.testing.assert_allclose(hits["t"][hit], FIX["t"][hit], rtol=2e-5)
+
+
+def test_instanced_render_matches_flattened():
+    sc = scenes.heightfield_blobs_instanced(**PARAMS)
+    sc.settings.update(max_path_length=6)
+    flat = sc.flatten()
+    means = []
+    for s, inst in ((sc, True), (flat, False)):
+        with CudaTracer(0) as t:
+            if inst:
+                t.initializeInstanced(s, seed=4)
+            else:
+                t.initializeBuffers(s, seed=4)
+            t.initializeImageBuffers(s.width, s.height)
+            st = TracerState(scene=s, filmWidth=s.width, filmHeight=s.height, pixelCount=s.width * s.height)
+            for _ in range(32):
+                t.run(st)
+            f = t.read_film()
+            means.append(f[:, :3] / f[:, 3:4])
+    a, b = means
+    assert abs(a.mean() - b.mean()) < 0.01 * b.mean()
+    # the same random streams: most pixels follow the same paths
+    close = np.abs(a - b).max(axis=1) < 1e-3 * np.maximum(1.0, np.abs(b).max(axis=1))
+    assert close.mean() > 0.8, close.mean()
+
+
+def test_instanced_scene_refuses_ray_frames():
+    sc = scenes.heightfield_blobs_instanced(instances=2, blob_level=1, hf_nx=16, hf_nz=8, width=16, height=8)
+    sc.settings["tracer"] = "ray"
+    with CudaTracer(0) as t:
+        t.initializeInstanced(sc)
+        t.initializeImageBuffers(sc.width, sc.height)
+        with pytest.raises(RaycerError):
+            t.run(TracerState(scene=sc, filmWidth=16, filmHeight=8, pixelCount=128))
+
+
+@pytest.mark.parametrize("ms", [1, 2])
+def test_dielectric_film_bit_exact(ms):
+    sc = small_room(width=40, height=30)
+    # make a third of the clutter glass
+    mats = list(sc.materials)
+    rng = np.random.default_rng(3)
+    for i in range(1, len(mats)):
+        if not mats[i].is_emissive and rng.random() < 0.35:
+            m = mats[i]
+            mats[i] = scenes.Material(diffuse=m.diffuse, dielectric=True, ior=float(np.float32(1.3 + 0.4 * rng.random())))
+    sc.materials = mats
+    sc.settings.update(multi_sample_count_sqrt=ms, max_path_length=6)
+    assert any(m.dielectric for m in mats)
+    with CudaTracer(0) as t:
+        t.initializeBuffers(sc, seed=8)
+        t.initializeImageBuffers(sc.width, sc.height)
+        t.run(TracerState(scene=sc, filmWidth=sc.width, filmHeight=sc.height, pixelCount=sc.width * sc.height))
+        film = t.read_film()
+        cam = camera_floats(camera_record(sc))
+    orc = oracle.Oracle(sc)
+    ref, _ = orc.render_path32(cam, sc.width, sc.width * sc.height, ms, 1, 4, (0.5, 0.5), 1e-5, 6, 0, 1, 8, 0)
+    assert np.array_equal(film, ref), f"{(film != ref).any(axis=1).sum()} pixels differ"
+
+
+def test_cache_renders_instanced_dielectric_scene():
+    from raycer_gb300.nrc import RadianceCache
+    sc = scenes.heightfield_blobs_instanced(**PARAMS, dielectric_fraction=0.3)
+    with CudaTracer(0) as t:
+        t.initializeInstanced(sc, seed=2)
+        t.initializeImageBuffers(sc.width, sc.height)
+        c = RadianceCache(t)
+        st = TracerState(scene=sc, filmWidth=sc.width, filmHeight=sc.height, pixelCount=sc.width * sc.height)
+        for _ in range(8):
+            t.run(st)
+        film = t.read_film()
+        stats = c.stats()
+    assert np.isfinite(film).all() and film[:, :3].mean() > 0.05
+    assert stats["lookups"] > 0 and stats["training_samples"] > 0 and np.isfinite(stats["last_loss"])
