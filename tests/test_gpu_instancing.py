@@ -50,9 +50,14 @@ def test_instanced_render_matches_flattened():
             means.append(f[:, :3] / f[:, 3:4])
     a, b = means
     assert abs(a.mean() - b.mean()) < 0.01 * b.mean()
-    # the same random streams: most pixels follow the same paths
-    close = np.abs(a - b).max(axis=1) < 1e-3 * np.maximum(1.0, np.abs(b).max(axis=1))
-    assert close.mean() > 0.8, close.mean()
+    # An instance transforms its mesh's shading frame (Instance.cpp:98-99), the
+    # flattened triangle builds its own: same distribution, other directions
+    # for the same random numbers, so compare 8x8-block means.
+    h, w = sc.height, sc.width
+    ba = a.mean(axis=1).reshape(h // 8, 8, w // 8, 8).mean(axis=(1, 3))
+    bb = b.mean(axis=1).reshape(h // 8, 8, w // 8, 8).mean(axis=(1, 3))
+    rel = np.sqrt(np.mean((ba - bb) ** 2)) / bb.mean()
+    assert rel < 0.05, rel
 
 
 def test_instanced_scene_refuses_ray_frames():
