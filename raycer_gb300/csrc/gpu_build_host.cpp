@@ -238,6 +238,11 @@ rc_status upload_gpu_built(rc_tracer* h, const double* v, const uint32_t* matIdx
     }
     h->rootLink = rootLink;
     h->bvhDepth = flatDepth;
+    for (int k = 0; k < 3; ++k)
+    {
+        h->bounds[k] = flat[0].bmin[k];
+        h->bounds[3 + k] = flat[0].bmax[k];
+    }
     h->bvhInner = kept;
     h->hostNodes = std::move(flat);
     h->hostOrder = std::move(order);

@@ -92,6 +92,7 @@ struct rc_tracer
     bool sceneReady = false;
     std::vector<rcx::BuildNode> hostNodes;
     std::vector<uint32_t> hostOrder;
+    double bounds[6] = { 0, 0, 0, 0, 0, 0 };  // scene box: min xyz, max xyz
     // Two-level scenes (rc_upload_instanced): top-level BVH over instances.
     rcx::DevNode* dTlas = nullptr;
     size_t tlasCount = 0;

@@ -306,6 +306,13 @@ extern "C" rc_status rc_upload_instanced(rc_tracer* h, const rc_mesh* meshes, in
 
     BuildResult tb;
     std::string err;
+    double sceneBox[6] = { 1e300, 1e300, 1e300, -1e300, -1e300, -1e300 };
+    for (int64_t k = 0; k < ni; ++k)
+        for (int a = 0; a < 3; ++a)
+        {
+            sceneBox[a] = std::min(sceneBox[a], boxTris[size_t(k) * 9 + a]);
+            sceneBox[3 + a] = std::max(sceneBox[3 + a], boxTris[size_t(k) * 9 + 3 + a]);
+        }
     if (!buildFlatBVH(boxTris.data(), ni, 2, 0, tb, err))
         return fail(h, RC_INVALID_ARG, "upload_instanced: top-level build: " + err);
     if (tb.depth > 32)
@@ -384,6 +391,8 @@ extern "C" rc_status rc_upload_instanced(rc_tracer* h, const rc_mesh* meshes, in
                       mats.size() * sizeof(DevMat) + tn.size() * sizeof(DevNode) + ordered.size() * sizeof(DevInstance);
     h->hostNodes.clear();
     h->hostOrder.clear();
+    for (int k = 0; k < 6; ++k)
+        h->bounds[k] = sceneBox[k];
     h->sceneReady = true;
     h->stats.build_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     return RC_OK;

@@ -171,12 +171,12 @@ rc_status encoding_box(rc_tracer* h, NrcBox& box)
     }
     else
     {
-        if (!h->sceneReady || h->hostNodes.empty())
+        if (!h->sceneReady)
             return fail(h, RC_NOT_READY, "nrc: no encoding box configured and no scene bounds");
         for (int k = 0; k < 3; ++k)
         {
-            lo[k] = h->hostNodes[0].bmin[k];
-            hi[k] = h->hostNodes[0].bmax[k];
+            lo[k] = h->bounds[k];
+            hi[k] = h->bounds[3 + k];
             if (!(hi[k] > lo[k]))
                 hi[k] = lo[k] + 1.0;
         }

@@ -355,6 +355,11 @@ rc_status upload_host_scene(rc_tracer* h, HostScene&& hs)
     h->rootLink = rootLink;
     h->bvhDepth = hs.depth;
     h->bvhInner = inner;
+    for (int k = 0; k < 3; ++k)
+    {
+        h->bounds[k] = hs.flat[0].bmin[k];
+        h->bounds[3 + k] = hs.flat[0].bmax[k];
+    }
     h->hostNodes = std::move(hs.flat);
     h->hostOrder = std::move(hs.order);
     h->sceneReady = true;

@@ -52,10 +52,10 @@ def test_instanced_render_matches_flattened():
     assert abs(a.mean() - b.mean()) < 0.01 * b.mean()
     # An instance transforms its mesh's shading frame (Instance.cpp:98-99), the
     # flattened triangle builds its own: same distribution, other directions
-    # for the same random numbers, so compare 8x8-block means.
+    # for the same random numbers, so compare 10x10-block means.
     h, w = sc.height, sc.width
-    ba = a.mean(axis=1).reshape(h // 8, 8, w // 8, 8).mean(axis=(1, 3))
-    bb = b.mean(axis=1).reshape(h // 8, 8, w // 8, 8).mean(axis=(1, 3))
+    ba = a.mean(axis=1).reshape(h // 10, 10, w // 10, 10).mean(axis=(1, 3))
+    bb = b.mean(axis=1).reshape(h // 10, 10, w // 10, 10).mean(axis=(1, 3))
     rel = np.sqrt(np.mean((ba - bb) ** 2)) / bb.mean()
     assert rel < 0.05, rel
 
