@@ -52,10 +52,10 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--order", choices=["nearest", "reference"], default="nearest")
-    ap.add_argument("--workload", choices=["raycast", "batch", "nrc", "build"], default="raycast",
+    ap.add_argument("--workload", choices=["raycast", "batch", "nrc", "build", "large"], default="raycast",
                     help="raycast: the 1080p heightfield frame (default); batch: 64 rooms in one graph launch; "
                          "nrc: time to display RMSE 0.01, radiance cache vs plain path tracing")
-    ap.add_argument("--gt-spp", type=int, default=4096, help="nrc: ground-truth samples per pixel")
+    ap.add_argument("--gt-spp", type=int, default=4096, help="nrc / large: ground-truth samples per pixel")
     ap.add_argument("--scale", type=float, default=1.0, help="nrc: film scale (1 = 1920x1080)")
     ap.add_argument("--terminate-segment", type=int, default=2,
                     help="nrc: paths end into the cache at the hit of this segment")
@@ -548,6 +548,74 @@ def run_build(args, rank, world):
     return 0
 
 
+def run_large(args, rank, world):
+    """The combined run: 3840x2160, depth 16, a 4,188,162-triangle fBm
+    heightfield (seed 5) + 800 instances of a 20,480-triangle blob (30 %
+    dielectric, IOR U(1.3, 1.7)), sky-lit. Plain path tracing for 256 frames
+    of 1 spp, then the radiance-cache tracer until its display RMSE against a
+    float64 ground truth (1,024 spp: 64 frames of 16 paths per pixel) reaches
+    the plain run's; times are the renders' wall clock."""
+    if rank != 0:
+        return 0
+    from raycer_gb300 import scenes
+    from raycer_gb300.nrc import GroundTruth, RadianceCache
+    from raycer_gb300.nrc_eval import _run
+    from raycer_gb300.tracer import CudaTracer, TracerState, general_record
+
+    w, h = int(round(3840 * args.scale)), int(round(2160 * args.scale))
+    t0 = time.perf_counter()
+    sc = scenes.heightfield_blobs_instanced(instances=800, blob_level=5, seed=5, hf_nx=2048, hf_nz=1024, width=w,
+                                            height=h, dielectric_fraction=0.3, hf_seed=5)
+    sc.settings.update(max_path_length=16)
+    gen_s = time.perf_counter() - t0
+    log = lambda m: print(m, file=sys.stderr, flush=True)
+    with CudaTracer(0) as t:
+        t.initializeInstanced(sc, seed=5)
+        upload_ms = t.stats()["build_ms"]
+        t.initializeImageBuffers(w, h)
+        st = TracerState(scene=sc, filmWidth=w, filmHeight=h, pixelCount=w * h)
+        gt_settings = dict(sc.settings, path_sample_count=16)
+        gt_scene = scenes.InstancedScene(**{**sc.__dict__, "settings": gt_settings})
+        t.set_general(general_record(gt_scene, seed=5))
+        gt = GroundTruth(t)
+        t1 = time.perf_counter()
+        for i in range(args.gt_spp // 16):
+            t.run(st)
+            gt.add_film(clear_film=True)
+        gt_s = time.perf_counter() - t1
+        log(f"ground truth {args.gt_spp} spp in {gt_s:.1f} s")
+        t.set_general(general_record(sc, seed=5 + 7919))
+        plain = _run(t, st, gt, 0.0, 256, 1e9, 256)
+        log(f"plain 256 frames: {plain.seconds:.2f} s, rmse {plain.rmse:.4f}")
+        cache = RadianceCache(t)
+        cached = _run(t, st, gt, plain.rmse, 1024, 180.0, 4)
+        log(f"cache: {cached.frames} frames, {cached.seconds:.2f} s, rmse {cached.rmse:.4f}")
+        stats = cache.stats()
+    line = {
+        "metric": "Mrays/s", "value": round(plain.rays / plain.seconds / 1e6, 1), "unit": "Mrays/s",
+        "n_gpus": 1, "steps": plain.frames, "warmup": 0,
+        "ms_per_step": round(1e3 * plain.seconds / plain.frames, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 (paths) / bf16 (cache MLP)",
+        "data": "synthetic (seeded heightfield + blob instances)",
+        "config": {"workload": f"combined run: {w}x{h}, depth 16, heightfield 4,188,162 tris + 800 x 20,480-tri "
+                               f"blob instances ({sc.triangle_count} flattened), 30 % dielectric, sky-lit",
+                   "scene_generation_s": round(gen_s, 1), "upload_and_build_ms": round(upload_ms, 1),
+                   "gt_spp": args.gt_spp, "gt_seconds": round(gt_s, 1)},
+        "plain_256spp": {"seconds": round(plain.seconds, 3), "rmse": round(plain.rmse, 5),
+                         "mrays_per_s": round(plain.rays / plain.seconds / 1e6, 1)},
+        "cache_equal_rmse": {"frames": cached.frames, "seconds": round(cached.seconds, 3),
+                             "rmse": round(cached.rmse, 5), "reached": cached.reached,
+                             "mrays_per_s": round(cached.rays / max(cached.seconds, 1e-9) / 1e6, 1)},
+        "time_ratio_cache_over_plain": round(cached.seconds / plain.seconds, 3) if cached.reached else None,
+        "cache_stats": {k: (round(v, 4) if isinstance(v, float) else v) for k, v in stats.items()},
+        "cpu_baseline": None,
+        "cpu_baseline_note": "the reference's CPU path tracer has no dielectrics and its instancing is host-only; "
+                             "the CPU comparison is the RAY-frame workload's",
+    }
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     args = parse_args()
     rank, local_rank, world = dist_env()
@@ -557,6 +625,8 @@ def main():
         return run_nrc(args, rank, world)
     if args.workload == "build":
         return run_build(args, rank, world)
+    if args.workload == "large":
+        return run_large(args, rank, world)
     if args.impl == "reference":
         return run_reference(args, rank, world)
     return run_ours(args, rank, local_rank, world)

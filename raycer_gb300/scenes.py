@@ -514,13 +514,13 @@ def instance_matrix(mesh_vertices: np.ndarray, inst: InstanceDesc) -> np.ndarray
 
 def heightfield_blobs_instanced(instances: int = 200, blob_level: int = 5, seed: int = 4, hf_nx: int = 1024,
                                 hf_nz: int = 512, width: int = 1920, height: int = 1080, sky=(1.0, 1.0, 1.0),
-                                dielectric_fraction: float = 0.0) -> InstancedScene:
+                                dielectric_fraction: float = 0.0, hf_seed: int = 2) -> InstancedScene:
     """The heightfield (an identity instance of its own mesh) plus `instances`
     placed copies of one random blob: uniform positions over the terrain,
     Euler rotations U(0, 360)^3, uniform scale U(0.25, 0.6), each copy its
     own material (albedo U(0.1, 0.9)^3; a fraction of them dielectric with
     IOR U(1.3, 1.7))."""
-    hf = heightfield_scene(seed=2, nx=hf_nx, nz=hf_nz, width=width, height=height)
+    hf = heightfield_scene(seed=hf_seed, nx=hf_nx, nz=hf_nz, width=width, height=height)
     blob = blob_mesh(seed=seed, level=blob_level)
     rng = np.random.Generator(np.random.PCG64(seed))
     px = -9.0 + 18.0 * rng.random(instances)
