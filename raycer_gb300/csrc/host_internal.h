@@ -142,6 +142,13 @@ struct rc_tracer
     size_t capTmpB = 0;
 
     rcx::DevControl* dCtl = nullptr;
+    // Host-buffer ray casts: copies on their own streams, overlapped with
+    // the kernels chunk by chunk.
+    cudaStream_t copyIn = nullptr;
+    cudaStream_t copyOut = nullptr;
+    std::vector<cudaEvent_t> evChunk;
+    void* dCtlChunks = nullptr;
+    size_t capCtlChunks = 0;
     rc_stats stats{};
     size_t deviceBytes = 0;
 

@@ -572,6 +572,14 @@ void rc_destroy(rc_tracer* h)
         cudaEventDestroy(h->evMid);
     for (cudaEvent_t e : h->evPool)
         cudaEventDestroy(e);
+    for (cudaEvent_t e : h->evChunk)
+        cudaEventDestroy(e);
+    if (h->dCtlChunks)
+        cudaFree(h->dCtlChunks);
+    if (h->copyIn)
+        cudaStreamDestroy(h->copyIn);
+    if (h->copyOut)
+        cudaStreamDestroy(h->copyOut);
     if (h->stream)
         cudaStreamDestroy(h->stream);
     delete h;
@@ -1026,22 +1034,102 @@ rc_status rc_cast_with_shadow(rc_tracer* h, const rc_ray* rays, int64_t n, int32
         return fail(h, RC_INVALID_ARG, "cast_with_shadow: bad ray count or null buffer");
     if (order != RC_ORDER_REFERENCE && order != RC_ORDER_NEAREST)
         return fail(h, RC_INVALID_ARG, "cast_with_shadow: invalid traversal order");
+    if (h->nInstances > 0)
+        return fail(h, RC_UNSUPPORTED, "cast_with_shadow: instanced scenes are traced by rc_cast and PATH renders");
     cudaSetDevice(h->device);
     rc_status s;
+    // Chunks of at least 512k rays: chunk i's upload, chunk i-1's kernels and
+    // chunk i-2's download run at the same time on three streams.
+    constexpr int64_t kMinChunk = int64_t(1) << 19;
+    constexpr int kMaxChunks = 8;
+    const int chunks = int(std::max<int64_t>(1, std::min<int64_t>(kMaxChunks, n / kMinChunk)));
+    const int64_t per = (n + chunks - 1) / chunks;
     size_t rayBytes = size_t(n) * sizeof(rc_ray);
     size_t outBytes = size_t(n) * (sizeof(rc_cast_pixel) + 2 * sizeof(int));
     if ((s = ensure_bytes(h, &h->dTmpA, &h->capTmpA, rayBytes, "allocate ray buffer")) != RC_OK ||
-        (s = ensure_bytes(h, &h->dTmpB, &h->capTmpB, outBytes, "allocate output buffer")) != RC_OK)
+        (s = ensure_bytes(h, &h->dTmpB, &h->capTmpB, outBytes, "allocate output buffer")) != RC_OK ||
+        (s = ensure_bytes(h, &h->dCtlChunks, &h->capCtlChunks, size_t(kMaxChunks) * sizeof(DevControl),
+                          "allocate control blocks")) != RC_OK)
         return s;
-    RC_CUDA_TRY(h, cudaMemcpyAsync(h->dTmpA, rays, rayBytes, cudaMemcpyHostToDevice, h->stream), "upload rays");
+    if (!h->copyIn)
+        RC_CUDA_TRY(h, cudaStreamCreateWithFlags(&h->copyIn, cudaStreamNonBlocking), "create copy stream");
+    if (!h->copyOut)
+        RC_CUDA_TRY(h, cudaStreamCreateWithFlags(&h->copyOut, cudaStreamNonBlocking), "create copy stream");
+    while (h->evChunk.size() < size_t(2 * kMaxChunks + 1))
+    {
+        cudaEvent_t e;
+        RC_CUDA_TRY(h, cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "create event");
+        h->evChunk.push_back(e);
+    }
+    const rc_ray* dRays = static_cast<const rc_ray*>(h->dTmpA);
     rc_cast_pixel* dOut = static_cast<rc_cast_pixel*>(h->dTmpB);
     int* dQueue = reinterpret_cast<int*>(dOut + n);
-    s = raycast_into(h, static_cast<const rc_ray*>(h->dTmpA), 0, uint64_t(n), order, dOut, dQueue);
-    if (s != RC_OK)
-        return s;
-    RC_CUDA_TRY(h, cudaMemcpyAsync(out, dOut, size_t(n) * sizeof(rc_cast_pixel), cudaMemcpyDeviceToHost, h->stream),
-                "download results");
+    DevControl* ctl = static_cast<DevControl*>(h->dCtlChunks);
+    float3 L = make_float3(0.0f, 0.0f, 0.0f);
+    const int castShadow = h->lights.empty() ? 0 : 1;
+    if (castShadow)
+        L = make_float3(-h->lights[0].direction[0], -h->lights[0].direction[1], -h->lights[0].direction[2]);
+    const DevCamera cam = dev_camera(h->camera);
+    const DevScene sc = dev_scene(h);
+    LaunchInfo li = launch_info(h);
+
+    // the previous call's downloads must be done before this call's kernels
+    // rewrite the output buffer
+    RC_CUDA_TRY(h, cudaEventRecord(h->evChunk[2 * kMaxChunks], h->copyOut), "record event");
+    RC_CUDA_TRY(h, cudaStreamWaitEvent(h->stream, h->evChunk[2 * kMaxChunks], 0), "order streams");
+    RC_CUDA_TRY(h, cudaMemsetAsync(ctl, 0, size_t(chunks) * sizeof(DevControl), h->stream), "reset control blocks");
+    RC_CUDA_TRY(h, cudaEventRecord(h->ev0, h->stream), "record start event");
+    RC_CUDA_TRY(h, cudaStreamWaitEvent(h->copyIn, h->ev0, 0), "order streams");
+    for (int c = 0; c < chunks; ++c)
+    {
+        const int64_t off = c * per;
+        const int64_t cnt = std::min<int64_t>(per, n - off);
+        if (cnt <= 0)
+            break;
+        RC_CUDA_TRY(h, cudaMemcpyAsync(const_cast<rc_ray*>(dRays) + off, rays + off, size_t(cnt) * sizeof(rc_ray),
+                                       cudaMemcpyHostToDevice, h->copyIn),
+                    "upload rays");
+        RC_CUDA_TRY(h, cudaEventRecord(h->evChunk[2 * c], h->copyIn), "record event");
+        RC_CUDA_TRY(h, cudaStreamWaitEvent(h->stream, h->evChunk[2 * c], 0), "order streams");
+        RC_CUDA_TRY(h,
+                    launch_raycast(li, sc, cam, dRays + off, 0, cnt, 1, order, castShadow, L,
+                                   h->general.ray_start_offset, dOut + off, dQueue, ctl + c, nullptr),
+                    "launch ray-cast kernels");
+        RC_CUDA_TRY(h, cudaEventRecord(h->evChunk[2 * c + 1], h->stream), "record event");
+        RC_CUDA_TRY(h, cudaStreamWaitEvent(h->copyOut, h->evChunk[2 * c + 1], 0), "order streams");
+        RC_CUDA_TRY(h, cudaMemcpyAsync(out + off, dOut + off, size_t(cnt) * sizeof(rc_cast_pixel),
+                                       cudaMemcpyDeviceToHost, h->copyOut),
+                    "download results");
+    }
+    RC_CUDA_TRY(h, cudaEventRecord(h->ev1, h->copyOut), "record end event");
+    std::vector<DevControl> ctls(static_cast<size_t>(chunks));
+    RC_CUDA_TRY(h, cudaMemcpyAsync(ctls.data(), ctl, size_t(chunks) * sizeof(DevControl), cudaMemcpyDeviceToHost,
+                                   h->stream),
+                "read control blocks");
     RC_CUDA_TRY(h, cudaStreamSynchronize(h->stream), "cast_with_shadow");
+    RC_CUDA_TRY(h, cudaStreamSynchronize(h->copyOut), "cast_with_shadow");
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+    const double buildMs = h->stats.build_ms;
+    h->stats = rc_stats{};
+    h->stats.build_ms = buildMs;
+    h->stats.last_ms = double(ms);
+    int err = 0;
+    for (const DevControl& c : ctls)
+    {
+        for (int k = 0; k < 2; ++k)
+        {
+            h->stats.stage_rays[k] += c.stats[3 * k + 0];
+            h->stats.stage_nodes[k] += c.stats[3 * k + 1];
+            h->stats.stage_tris[k] += c.stats[3 * k + 2];
+        }
+        err |= c.error;
+    }
+    h->stats.rays_traced = h->stats.stage_rays[0] + h->stats.stage_rays[1];
+    h->stats.node_visits = h->stats.stage_nodes[0] + h->stats.stage_nodes[1];
+    h->stats.tri_tests = h->stats.stage_tris[0] + h->stats.stage_tris[1];
+    if (err & 1)
+        return fail(h, RC_DEVICE_ERROR, "cast_with_shadow: traversal stack overflow");
     return RC_OK;
 }
 

@@ -62,3 +62,23 @@ def test_cast_random_rays_bit_exact(any_hit, order):
     assert np.array_equal(hits["t"], tt)
     assert np.array_equal(hits["u"], u)
     assert np.array_equal(hits["v"], v)
+
+
+def test_cast_with_shadow_chunked_equals_frame():
+    """2,073,600 caller rays go through the chunked, copy-overlapped path
+    (4 chunks on three streams); the results equal the RAY frame's."""
+    from raycer_gb300.tracer import RAY_DTYPE, TracerState
+
+    sc = small_heightfield(width=1920, height=1080)
+    sc.settings["tracer"] = "ray"
+    n = sc.width * sc.height
+    with CudaTracer(0) as t:
+        t.initializeBuffers(sc)
+        t.initializeImageBuffers(sc.width, sc.height)
+        t.run(TracerState(scene=sc, filmWidth=sc.width, filmHeight=sc.height, pixelCount=n))
+        frame = t.read_cast()
+        rays = oracle.camera_rays32(camera_floats(camera_record(sc)), sc.width, n)
+        out = t.cast_with_shadow(np.ascontiguousarray(rays).view(RAY_DTYPE).reshape(-1))
+        stats = t.stats()
+    assert np.array_equal(out, frame)
+    assert stats["rays_traced"] == n + int((frame["prim"] >= 0).sum())
