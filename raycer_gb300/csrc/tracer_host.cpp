@@ -1038,9 +1038,13 @@ rc_status rc_cast_with_shadow(rc_tracer* h, const rc_ray* rays, int64_t n, int32
         return fail(h, RC_UNSUPPORTED, "cast_with_shadow: instanced scenes are traced by rc_cast and PATH renders");
     cudaSetDevice(h->device);
     rc_status s;
-    // Chunks of at least 512k rays: chunk i's upload, chunk i-1's kernels and
-    // chunk i-2's download run at the same time on three streams.
-    constexpr int64_t kMinChunk = int64_t(1) << 19;
+    // Chunks of at least 2^RC_CAST_MIN_CHUNK_LOG2 rays: chunk i's upload,
+    // chunk i-1's kernels and chunk i-2's download run at the same time on
+    // three streams.
+#ifndef RC_CAST_MIN_CHUNK_LOG2
+#define RC_CAST_MIN_CHUNK_LOG2 19
+#endif
+    constexpr int64_t kMinChunk = int64_t(1) << RC_CAST_MIN_CHUNK_LOG2;
     constexpr int kMaxChunks = 8;
     const int chunks = int(std::max<int64_t>(1, std::min<int64_t>(kMaxChunks, n / kMinChunk)));
     const int64_t per = (n + chunks - 1) / chunks;
