@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <chrono>
 #include <cfloat>
 #include <cmath>
@@ -1024,6 +1025,32 @@ rc_status rc_cast(rc_tracer* h, const rc_ray* rays, int64_t n, int32_t any_hit, 
     return RC_OK;
 }
 
+// Device address of a caller's host buffer when kernels may access it in
+// place: page-locked memory mapped into the device's address space, or any
+// memory on a device that reads pageable memory coherently (Grace-class
+// hosts). nullptr otherwise.
+void* device_view(rc_tracer* h, const void* p)
+{
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess)
+    {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type == cudaMemoryTypeHost && a.devicePointer && a.device == h->device)
+        return a.devicePointer;
+    if (a.type == cudaMemoryTypeManaged || (a.type == cudaMemoryTypeDevice && a.device == h->device))
+        return const_cast<void*>(p);
+    int pageable = 0;
+    if (a.type == cudaMemoryTypeUnregistered &&
+        cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccessUsesHostPageTables, h->device) ==
+            cudaSuccess &&
+        pageable)
+        return const_cast<void*>(p);
+    cudaGetLastError();
+    return nullptr;
+}
+
 rc_status rc_cast_with_shadow(rc_tracer* h, const rc_ray* rays, int64_t n, int32_t order, rc_cast_pixel* out)
 {
     if (!h)
@@ -1038,6 +1065,26 @@ rc_status rc_cast_with_shadow(rc_tracer* h, const rc_ray* rays, int64_t n, int32
         return fail(h, RC_UNSUPPORTED, "cast_with_shadow: instanced scenes are traced by rc_cast and PATH renders");
     cudaSetDevice(h->device);
     rc_status s;
+    // In place when the device can reach both host buffers (16-byte aligned):
+    // the kernels read the rays and write the results over the host link, so
+    // no separate copy has to wait for the persistent kernels.
+    // (RC_CAST_COPY=1 in the environment forces the copy path.)
+    const char* forceCopy = std::getenv("RC_CAST_COPY");
+    if (!(forceCopy && forceCopy[0] == '1'))
+    {
+        void* vr = device_view(h, rays);
+        void* vo = vr ? device_view(h, out) : nullptr;
+        if (vr && vo && ((reinterpret_cast<uintptr_t>(vr) | reinterpret_cast<uintptr_t>(vo)) & 15u) == 0)
+        {
+            if ((s = ensure_bytes(h, &h->dTmpB, &h->capTmpB, size_t(n) * 2 * sizeof(int), "allocate shadow queue")) !=
+                RC_OK)
+                return s;
+            s = raycast_into(h, static_cast<const rc_ray*>(vr), 0, uint64_t(n), order, static_cast<rc_cast_pixel*>(vo),
+                             static_cast<int*>(h->dTmpB));
+            h->stats.stage_ms[0] = h->stats.stage_ms[1] = 0.0;
+            return s;
+        }
+    }
     // Chunks of at least 2^RC_CAST_MIN_CHUNK_LOG2 rays: chunk i's upload,
     // chunk i-1's kernels and chunk i-2's download run at the same time on
     // three streams.

@@ -64,11 +64,16 @@ def test_cast_random_rays_bit_exact(any_hit, order):
     assert np.array_equal(hits["v"], v)
 
 
-def test_cast_with_shadow_chunked_equals_frame():
-    """2,073,600 caller rays go through the chunked, copy-overlapped path
-    (4 chunks on three streams); the results equal the RAY frame's."""
+@pytest.mark.parametrize("copy", [False, True])
+def test_cast_with_shadow_host_buffers_equal_frame(copy, monkeypatch):
+    """2,073,600 caller rays from host buffers: traced in place where the
+    device reaches host memory, else (and with RC_CAST_COPY=1) through the
+    chunked copy path (4 chunks on three streams); the results equal the RAY
+    frame's either way."""
     from raycer_gb300.tracer import RAY_DTYPE, TracerState
 
+    if copy:
+        monkeypatch.setenv("RC_CAST_COPY", "1")
     sc = small_heightfield(width=1920, height=1080)
     sc.settings["tracer"] = "ray"
     n = sc.width * sc.height
