@@ -52,7 +52,7 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--order", choices=["nearest", "reference"], default="nearest")
-    ap.add_argument("--workload", choices=["raycast", "batch", "nrc", "build", "large"], default="raycast",
+    ap.add_argument("--workload", choices=["raycast", "batch", "nrc", "build", "large", "path"], default="raycast",
                     help="raycast: the 1080p heightfield frame (default); batch: 64 rooms in one graph launch; "
                          "nrc: time to display RMSE 0.01, radiance cache vs plain path tracing")
     ap.add_argument("--gt-spp", type=int, default=4096, help="nrc / large: ground-truth samples per pixel")
@@ -616,6 +616,42 @@ def run_large(args, rank, world):
     return 0
 
 
+def run_path(args, rank, world):
+    """Plain path-tracing throughput (PATH renders, device time of rc_render):
+    the room (2,012 triangles, 320x240, 16 spp CMJ, depth 4, box filter) and
+    the 5,141,506-triangle heightfield + blobs at 1920x1080, 1 spp, depth 12,
+    sky-lit."""
+    if rank != 0:
+        return 0
+    from raycer_gb300 import scenes
+    from raycer_gb300.tracer import CudaTracer, TracerState
+
+    out = {}
+    cases = (("room_320x240_16spp_depth4", lambda: scenes.room_scene()),
+             ("heightfield_blobs_1080p_1spp_depth12", lambda: scenes.heightfield_blobs_scene()))
+    for name, make in cases:
+        sc = make()
+        with CudaTracer(0) as t:
+            t.initializeBuffers(sc, seed=1)
+            t.initializeImageBuffers(sc.width, sc.height)
+            st = TracerState(scene=sc, filmWidth=sc.width, filmHeight=sc.height, pixelCount=sc.width * sc.height)
+            for _ in range(args.warmup):
+                t.run(st)
+            ms, rays = [], []
+            for _ in range(args.steps):
+                t.run(st)
+                s2 = t.stats()
+                ms.append(s2["last_ms"])
+                rays.append(s2["rays_traced"])
+            out[name] = {"triangles": sc.triangle_count, "ms_per_frame": round(statistics.mean(ms), 3),
+                         "mrays_per_s": round(sum(rays) / (sum(ms) / 1e3) / 1e6, 1),
+                         "rays_per_frame": int(statistics.mean(rays)),
+                         "extend_ms": round(s2["stage_ms"][0], 3)}
+    print(json.dumps({"metric": "Mrays/s", "workload": "path", "unit": "Mrays/s", "higher_is_better": True,
+                      "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "results": out}))
+    return 0
+
+
 def main():
     args = parse_args()
     rank, local_rank, world = dist_env()
@@ -627,6 +663,8 @@ def main():
         return run_build(args, rank, world)
     if args.workload == "large":
         return run_large(args, rank, world)
+    if args.workload == "path":
+        return run_path(args, rank, world)
     if args.impl == "reference":
         return run_reference(args, rank, world)
     return run_ours(args, rank, local_rank, world)
