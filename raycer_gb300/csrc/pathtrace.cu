@@ -40,6 +40,14 @@ namespace
 #ifndef RC_TRACE_MIN_BLOCKS
 #define RC_TRACE_MIN_BLOCKS 10
 #endif
+#ifndef RC_REFILL_MIN
+#define RC_REFILL_MIN 8
+#endif
+// Resident 128-thread blocks per SM the extend kernel is compiled for (its
+// register budget: 65,536 / (128 x this)).
+#ifndef RC_EXTEND_MIN_BLOCKS
+#define RC_EXTEND_MIN_BLOCKS 8
+#endif
 
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
 
@@ -173,8 +181,94 @@ __device__ __forceinline__ DevScene scene_of_slot(const PassParams& p, int s)
     return p.scenes[p.chunks[p.chunkOf[s]].scene].sc;
 }
 
+__device__ __forceinline__ void flush_extend_counts(const PassParams& p, unsigned long long done, const TravCount& cnt,
+                                                    int err)
+{
+    unsigned long long n = cnt.nodes, t = cnt.tris;
+    for (int o = 16; o > 0; o >>= 1)
+    {
+        done += __shfl_down_sync(0xffffffffu, done, o);
+        n += __shfl_down_sync(0xffffffffu, n, o);
+        t += __shfl_down_sync(0xffffffffu, t, o);
+    }
+    if (lane_id() == 0)
+    {
+        atomicAdd(&p.ctl->stats[0], done);
+        atomicAdd(&p.ctl->stats[1], n);
+        atomicAdd(&p.ctl->stats[2], t);
+    }
+    if (err)
+        atomicOr(&p.ctl->error, 1);
+}
+
 template <int ORDER, bool COUNT, int BLOCK>
-__global__ void __launch_bounds__(BLOCK, (RC_TRACE_MIN_BLOCKS * 128) / BLOCK) k_extend(PassParams p, int segment)
+__global__ void __launch_bounds__(BLOCK, (RC_EXTEND_MIN_BLOCKS * 128) / BLOCK) k_extend(PassParams p, int segment)
+{
+    const unsigned total = *reinterpret_cast<volatile unsigned*>(&p.counts[segment * 4 + 0]);
+    const int* __restrict__ queue = (segment & 1) ? p.qb : p.qa;
+    unsigned* head = &p.counts[segment * 4 + 1];
+    TravCount cnt{ 0, 0 };
+    int err = 0;
+    unsigned long long done = 0;
+    // Each lane traces its ray a step at a time; once RC_REFILL_MIN lanes of
+    // the warp are idle (or all are), they take the next queue entries
+    // together, so a warp is not held by its slowest ray (Aila & Laine 2009,
+    // replacing terminated rays). Every ray's traversal is unchanged.
+    int stack[kMaxStack];
+    float sdist[ORDER == ORDER_NEAREST ? kMaxStack : 1];
+    TravState st;
+    int s = -1;
+    bool active = false;
+    bool exhausted = false;  // warp-uniform
+    const unsigned below = (1u << lane_id()) - 1u;
+    while (true)
+    {
+        const unsigned idle = __ballot_sync(0xffffffffu, !active);
+        if (!exhausted && idle != 0u && (__popc(idle) >= RC_REFILL_MIN || idle == 0xffffffffu))
+        {
+            const int leader = __ffs(idle) - 1;
+            unsigned base = 0;
+            if (int(lane_id()) == leader)
+                base = atomicAdd(head, unsigned(__popc(idle)));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (!active)
+            {
+                const unsigned q = base + unsigned(__popc(idle & below));
+                if (q < total)
+                {
+                    s = queue[q];
+                    const DevScene sc = scene_of_slot(p, s);
+                    const float4 o = p.o[s];
+                    const float4 d = p.d[s];
+                    const RayF ray = make_ray(v3(o.x, o.y, o.z), v3(d.x, d.y, d.z), 0.0f, FLT_MAX);
+                    trav_begin(st, sc, ray, __float_as_int(o.w));
+                    active = true;
+                }
+            }
+            if (base + unsigned(__popc(idle)) >= total)
+                exhausted = true;
+        }
+        if (!__any_sync(0xffffffffu, active))
+        {
+            if (exhausted)
+                break;
+            continue;
+        }
+        if (active && trav_step<ORDER, COUNT>(st, stack, sdist, cnt, err))
+        {
+            p.hit[s] = make_int4(st.found ? st.hit.slot : -1, __float_as_int(st.hit.t), __float_as_int(st.hit.u),
+                                 __float_as_int(st.hit.v));
+            done++;
+            active = false;
+        }
+    }
+    flush_extend_counts(p, done, cnt, err);
+}
+
+// Extend for passes with two-level scenes: 32 queue entries per warp fetch,
+// each ray traced in one go.
+template <bool COUNT>
+__global__ void __launch_bounds__(128) k_extend_instanced(PassParams p, int segment)
 {
     const unsigned total = *reinterpret_cast<volatile unsigned*>(&p.counts[segment * 4 + 0]);
     const int* __restrict__ queue = (segment & 1) ? p.qb : p.qa;
@@ -195,32 +289,15 @@ __global__ void __launch_bounds__(BLOCK, (RC_TRACE_MIN_BLOCKS * 128) / BLOCK) k_
             float4 d = p.d[s];
             RayF ray = make_ray(v3(o.x, o.y, o.z), v3(d.x, d.y, d.z), 0.0f, FLT_MAX);
             HitF h{ -1, FLT_MAX, 0.0f, 0.0f, -1 };
-            bool found = traverse_scene<false, ORDER, COUNT>(sc, ray, h, cnt, err, __float_as_int(o.w),
-                                                             __float_as_int(d.w));
+            bool found = traverse_scene<false, ORDER_NEAREST, COUNT>(sc, ray, h, cnt, err, __float_as_int(o.w),
+                                                                     __float_as_int(d.w));
             // w: v, or the instance of a two-level scene's hit (shading uses neither u nor v)
             p.hit[s] = make_int4(found ? h.slot : -1, __float_as_int(h.t), __float_as_int(h.u),
                                  sc.numInstances > 0 ? h.inst : __float_as_int(h.v));
             done++;
         }
     }
-    unsigned long long n = cnt.nodes, t = cnt.tris;
-    for (int o = 16; o > 0; o >>= 1)
-    {
-        done += __shfl_down_sync(0xffffffffu, done, o);
-        n += __shfl_down_sync(0xffffffffu, n, o);
-        t += __shfl_down_sync(0xffffffffu, t, o);
-    }
-    if (lane_id() == 0)
-    {
-        atomicAdd(&p.ctl->stats[0], done);
-        if (COUNT)
-        {
-            atomicAdd(&p.ctl->stats[1], n);
-            atomicAdd(&p.ctl->stats[2], t);
-        }
-    }
-    if (err)
-        atomicOr(&p.ctl->error, 1);
+    flush_extend_counts(p, done, cnt, err);
 }
 
 // Shading frame of a hit: the triangle's normal, tangent and bitangent
@@ -579,6 +656,17 @@ cudaError_t extend_t(const PassParams& p, int segment, int block, cudaStream_t s
     return extend_b<ORDER, COUNT, 128>(p, segment, stream, numSMs);
 }
 
+template <bool COUNT>
+cudaError_t extend_inst(const PassParams& p, int segment, cudaStream_t stream, int numSMs)
+{
+    auto k = k_extend_instanced<COUNT>;
+    static int grid = 0;
+    if (grid == 0)
+        grid = persistent_blocks(k, 128, numSMs);
+    k<<<grid, 128, 0, stream>>>(p, segment);
+    return cudaGetLastError();
+}
+
 template <int BLOCK, bool NRC>
 cudaError_t shade_b(const PassParams& p, int segment, cudaStream_t stream, int numSMs)
 {
@@ -659,7 +747,9 @@ cudaError_t launch_path_segments(const PassParams& p, int order, int counting, c
     {
         if (extendEvents && (e = cudaEventRecord(extendEvents[2 * seg], stream)) != cudaSuccess)
             return e;
-        if (order == ORDER_NEAREST)
+        if (p.instanced)
+            e = counting ? extend_inst<true>(p, seg, stream, numSMs) : extend_inst<false>(p, seg, stream, numSMs);
+        else if (order == ORDER_NEAREST)
             e = counting ? extend_t<ORDER_NEAREST, true>(p, seg, shape.extendBlock, stream, numSMs)
                          : extend_t<ORDER_NEAREST, false>(p, seg, shape.extendBlock, stream, numSMs);
         else

@@ -99,6 +99,7 @@ struct PassParams
     unsigned* counts;  // per segment: [queue count, extend head, shade head, unused]
     DevControl* ctl;
     NrcPass nrc;
+    int instanced;   // 1: the pass has two-level scenes (k_extend_instanced)
 };
 
 // Bytes of path state per slot (o, d, thr, res, hit, two queue entries, chunk id).

@@ -268,6 +268,7 @@ rc_status render_path(rc_tracer* h, uint64_t pixelStart, uint64_t count, const v
     pp.scenes = dScene;
     pp.numChunks = 1;
     pp.segments = g.max_path_length;
+    pp.instanced = h->nInstances > 0 ? 1 : 0;
     PassShape shape;
     const bool nrc = nrc_active(h);
     if (nrc)
