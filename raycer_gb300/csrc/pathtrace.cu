@@ -43,6 +43,10 @@ namespace
 #ifndef RC_REFILL_MIN
 #define RC_REFILL_MIN 8
 #endif
+// Traversal steps a lane takes between two refill checks of its warp.
+#ifndef RC_REFILL_STEPS
+#define RC_REFILL_STEPS 1
+#endif
 // Resident 128-thread blocks per SM the extend kernel is compiled for (its
 // register budget: 65,536 / (128 x this)).
 #ifndef RC_EXTEND_MIN_BLOCKS
@@ -254,12 +258,15 @@ __global__ void __launch_bounds__(BLOCK, (RC_EXTEND_MIN_BLOCKS * 128) / BLOCK) k
                 break;
             continue;
         }
-        if (active && trav_step<ORDER, COUNT>(st, stack, sdist, cnt, err))
+        for (int k = 0; k < RC_REFILL_STEPS && active; ++k)
         {
-            p.hit[s] = make_int4(st.found ? st.hit.slot : -1, __float_as_int(st.hit.t), __float_as_int(st.hit.u),
-                                 __float_as_int(st.hit.v));
-            done++;
-            active = false;
+            if (trav_step<ORDER, COUNT>(st, stack, sdist, cnt, err))
+            {
+                p.hit[s] = make_int4(st.found ? st.hit.slot : -1, __float_as_int(st.hit.t), __float_as_int(st.hit.u),
+                                     __float_as_int(st.hit.v));
+                done++;
+                active = false;
+            }
         }
     }
     flush_extend_counts(p, done, cnt, err);
