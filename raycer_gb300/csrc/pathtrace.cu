@@ -40,17 +40,10 @@ namespace
 #ifndef RC_TRACE_MIN_BLOCKS
 #define RC_TRACE_MIN_BLOCKS 10
 #endif
-#ifndef RC_REFILL_MIN
-#define RC_REFILL_MIN 8
-#endif
-// Traversal steps a lane takes between two refill checks of its warp.
-#ifndef RC_REFILL_STEPS
-#define RC_REFILL_STEPS 1
-#endif
 // Resident 128-thread blocks per SM the extend kernel is compiled for (its
 // register budget: 65,536 / (128 x this)).
 #ifndef RC_EXTEND_MIN_BLOCKS
-#define RC_EXTEND_MIN_BLOCKS 8
+#define RC_EXTEND_MIN_BLOCKS 10
 #endif
 
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
@@ -210,63 +203,26 @@ __global__ void __launch_bounds__(BLOCK, (RC_EXTEND_MIN_BLOCKS * 128) / BLOCK) k
 {
     const unsigned total = *reinterpret_cast<volatile unsigned*>(&p.counts[segment * 4 + 0]);
     const int* __restrict__ queue = (segment & 1) ? p.qb : p.qa;
-    unsigned* head = &p.counts[segment * 4 + 1];
     TravCount cnt{ 0, 0 };
     int err = 0;
     unsigned long long done = 0;
-    // Each lane traces its ray a step at a time; once RC_REFILL_MIN lanes of
-    // the warp are idle (or all are), they take the next queue entries
-    // together, so a warp is not held by its slowest ray (Aila & Laine 2009,
-    // replacing terminated rays). Every ray's traversal is unchanged.
-    int stack[kMaxStack];
-    float sdist[ORDER == ORDER_NEAREST ? kMaxStack : 1];
-    TravState st;
-    int s = -1;
-    bool active = false;
-    bool exhausted = false;  // warp-uniform
-    const unsigned below = (1u << lane_id()) - 1u;
     while (true)
     {
-        const unsigned idle = __ballot_sync(0xffffffffu, !active);
-        if (!exhausted && idle != 0u && (__popc(idle) >= RC_REFILL_MIN || idle == 0xffffffffu))
+        unsigned base = warp_fetch(&p.counts[segment * 4 + 1], 32u);
+        if (base >= total)
+            break;
+        unsigned q = base + lane_id();
+        if (q < total)
         {
-            const int leader = __ffs(idle) - 1;
-            unsigned base = 0;
-            if (int(lane_id()) == leader)
-                base = atomicAdd(head, unsigned(__popc(idle)));
-            base = __shfl_sync(0xffffffffu, base, leader);
-            if (!active)
-            {
-                const unsigned q = base + unsigned(__popc(idle & below));
-                if (q < total)
-                {
-                    s = queue[q];
-                    const DevScene sc = scene_of_slot(p, s);
-                    const float4 o = p.o[s];
-                    const float4 d = p.d[s];
-                    const RayF ray = make_ray(v3(o.x, o.y, o.z), v3(d.x, d.y, d.z), 0.0f, FLT_MAX);
-                    trav_begin(st, sc, ray, __float_as_int(o.w));
-                    active = true;
-                }
-            }
-            if (base + unsigned(__popc(idle)) >= total)
-                exhausted = true;
-        }
-        if (!__any_sync(0xffffffffu, active))
-        {
-            if (exhausted)
-                break;
-            continue;
-        }
-        for (int k = 0; k < RC_REFILL_STEPS && active; ++k)
-        {
-            if (trav_step<ORDER, COUNT>(st, stack, sdist, cnt, err))
-            {
-                p.hit[s] = make_int4(st.found ? st.hit.slot : -1, __float_as_int(st.hit.t), __float_as_int(st.hit.u),
-                                     __float_as_int(st.hit.v));
-                done++;
-                active = false;
-            }
+            int s = queue[q];
+            const DevScene sc = scene_of_slot(p, s);
+            float4 o = p.o[s];
+            float4 d = p.d[s];
+            RayF ray = make_ray(v3(o.x, o.y, o.z), v3(d.x, d.y, d.z), 0.0f, FLT_MAX);
+            HitF h{ -1, FLT_MAX, 0.0f, 0.0f, -1 };
+            bool found = traverse<false, ORDER, COUNT>(sc, ray, h, cnt, err, __float_as_int(o.w));
+            p.hit[s] = make_int4(found ? h.slot : -1, __float_as_int(h.t), __float_as_int(h.u), __float_as_int(h.v));
+            done++;
         }
     }
     flush_extend_counts(p, done, cnt, err);

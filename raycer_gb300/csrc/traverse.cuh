@@ -203,144 +203,6 @@ __device__ __forceinline__ bool traverse(const DevScene& sc, const RayF& ray, Hi
     }
 }
 
-// Resumable closest-hit traversal of a single-level scene: the same node
-// tests, child order, culling, triangle order and acceptance rule as
-// traverse<false, ORDER, COUNT>, one step at a time, so a persistent kernel
-// can give a lane a new ray as soon as its ray is done. A step is one inner
-// node (descending into a child, or falling through to the pops) or one
-// leaf's triangles followed by the pops.
-struct TravState
-{
-    RayF ray;
-    HitF hit;
-    const DevNode* nodes;
-    const DevTri* tris;
-    int cur;
-    int sp;
-    int skip;
-    bool found;
-};
-
-__device__ __forceinline__ void trav_begin(TravState& st, const DevScene& sc, const RayF& ray, int skip)
-{
-    st.ray = ray;
-    st.hit = HitF{ -1, FLT_MAX, 0.0f, 0.0f, -1 };
-    st.nodes = sc.nodes;
-    st.tris = sc.tris;
-    st.cur = sc.rootLink;
-    st.sp = 0;
-    st.skip = skip;
-    st.found = false;
-}
-
-// Returns true when the traversal has ended (err = 1 on a stack overflow).
-template <int ORDER, bool COUNT>
-__device__ __forceinline__ bool trav_step(TravState& st, int* stack, float* sdist, TravCount& cnt, int& err)
-{
-    if (st.cur >= 0)
-    {
-        float4 a, b, c;
-        int4 l;
-        load_node(st.nodes, st.cur, a, b, c, l);
-        if (COUNT)
-            cnt.nodes++;
-        float e0, e1;
-        bool h0, h1;
-        if (st.ray.finite)
-        {
-            h0 = slab_finite(st.ray, a.x, a.y, a.z, a.w, c.x, c.y, e0);
-            h1 = slab_finite(st.ray, b.x, b.y, b.z, b.w, c.z, c.w, e1);
-        }
-        else
-        {
-            h0 = slab(st.ray, a.x, a.y, a.z, a.w, c.x, c.y, e0);
-            h1 = slab(st.ray, b.x, b.y, b.z, b.w, c.z, c.w, e1);
-        }
-        if (ORDER == ORDER_NEAREST)
-        {
-            h0 = h0 && !(e0 > st.hit.t);
-            h1 = h1 && !(e1 > st.hit.t);
-        }
-        if (h0 && h1)
-        {
-            int nearC = l.x, farC = l.y;
-            float farD = e1;
-            if (ORDER == ORDER_NEAREST && e1 < e0)
-            {
-                nearC = l.y;
-                farC = l.x;
-                farD = e0;
-            }
-            if (st.sp >= kMaxStack)
-            {
-                err = 1;
-                return true;
-            }
-            stack[st.sp] = farC;
-            if (ORDER == ORDER_NEAREST)
-                sdist[st.sp] = farD;
-            st.sp++;
-            st.cur = nearC;
-            return false;
-        }
-        if (h0)
-        {
-            st.cur = l.x;
-            return false;
-        }
-        if (h1)
-        {
-            st.cur = l.y;
-            return false;
-        }
-    }
-    else
-    {
-        const int leaf = ~st.cur;
-        const int start = leaf >> kLeafCountBits;
-        const int count = leaf & ((1 << kLeafCountBits) - 1);
-        for (int i = 0; i < count; ++i)
-        {
-            const int slot = start + i;
-            if (slot == st.skip)
-                continue;
-            const float4* tp = reinterpret_cast<const float4*>(st.tris + slot);
-            const float4 ta = __ldg(tp + 0);
-            const float4 tb = __ldg(tp + 1);
-            const float4 tc = __ldg(tp + 2);
-            if (COUNT)
-                cnt.tris++;
-            float t, u, v;
-            if (tri_hit(st.ray, v3(ta.x, ta.y, ta.z), v3(ta.w, tb.x, tb.y), v3(tb.z, tb.w, tc.x), t, u, v))
-            {
-                bool take;
-                if (ORDER == ORDER_REF)
-                    take = !(t > st.hit.t);
-                else
-                    take = t < st.hit.t || (t == st.hit.t && slot > st.hit.slot);
-                if (take)
-                {
-                    st.hit.slot = slot;
-                    st.hit.t = t;
-                    st.hit.u = u;
-                    st.hit.v = v;
-                    st.found = true;
-                }
-            }
-        }
-    }
-    while (true)
-    {
-        if (st.sp == 0)
-            return true;
-        st.sp--;
-        st.cur = stack[st.sp];
-        if (ORDER == ORDER_NEAREST && sdist[st.sp] > st.hit.t)
-            continue;
-        return false;
-    }
-}
-
 // Ray in an instance's object space: o' = A o + b, d' = A d. d' is not
 // renormalised, so a hit's parameter t is the same in both spaces and the
 // levels share one closest distance. (The reference's Instance normalises
