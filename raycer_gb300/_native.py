@@ -115,7 +115,8 @@ class rc_nrc_config(C.Structure):
     _fields_ = [("enabled", C.c_int32), ("terminate_segment", C.c_int32), ("train_stride", C.c_int32),
                 ("train_steps", C.c_int32), ("train_batch", C.c_int32), ("min_suffix", C.c_int32),
                 ("learning_rate", C.c_float), ("beta1", C.c_float), ("beta2", C.c_float), ("epsilon", C.c_float),
-                ("box_min", C.c_float * 3), ("box_max", C.c_float * 3), ("seed", C.c_uint64)]
+                ("box_min", C.c_float * 3), ("box_max", C.c_float * 3), ("seed", C.c_uint64),
+                ("lookup_kernel", C.c_int32), ("reserved", C.c_int32)]
 
 
 class rc_nrc_stats(C.Structure):
@@ -140,6 +141,8 @@ class rc_scene_file_info(C.Structure):
 RC_GENERAL_SKY = 1
 RC_BUILDER_REFERENCE_SAH = 0
 RC_BUILDER_GPU_LBVH = 1
+RC_NRC_MMA_SYNC = 0
+RC_NRC_TCGEN05 = 1
 RC_NRC_PARAMS = 20992
 RC_NRC_QUERY_FLOATS = 12
 RC_NRC_INPUTS = 128

@@ -295,7 +295,10 @@ rc_status nrc_lookups(rc_tracer* h, const PassParams& pp)
     ip.thr = pp.thr;
     ip.res = pp.res;
     NRC_STATUS(encoding_box(h, ip.box));
-    NRC_TRY(h, launch_nrc_infer(ip, pp.nslots, h->stream, h->numSMs), "launch cache lookups");
+    if (n.cfg.lookup_kernel == RC_NRC_TCGEN05)
+        NRC_TRY(h, launch_nrc_infer_tc(ip, pp.nslots, &pp.ctl->error, h->stream, h->numSMs), "launch cache lookups");
+    else
+        NRC_TRY(h, launch_nrc_infer(ip, pp.nslots, h->stream, h->numSMs), "launch cache lookups");
     return RC_OK;
 }
 
@@ -375,6 +378,8 @@ rc_status rc_nrc_configure(rc_tracer* h, const rc_nrc_config* c)
     if (!(c->learning_rate > 0.0f) || !(c->beta1 >= 0.0f && c->beta1 < 1.0f) || !(c->beta2 >= 0.0f && c->beta2 < 1.0f) ||
         !(c->epsilon > 0.0f))
         return fail(h, RC_INVALID_ARG, "nrc_configure: invalid optimizer settings");
+    if ((c->lookup_kernel != RC_NRC_MMA_SYNC && c->lookup_kernel != RC_NRC_TCGEN05) || c->reserved != 0)
+        return fail(h, RC_INVALID_ARG, "nrc_configure: unknown lookup kernel / reserved not 0");
     cudaSetDevice(h->device);
     h->nrc.cfg = *c;
     NRC_STATUS(alloc_state(h));
@@ -441,10 +446,22 @@ rc_status rc_nrc_infer(rc_tracer* h, const float* queries, int64_t n, float* rgb
     ip.count = st.dCounters + 2;
     ip.out = static_cast<float*>(st.dApiOut);
     NRC_STATUS(encoding_box(h, ip.box));
-    NRC_TRY(h, launch_nrc_infer(ip, int(n), h->stream, h->numSMs), "launch inference");
+    int errWord = 0;
+    if (st.cfg.lookup_kernel == RC_NRC_TCGEN05)
+    {
+        NRC_TRY(h, cudaMemsetAsync(st.dCounters + 3, 0, sizeof(unsigned), h->stream), "reset error word");
+        NRC_TRY(h, launch_nrc_infer_tc(ip, int(n), reinterpret_cast<int*>(st.dCounters + 3), h->stream, h->numSMs),
+                "launch inference");
+        NRC_TRY(h, cudaMemcpyAsync(&errWord, st.dCounters + 3, sizeof(int), cudaMemcpyDeviceToHost, h->stream),
+                "read error word");
+    }
+    else
+        NRC_TRY(h, launch_nrc_infer(ip, int(n), h->stream, h->numSMs), "launch inference");
     NRC_TRY(h, cudaMemcpyAsync(rgb, st.dApiOut, size_t(n) * 3 * 4, cudaMemcpyDeviceToHost, h->stream),
             "download outputs");
     NRC_TRY(h, cudaStreamSynchronize(h->stream), "inference");
+    if (errWord & kNrcTcTimeout)
+        return fail(h, RC_DEVICE_ERROR, "nrc_infer: a tensor-core wait timed out");
     return RC_OK;
 }
 

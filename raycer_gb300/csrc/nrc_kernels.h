@@ -75,9 +75,15 @@ struct NrcAdamParams
     __nv_bfloat16* weights;
 };
 
+// Error-word bit set by the tcgen05 kernel when an mbarrier wait ran out.
+constexpr int kNrcTcTimeout = 2;
+
 size_t nrc_train_smem();
 int nrc_train_blocks(int numSMs);
 cudaError_t launch_nrc_infer(const NrcInferParams& p, int maxRecords, cudaStream_t stream, int numSMs);
+// The same lookups with tcgen05.mma / TMEM (nrc_tc.cu), 128 queries per tile.
+cudaError_t launch_nrc_infer_tc(const NrcInferParams& p, int maxRecords, int* errorWord, cudaStream_t stream,
+                                int numSMs);
 cudaError_t launch_nrc_train(const NrcTrainParams& p, int blocks, cudaStream_t stream);
 cudaError_t launch_nrc_adam(const NrcAdamParams& p, cudaStream_t stream);
 // BF16 input features of n records ([n][128]), for tests of the encoding.

@@ -347,6 +347,8 @@ rc_status render_path(rc_tracer* h, uint64_t pixelStart, uint64_t count, const v
     h->frameIndex++;
     if (ctl.error & 1)
         return fail(h, RC_DEVICE_ERROR, "path tracing: traversal stack overflow");
+    if (ctl.error & kNrcTcTimeout)
+        return fail(h, RC_DEVICE_ERROR, "path tracing: a radiance-cache tensor-core wait timed out");
     return RC_OK;
 }
 
