@@ -114,10 +114,11 @@ def main(argv=None) -> int:
     ap.add_argument("--scale", type=float, default=0.5, help="film scale (1 = 1920x1080)")
     ap.add_argument("--frames", type=int, default=4)
     ap.add_argument("--instances", type=int, default=200)
+    ap.add_argument("--lookup-kernel", type=int, default=0, help="0: mma.sync, 1: tcgen05 with TMEM")
     args = ap.parse_args(argv)
     w, h = int(round(1920 * args.scale)), int(round(1080 * args.scale))
     sc = scenes.heightfield_blobs_scene(instances=args.instances, width=w, height=h)
-    print(json.dumps(render_frames(sc, args.frames)))
+    print(json.dumps(render_frames(sc, args.frames, cache_config=dict(lookup_kernel=args.lookup_kernel))))
     sys.stdout.flush()
     return 0
 
