@@ -81,10 +81,10 @@ __device__ __forceinline__ void encode_fragments(const float* q0, const float* q
     {
         int c0 = 16 * t + tig * 2;
         int c1 = c0 + 8;
-        A[t][0] = pack_bf16(nrc_feature(c0, q0, box), nrc_feature(c0 + 1, q0, box));
-        A[t][1] = pack_bf16(nrc_feature(c0, q1, box), nrc_feature(c0 + 1, q1, box));
-        A[t][2] = pack_bf16(nrc_feature(c1, q0, box), nrc_feature(c1 + 1, q0, box));
-        A[t][3] = pack_bf16(nrc_feature(c1, q1, box), nrc_feature(c1 + 1, q1, box));
+        A[t][0] = nrc_feature_bf16x2(c0, q0, box);
+        A[t][1] = nrc_feature_bf16x2(c0, q1, box);
+        A[t][2] = nrc_feature_bf16x2(c1, q0, box);
+        A[t][3] = nrc_feature_bf16x2(c1, q1, box);
     }
 }
 
