@@ -536,8 +536,8 @@ typedef struct rc_nrc_config
     float box_min[3];           /* position-encoding box; box_max <= box_min on any */
     float box_max[3];           /*   axis = the scene's bounds at render time        */
     uint64_t seed;              /* weight initialisation and training-slot choice    */
-    int32_t lookup_kernel;      /* RC_NRC_MMA_SYNC (warp-level mma.sync, default) or */
-                                /* RC_NRC_TCGEN05 (tcgen05.mma, TMEM accumulators)   */
+    int32_t lookup_kernel;      /* RC_NRC_TCGEN05 (tcgen05.mma, TMEM accumulators;   */
+                                /* default) or RC_NRC_MMA_SYNC (warp-level mma.sync) */
     int32_t reserved;           /* 0                                                 */
 } rc_nrc_config;
 

@@ -363,6 +363,7 @@ rc_status rc_nrc_defaults(rc_nrc_config* c)
     c->beta2 = 0.99f;
     c->epsilon = 1e-8f;
     c->seed = 1;
+    c->lookup_kernel = RC_NRC_TCGEN05;
     return RC_OK;
 }
 

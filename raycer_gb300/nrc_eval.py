@@ -114,7 +114,7 @@ def main(argv=None) -> int:
     ap.add_argument("--scale", type=float, default=0.5, help="film scale (1 = 1920x1080)")
     ap.add_argument("--frames", type=int, default=4)
     ap.add_argument("--instances", type=int, default=200)
-    ap.add_argument("--lookup-kernel", type=int, default=0, help="0: mma.sync, 1: tcgen05 with TMEM")
+    ap.add_argument("--lookup-kernel", type=int, default=1, help="0: mma.sync, 1: tcgen05 with TMEM")
     args = ap.parse_args(argv)
     w, h = int(round(1920 * args.scale)), int(round(1080 * args.scale))
     sc = scenes.heightfield_blobs_scene(instances=args.instances, width=w, height=h)
