@@ -10,6 +10,8 @@
 #include <cfloat>
 
 #include "kernels.h"
+#include <cstdlib>
+
 #include "traverse.cuh"
 
 namespace rcx
@@ -27,6 +29,7 @@ constexpr int kBlock = 128;
 #ifndef RC_TRACE_TILES
 #define RC_TRACE_TILES 1
 #endif
+constexpr int kWarpsPerBlock = kBlock / 32;
 
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
 
@@ -116,16 +119,20 @@ __device__ __forceinline__ RayF primary_ray(const DevCamera& cam, const rc_ray* 
 }
 
 // Stage 1 of the RAY frame: closest hit of every pixel's primary ray.
-// Whole frames from the camera (tilesX > 0) are walked in 8x4-pixel tiles, one
-// tile per warp fetch, so a warp's rays are spatially coherent; pixel ranges
-// and caller rays are walked in order.
-template <int ORDER, bool COUNT>
+// Whole frames (tilesX > 0: camera rays, or caller rays one per pixel) are
+// walked in 8x4-pixel tiles, one tile per warp fetch, so a warp's rays are
+// spatially coherent; pixel ranges are walked in order.
+// PACKET: the warp traverses its 32 rays together (traverse_packet); the
+// counted frame keeps one traversal per lane, whose node and triangle counts
+// are the algorithm's.
+template <int ORDER, bool COUNT, bool PACKET>
 __global__ void __launch_bounds__(kBlock, RC_TRACE_MIN_BLOCKS) k_raycast_primary(DevScene sc, DevCamera cam, const rc_ray* __restrict__ rays,
                                                             uint64_t pixelStart, int64_t count, int64_t width,
                                                             int64_t height, int64_t tilesX, int castShadow,
                                                             rc_cast_pixel* __restrict__ out, int* __restrict__ queue,
                                                             DevControl* ctl)
 {
+    __shared__ PacketEntry wstack[PACKET ? kWarpsPerBlock : 1][PACKET ? kMaxStack : 1];
     TravCount cnt{ 0, 0 };
     int err = 0;
     unsigned long long done = 0;
@@ -147,7 +154,26 @@ __global__ void __launch_bounds__(kBlock, RC_TRACE_MIN_BLOCKS) k_raycast_primary
         }
         bool hitAny = false;
         int hitSlot = -1;
-        if (valid)
+        if (PACKET)
+        {
+            // all lanes together, the ray of an invalid lane unused
+            RayF ray = primary_ray(cam, rays, valid ? pixelStart + uint64_t(i) : pixelStart, valid ? i : 0, width);
+            HitF h{ -1, FLT_MAX, 0.0f, 0.0f, -1 };
+            bool found = traverse_packet<ORDER>(sc, ray, h, err, -1, valid, wstack[threadIdx.x >> 5]);
+            if (valid)
+            {
+                int4 o;
+                o.x = found ? caller_index(sc, h.slot) : -1;
+                o.y = __float_as_int(found ? h.t : -1.0f);
+                o.z = -1;
+                o.w = found ? 1 : 0;
+                reinterpret_cast<int4*>(out)[i] = o;
+                hitAny = found && castShadow;
+                hitSlot = h.slot;
+                done++;
+            }
+        }
+        else if (valid)
         {
             RayF ray = primary_ray(cam, rays, pixelStart + uint64_t(i), i, width);
             HitF h{ -1, FLT_MAX, 0.0f, 0.0f, -1 };
@@ -239,23 +265,47 @@ cudaError_t cast_t(const LaunchInfo& li, const DevScene& sc, const rc_ray* rays,
     return cudaGetLastError();
 }
 
-template <int ORDER, bool COUNT>
+// Warp-wide traversal of the primary rays of uncounted RAY frames walked in
+// pixel tiles: RC_TRACE_PACKETS = 2 (default) for camera frames and caller
+// ray frames, 1 for camera frames only, 0 never (read once). On the 1080p
+// heightfield the primary rays of an 8x4-pixel tile take 0.302 ms this way
+// against 0.327 ms per lane, and the caller-ray frame through host memory
+// gains 3 %. A caller frame whose neighbouring rays are not coherent would
+// lose instead (mode 1). Shadow rays stay per lane: each stops at its first
+// occluder, and the warp-wide walk of the union of their paths measured 1.8x
+// slower (0.306 vs 0.172 ms).
+int trace_packets()
+{
+    static const int mode = [] {
+        const char* v = std::getenv("RC_TRACE_PACKETS");
+        return v && v[0] >= '0' && v[0] <= '2' ? int(v[0] - '0') : 2;
+    }();
+    return mode;
+}
+
+// A whole image of at least one 8x4 tile (pixel ranges, and ray lists passed
+// as one row, are walked in order).
+bool whole_frame(uint64_t pixelStart, int64_t count, int64_t width)
+{
+    return RC_TRACE_TILES && pixelStart == 0 && width >= 8 && count / width >= 4 && (count / width) * width == count;
+}
+
+template <int ORDER, bool COUNT, bool PACKET>
 cudaError_t raycast_t(const LaunchInfo& li, const DevScene& sc, const DevCamera& cam, const rc_ray* rays,
                       uint64_t pixelStart, int64_t count, int64_t width, int castShadow, float3 L, float off,
                       rc_cast_pixel* out, int* queue, DevControl* ctl, cudaEvent_t between)
 {
-    auto kp = k_raycast_primary<ORDER, COUNT>;
+    auto kp = k_raycast_primary<ORDER, COUNT, PACKET>;
     auto ks = k_raycast_shadow<COUNT>;
     static int gp = 0, gs = 0;
     if (gp == 0)
         gp = persistent_blocks(kp, li.numSMs);
     if (gs == 0)
         gs = persistent_blocks(ks, li.numSMs);
-    // Tile a whole camera frame (pixel range = the full image).
-    int64_t height = width > 0 ? count / width : 0;
-    int64_t tilesX = (RC_TRACE_TILES && !rays && pixelStart == 0 && width > 0 && height * width == count)
-                         ? (width + 7) / 8
-                         : 0;
+    // Tile a whole frame (pixel range = the full image; camera rays or one
+    // caller ray per pixel): only the order the warps take the pixels in.
+    const int64_t height = width > 0 ? count / width : 0;
+    const int64_t tilesX = whole_frame(pixelStart, count, width) ? (width + 7) / 8 : 0;
     kp<<<gp, kBlock, 0, li.stream>>>(sc, cam, rays, pixelStart, count, width, height, tilesX, castShadow, out, queue,
                                      ctl);
     cudaError_t e = cudaGetLastError();
@@ -291,15 +341,18 @@ cudaError_t launch_raycast(const LaunchInfo& li, const DevScene& sc, const DevCa
 {
     if (count <= 0)
         return cudaSuccess;
-    if (order == ORDER_NEAREST)
-        return li.counting ? raycast_t<ORDER_NEAREST, true>(li, sc, cam, rays, pixelStart, count, width, castShadow,
-                                                            dirToLight, rayStartOffset, out, shadowQueue, ctl, between)
-                           : raycast_t<ORDER_NEAREST, false>(li, sc, cam, rays, pixelStart, count, width, castShadow,
-                                                             dirToLight, rayStartOffset, out, shadowQueue, ctl, between);
-    return li.counting ? raycast_t<ORDER_REF, true>(li, sc, cam, rays, pixelStart, count, width, castShadow,
-                                                    dirToLight, rayStartOffset, out, shadowQueue, ctl, between)
-                       : raycast_t<ORDER_REF, false>(li, sc, cam, rays, pixelStart, count, width, castShadow,
-                                                     dirToLight, rayStartOffset, out, shadowQueue, ctl, between);
+#define RC_RAYCAST_ARGS li, sc, cam, rays, pixelStart, count, width, castShadow, dirToLight, rayStartOffset, out, \
+                        shadowQueue, ctl, between
+    if (li.counting)
+        return order == ORDER_NEAREST ? raycast_t<ORDER_NEAREST, true, false>(RC_RAYCAST_ARGS)
+                                      : raycast_t<ORDER_REF, true, false>(RC_RAYCAST_ARGS);
+    const int packets = trace_packets();
+    if (whole_frame(pixelStart, count, width) && (packets == 2 || (packets == 1 && !rays)))
+        return order == ORDER_NEAREST ? raycast_t<ORDER_NEAREST, false, true>(RC_RAYCAST_ARGS)
+                                      : raycast_t<ORDER_REF, false, true>(RC_RAYCAST_ARGS);
+    return order == ORDER_NEAREST ? raycast_t<ORDER_NEAREST, false, false>(RC_RAYCAST_ARGS)
+                                  : raycast_t<ORDER_REF, false, false>(RC_RAYCAST_ARGS);
+#undef RC_RAYCAST_ARGS
 }
 
 }  // namespace rcx

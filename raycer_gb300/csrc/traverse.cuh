@@ -203,6 +203,162 @@ __device__ __forceinline__ bool traverse(const DevScene& sc, const RayF& ray, Hi
     }
 }
 
+// One stack entry of the warp-wide traversal: a node link and the lanes
+// whose rays take part in its subtree.
+struct PacketEntry
+{
+    int link;
+    unsigned lanes;
+};
+
+// Warp-wide (masked packet) closest-hit traversal: the 32 lanes of a warp,
+// one ray each, walk one shared node sequence, so every node and triangle
+// record is one broadcast load and the control flow stays converged. Must be
+// called by all 32 lanes together; `active` marks the lanes with a ray;
+// `wstack` is this warp's kMaxStack-entry stack in shared memory. Each lane
+// makes the tests its own traverse() call would make, in the same order:
+//   ORDER_REF      the shared sequence is the tree's preorder restricted to
+//                  the boxes some lane hits (left subtree first); a lane takes
+//                  part only in the subtrees whose box its ray hits, so it
+//                  meets its triangles in its per-ray order and gets the same
+//                  closest hit (ties to the later triangle).
+//   ORDER_NEAREST  the warp descends first into the child that most of its
+//                  lanes find nearer; each lane culls boxes whose entry
+//                  distance lies beyond its own current hit. The accepted hit
+//                  (minimum t, ties to the larger slot) does not depend on
+//                  the order.
+// It pays for coherent rays (the primary rays of a pixel tile); any-hit
+// shadow rays, which stop at different depths, ran slower this way than one
+// traversal per lane. Node and triangle counts are not kept: counted frames
+// use traverse().
+template <int ORDER>
+__device__ __forceinline__ bool traverse_packet(const DevScene& sc, const RayF& ray, HitF& hit, int& err, int skip,
+                                                bool active, PacketEntry* __restrict__ wstack)
+{
+    constexpr bool CULL = ORDER == ORDER_NEAREST;
+    constexpr unsigned kAll = 0xffffffffu;
+    float sdist[CULL ? kMaxStack : 1];  // this lane's entry distance of each stacked box
+    const unsigned bit = 1u << (threadIdx.x & 31u);
+    bool found = false;
+    int sp = 0;
+    int cur = sc.rootLink;
+    unsigned curMask = __ballot_sync(kAll, active);
+    if (curMask == 0)
+        return false;
+
+    while (true)
+    {
+        if (cur >= 0)
+        {
+            float4 a, b, c;
+            int4 l;
+            load_node(sc.nodes, cur, a, b, c, l);
+            float e0 = 0.0f, e1 = 0.0f;
+            bool h0 = false, h1 = false;
+            if (curMask & bit)
+            {
+                if (ray.finite)
+                {
+                    h0 = slab_finite(ray, a.x, a.y, a.z, a.w, c.x, c.y, e0);
+                    h1 = slab_finite(ray, b.x, b.y, b.z, b.w, c.z, c.w, e1);
+                }
+                else
+                {
+                    h0 = slab(ray, a.x, a.y, a.z, a.w, c.x, c.y, e0);
+                    h1 = slab(ray, b.x, b.y, b.z, b.w, c.z, c.w, e1);
+                }
+                if (CULL)
+                {
+                    h0 = h0 && !(e0 > hit.t);
+                    h1 = h1 && !(e1 > hit.t);
+                }
+            }
+            const unsigned m0 = __ballot_sync(kAll, h0);
+            const unsigned m1 = __ballot_sync(kAll, h1);
+            if (m0 && m1)
+            {
+                bool rightFirst = false;
+                if (CULL)
+                {
+                    const unsigned vote = __ballot_sync(kAll, h0 && h1 && e1 < e0);
+                    rightFirst = 2 * __popc(vote) > __popc(m0 & m1);
+                }
+                if (sp >= kMaxStack)
+                {
+                    err = 1;
+                    return found;
+                }
+                __syncwarp();  // every lane has read the entry this push may replace
+                if ((threadIdx.x & 31u) == 0)
+                    wstack[sp] = PacketEntry{ rightFirst ? l.x : l.y, rightFirst ? m0 : m1 };
+                if (CULL)
+                    sdist[sp] = rightFirst ? e0 : e1;
+                sp++;
+                cur = rightFirst ? l.y : l.x;
+                curMask = rightFirst ? m1 : m0;
+                continue;
+            }
+            if (m0 | m1)
+            {
+                cur = m0 ? l.x : l.y;
+                curMask = m0 | m1;
+                continue;
+            }
+        }
+        else
+        {
+            const int leaf = ~cur;
+            const int start = leaf >> kLeafCountBits;
+            const int count = leaf & ((1 << kLeafCountBits) - 1);
+            const bool in = (curMask & bit) != 0;
+            for (int i = 0; i < count; ++i)
+            {
+                const int slot = start + i;
+                const float4* tp = reinterpret_cast<const float4*>(sc.tris + slot);
+                const float4 ta = __ldg(tp + 0);
+                const float4 tb = __ldg(tp + 1);
+                const float4 tc = __ldg(tp + 2);
+                if (!in || slot == skip)
+                    continue;
+                float t, u, v;
+                if (tri_hit(ray, v3(ta.x, ta.y, ta.z), v3(ta.w, tb.x, tb.y), v3(tb.z, tb.w, tc.x), t, u, v))
+                {
+                    bool take;
+                    if (ORDER == ORDER_REF)
+                        take = !(t > hit.t);
+                    else
+                        take = t < hit.t || (t == hit.t && slot > hit.slot);
+                    if (take)
+                    {
+                        hit.slot = slot;
+                        hit.t = t;
+                        hit.u = u;
+                        hit.v = v;
+                        found = true;
+                    }
+                }
+            }
+        }
+
+        // pop the next subtree some lane still takes part in
+        while (true)
+        {
+            if (sp == 0)
+                return found;
+            sp--;
+            __syncwarp();
+            const PacketEntry e = wstack[sp];
+            bool in = (e.lanes & bit) != 0;
+            if (CULL && in && sdist[sp] > hit.t)
+                in = false;
+            curMask = __ballot_sync(kAll, in);
+            cur = e.link;
+            if (curMask)
+                break;
+        }
+    }
+}
+
 // Ray in an instance's object space: o' = A o + b, d' = A d. d' is not
 // renormalised, so a hit's parameter t is the same in both spaces and the
 // levels share one closest distance. (The reference's Instance normalises
