@@ -444,8 +444,10 @@ rc_status rc_sync(rc_tracer* h);
 /* the mesh's box centre; a BVH over the instances' world boxes finds them. */
 /* Geometry that is not instanced is a mesh with an identity instance.     */
 /* Traced by rc_cast / rc_cast_device (hit prim = the flattened index:     */
-/* the triangles of instance 0, then of instance 1, ...) and PATH renders; */
-/* the RAY frame kernels and scene files take single-level scenes only.    */
+/* the triangles of instance 0, then of instance 1, ...), RAY frames and   */
+/* rc_cast_with_shadow (prim and occluder flattened the same way) and PATH */
+/* renders; scene files, rc_get_bvh and the allocation-free entry point    */
+/* take single-level scenes only.                                          */
 
 typedef struct rc_mesh
 {

@@ -124,8 +124,11 @@ __device__ __forceinline__ RayF primary_ray(const DevCamera& cam, const rc_ray* 
 // spatially coherent; pixel ranges are walked in order.
 // PACKET: the warp traverses its 32 rays together (traverse_packet); the
 // counted frame keeps one traversal per lane, whose node and triangle counts
-// are the algorithm's.
-template <int ORDER, bool COUNT, bool PACKET>
+// are the algorithm's. INST: a two-level scene (traverse_instanced; the
+// record's prim is the flattened index, instance's first + mesh-local, and
+// while a shadow ray is to follow its occluder field holds the hit's
+// instance, for the shadow ray to skip the hit triangle of that instance).
+template <int ORDER, bool COUNT, bool PACKET, bool INST>
 __global__ void __launch_bounds__(kBlock, RC_TRACE_MIN_BLOCKS) k_raycast_primary(DevScene sc, DevCamera cam, const rc_ray* __restrict__ rays,
                                                             uint64_t pixelStart, int64_t count, int64_t width,
                                                             int64_t height, int64_t tilesX, int castShadow,
@@ -177,11 +180,15 @@ __global__ void __launch_bounds__(kBlock, RC_TRACE_MIN_BLOCKS) k_raycast_primary
         {
             RayF ray = primary_ray(cam, rays, pixelStart + uint64_t(i), i, width);
             HitF h{ -1, FLT_MAX, 0.0f, 0.0f, -1 };
-            bool found = traverse<false, ORDER, COUNT>(sc, ray, h, cnt, err);
+            bool found;
+            if (INST)
+                found = traverse_instanced<false, COUNT>(sc, ray, h, cnt, err, -1, -1);
+            else
+                found = traverse<false, ORDER, COUNT>(sc, ray, h, cnt, err);
             int4 o;
-            o.x = found ? caller_index(sc, h.slot) : -1;
+            o.x = found ? caller_index(sc, h.slot) + (INST ? __ldg(&sc.instances[h.inst].primBase) : 0) : -1;
             o.y = __float_as_int(found ? h.t : -1.0f);
-            o.z = -1;
+            o.z = INST && found && castShadow ? h.inst : -1;
             o.w = found ? 1 : 0;
             reinterpret_cast<int4*>(out)[i] = o;
             hitAny = found && castShadow;
@@ -208,7 +215,7 @@ __global__ void __launch_bounds__(kBlock, RC_TRACE_MIN_BLOCKS) k_raycast_primary
 // (Raytracer::calculateShadowAmount, Raytracer.cpp:497-522 /
 // lighting.cl:28-48): origin = hit position + dirToLight * rayStartOffset;
 // the primary hit's own triangle is skipped (see traverse.cuh).
-template <bool COUNT>
+template <bool COUNT, bool INST>
 __global__ void __launch_bounds__(kBlock, RC_TRACE_MIN_BLOCKS) k_raycast_shadow(DevScene sc, DevCamera cam, const rc_ray* __restrict__ rays,
                                                            uint64_t pixelStart, int64_t width, float3 L,
                                                            float rayStartOffset, rc_cast_pixel* __restrict__ out,
@@ -235,8 +242,15 @@ __global__ void __launch_bounds__(kBlock, RC_TRACE_MIN_BLOCKS) k_raycast_shadow(
             V3 dl = v3(L.x, L.y, L.z);
             RayF sr = make_ray(vfma(dl, rayStartOffset, ip), dl, 0.0f, FLT_MAX);
             HitF h{ -1, FLT_MAX, 0.0f, 0.0f, -1 };
-            bool occ = traverse<true, ORDER_REF, COUNT>(sc, sr, h, cnt, err, e.y);
-            out[i].occluder = occ ? caller_index(sc, h.slot) : -1;
+            bool occ;
+            if (INST)
+            {
+                // the primary stage left the hit's instance in the occluder field
+                occ = traverse_instanced<true, COUNT>(sc, sr, h, cnt, err, e.y, out[i].occluder);
+            }
+            else
+                occ = traverse<true, ORDER_REF, COUNT>(sc, sr, h, cnt, err, e.y);
+            out[i].occluder = occ ? caller_index(sc, h.slot) + (INST ? __ldg(&sc.instances[h.inst].primBase) : 0) : -1;
             out[i].flags = 1 | 2 | (occ ? 4 : 0);
             done++;
         }
@@ -290,13 +304,13 @@ bool whole_frame(uint64_t pixelStart, int64_t count, int64_t width)
     return RC_TRACE_TILES && pixelStart == 0 && width >= 8 && count / width >= 4 && (count / width) * width == count;
 }
 
-template <int ORDER, bool COUNT, bool PACKET>
+template <int ORDER, bool COUNT, bool PACKET, bool INST>
 cudaError_t raycast_t(const LaunchInfo& li, const DevScene& sc, const DevCamera& cam, const rc_ray* rays,
                       uint64_t pixelStart, int64_t count, int64_t width, int castShadow, float3 L, float off,
                       rc_cast_pixel* out, int* queue, DevControl* ctl, cudaEvent_t between)
 {
-    auto kp = k_raycast_primary<ORDER, COUNT, PACKET>;
-    auto ks = k_raycast_shadow<COUNT>;
+    auto kp = k_raycast_primary<ORDER, COUNT, PACKET, INST>;
+    auto ks = k_raycast_shadow<COUNT, INST>;
     static int gp = 0, gs = 0;
     if (gp == 0)
         gp = persistent_blocks(kp, li.numSMs);
@@ -343,15 +357,19 @@ cudaError_t launch_raycast(const LaunchInfo& li, const DevScene& sc, const DevCa
         return cudaSuccess;
 #define RC_RAYCAST_ARGS li, sc, cam, rays, pixelStart, count, width, castShadow, dirToLight, rayStartOffset, out, \
                         shadowQueue, ctl, between
+    // two-level scenes: the top level nearest-first, like rc_cast's
+    if (sc.numInstances > 0)
+        return li.counting ? raycast_t<ORDER_NEAREST, true, false, true>(RC_RAYCAST_ARGS)
+                           : raycast_t<ORDER_NEAREST, false, false, true>(RC_RAYCAST_ARGS);
     if (li.counting)
-        return order == ORDER_NEAREST ? raycast_t<ORDER_NEAREST, true, false>(RC_RAYCAST_ARGS)
-                                      : raycast_t<ORDER_REF, true, false>(RC_RAYCAST_ARGS);
+        return order == ORDER_NEAREST ? raycast_t<ORDER_NEAREST, true, false, false>(RC_RAYCAST_ARGS)
+                                      : raycast_t<ORDER_REF, true, false, false>(RC_RAYCAST_ARGS);
     const int packets = trace_packets();
     if (whole_frame(pixelStart, count, width) && (packets == 2 || (packets == 1 && !rays)))
-        return order == ORDER_NEAREST ? raycast_t<ORDER_NEAREST, false, true>(RC_RAYCAST_ARGS)
-                                      : raycast_t<ORDER_REF, false, true>(RC_RAYCAST_ARGS);
-    return order == ORDER_NEAREST ? raycast_t<ORDER_NEAREST, false, false>(RC_RAYCAST_ARGS)
-                                  : raycast_t<ORDER_REF, false, false>(RC_RAYCAST_ARGS);
+        return order == ORDER_NEAREST ? raycast_t<ORDER_NEAREST, false, true, false>(RC_RAYCAST_ARGS)
+                                      : raycast_t<ORDER_REF, false, true, false>(RC_RAYCAST_ARGS);
+    return order == ORDER_NEAREST ? raycast_t<ORDER_NEAREST, false, false, false>(RC_RAYCAST_ARGS)
+                                  : raycast_t<ORDER_REF, false, false, false>(RC_RAYCAST_ARGS);
 #undef RC_RAYCAST_ARGS
 }
 

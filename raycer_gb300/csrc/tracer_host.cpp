@@ -1061,8 +1061,6 @@ rc_status rc_cast_with_shadow(rc_tracer* h, const rc_ray* rays, int64_t n, int32
         return fail(h, RC_INVALID_ARG, "cast_with_shadow: bad ray count or null buffer");
     if (order != RC_ORDER_REFERENCE && order != RC_ORDER_NEAREST)
         return fail(h, RC_INVALID_ARG, "cast_with_shadow: invalid traversal order");
-    if (h->nInstances > 0)
-        return fail(h, RC_UNSUPPORTED, "cast_with_shadow: instanced scenes are traced by rc_cast and PATH renders");
     cudaSetDevice(h->device);
     rc_status s;
     // In place when the device can reach both host buffers (16-byte aligned):
@@ -1235,9 +1233,6 @@ namespace rcx
 rc_status raycast_into(rc_tracer* h, const rc_ray* dRays, uint64_t pixelStart, uint64_t count, int order,
                        rc_cast_pixel* dOut, int* dQueue)
 {
-    if (h->nInstances > 0)
-        return fail(h, RC_UNSUPPORTED, "the RAY tracer's primary + shadow kernels trace single-level scenes; "
-                                       "instanced scenes are traced by rc_cast and PATH renders");
     float3 L = make_float3(0.0f, 0.0f, 0.0f);
     int castShadow = h->lights.empty() ? 0 : 1;
     if (castShadow)

@@ -10,7 +10,7 @@ import pytest
 
 import oracle
 from raycer_gb300 import scenes
-from raycer_gb300.tracer import RAY_DTYPE, CudaTracer, RaycerError, TracerState, camera_record
+from raycer_gb300.tracer import RAY_DTYPE, CudaTracer, TracerState, camera_record
 
 from helpers import camera_floats, small_room
 from test_instancing import FIX, PARAMS, flat_to_mesh
@@ -60,14 +60,48 @@ def test_instanced_render_matches_flattened():
     assert rel < 0.05, rel
 
 
-def test_instanced_scene_refuses_ray_frames():
-    sc = scenes.heightfield_blobs_instanced(instances=2, blob_level=1, hf_nx=16, hf_nz=8, width=16, height=8)
+def test_instanced_ray_frames():
+    """RAY frames of a two-level scene: the primary records are rc_cast's
+    closest hits of the same camera rays (the same two-level traversal,
+    flattened primitive numbering), the shadow stage's occlusion agrees with
+    the flattened scene's RAY frame, and the caller-ray path through host
+    buffers returns the frame's records."""
+    sc = scenes.heightfield_blobs_instanced(**PARAMS)
     sc.settings["tracer"] = "ray"
+    sc.light_direction = (-1.0, -0.35, -0.2)  # low light: long shadows over the blobs
+    n = sc.width * sc.height
+    rays = np.ascontiguousarray(oracle.camera_rays32(camera_floats(camera_record(sc)), sc.width, n))
+    rays = rays.view(RAY_DTYPE).reshape(-1)
     with CudaTracer(0) as t:
         t.initializeInstanced(sc)
         t.initializeImageBuffers(sc.width, sc.height)
-        with pytest.raises(RaycerError):
-            t.run(TracerState(scene=sc, filmWidth=16, filmHeight=8, pixelCount=128))
+        t.run(TracerState(scene=sc, filmWidth=sc.width, filmHeight=sc.height, pixelCount=n))
+        frame = t.read_cast()
+        hits = t.cast(rays)
+        out = t.cast_with_shadow(rays)
+    assert np.array_equal(frame["prim"], hits["prim"])
+    assert np.array_equal(frame["t"][hits["prim"] >= 0], hits["t"][hits["prim"] >= 0])
+    assert np.array_equal(out, frame)
+    hit = frame["prim"] >= 0
+    assert hit.mean() > 0.5
+    # every hit pixel cast its shadow ray; misses did not
+    assert np.array_equal((frame["flags"] & 2) != 0, hit)
+    assert np.all(frame["occluder"][hit & ((frame["flags"] & 4) == 0)] == -1)
+    assert np.all(frame["occluder"][(frame["flags"] & 4) != 0] >= 0)
+
+    flat = sc.flatten()
+    flat.settings["tracer"] = "ray"
+    with CudaTracer(0) as t:
+        t.initializeBuffers(flat)
+        t.initializeImageBuffers(flat.width, flat.height)
+        t.run(TracerState(scene=flat, filmWidth=flat.width, filmHeight=flat.height, pixelCount=n))
+        ref = t.read_cast()
+    both = hit & (ref["prim"] >= 0)
+    assert both.mean() > 0.99 * hit.mean()
+    occ_i = (frame["flags"][both] & 4) != 0
+    occ_f = (ref["flags"][both] & 4) != 0
+    assert 0.1 < occ_f.mean() < 0.9, occ_f.mean()
+    assert (occ_i == occ_f).mean() > 0.99, (occ_i == occ_f).mean()
 
 
 @pytest.mark.parametrize("ms", [1, 2])
