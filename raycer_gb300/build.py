@@ -29,7 +29,7 @@ REFERENCE_SRC = Path("/root/reference")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["trace.cu", "pathtrace.cu", "tonemap.cu", "noalloc.cu", "nrc.cu", "nrc_tc.cu", "gpu_build.cu"]
-CPP_SOURCES = ["tracer_host.cpp", "render_path.cpp", "bvh_build.cpp", "batch.cpp", "nrc_host.cpp", "scene_file.cpp", "gpu_build_host.cpp", "instancing.cpp"]
+CPP_SOURCES = ["tracer_host.cpp", "render_path.cpp", "bvh_build.cpp", "batch.cpp", "nrc_host.cpp", "scene_file.cpp", "gpu_build_host.cpp", "instancing.cpp", "wide_bvh.cpp"]
 ORACLE_SOURCES = ["oracle64.cpp", "oracle32.cpp", "oracle_api.cpp", "nrc64.cpp"]
 
 

@@ -266,6 +266,10 @@ rc_status enqueue_passes(rc_batch* b, bool recordPassEvents)
         pp.nslots = int(ps.nslots);
         pp.npixels = int(ps.npixels);
         pp.segments = ps.segments;
+        pp.wide = 1;
+        for (const rc_tracer* h : b->scenes)
+            if (!h->dWide || h->nInstances > 0)
+                pp.wide = 0;
         RB_TRY(b, launch_path_pass(pp, RC_ORDER_NEAREST, 0, shape_of(b, ps.bucket), b->stream, b->numSMs, nullptr),
                "launch pass");
         if (recordPassEvents)

@@ -15,6 +15,12 @@
 //            bitangent (Triangle::initialize, Triangle.cpp:18-47, float64 on
 //            the host, cast like CLScene.cpp:214-216); read once per hit.
 //   DevMat   32 B per material.
+//   DevNode4 128 B per node of the 4-wide BVH collapsed from the DevNode tree
+//            (same leaves, same triangle order): the four children's boxes as
+//            one float4 per bound (child k in component k), their links, and
+//            the number of children. Read by the path tracer's uncounted
+//            nearest-first extend kernel (traverse_wide); the binary tree
+//            serves every other query.
 // Everything is 16-B aligned and fetched with 128-bit loads.
 #pragma once
 
@@ -35,6 +41,13 @@ struct __align__(16) DevNode
     float4 xy1;  // child 1: lo.x, hi.x, lo.y, hi.y
     float4 z01;  // child 0 lo.z, hi.z; child 1 lo.z, hi.z
     int4 link;   // child 0 (left), child 1 (right), depth-first subtree end, reserved
+};
+
+struct __align__(16) DevNode4
+{
+    float4 lox, hix, loy, hiy, loz, hiz;  // child k's box in component k
+    int4 link;   // child k: >= 0 DevNode4 index, < 0 leaf code ~((start << 4) | count)
+    int4 meta;   // x: number of children (2..4); y, z, w: 0
 };
 
 struct __align__(16) DevTri
@@ -101,6 +114,9 @@ struct DevScene
     const DevInstance* instances;
     int tlasRoot;
     int numInstances;  // 0: single-level scene
+    const DevNode4* wide;  // 4-wide BVH of a single-level scene, or null
+    int wideRoot;          // >= 0: DevNode4 0; < 0: the root is a leaf
+    int widePad;
 };
 
 // Float32 camera record used by the kernels (same fields as rc_camera).

@@ -99,6 +99,10 @@ struct rc_tracer
     rcx::DevInstance* dInstances = nullptr;
     int64_t nInstances = 0;
     int32_t tlasRoot = 0;
+    // 4-wide BVH of a single-level scene (wide_bvh.cpp), or none.
+    rcx::DevNode4* dWide = nullptr;
+    size_t wideCount = 0;
+    int32_t wideRoot = 0;
 
     // Per-frame records.
     rc_camera camera{};
@@ -171,6 +175,10 @@ void build_host_scene(const double* v, const uint32_t* matIdx, int64_t n, const 
                       std::vector<BuildNode>&& nodes, std::vector<uint32_t>&& order, uint32_t depth, HostScene& hs);
 rc_status upload_host_scene(rc_tracer* h, HostScene&& hs);
 void release_scene_data(rc_tracer* h);
+// Collapses the binary device nodes (root `rootLink`) into the 4-wide BVH and
+// uploads it (h->dWide); leaves it out where its stack need exceeds the
+// traversal stack. Failure to allocate is an error.
+rc_status upload_wide(rc_tracer* h, const std::vector<DevNode>& nodes, int32_t rootLink);
 void device_nodes(const std::vector<BuildNode>& nodes, std::vector<DevNode>& dn, int32_t& rootLink, uint64_t& inner);
 // Upload through the GPU BVH builder (gpu_build_host.cpp).
 rc_status upload_gpu_built(rc_tracer* h, const double* v, const uint32_t* matIdx, int64_t n, const rc_material* mats,

@@ -45,6 +45,10 @@ namespace
 #ifndef RC_EXTEND_MIN_BLOCKS
 #define RC_EXTEND_MIN_BLOCKS 10
 #endif
+// The same for the 4-wide traversal (four boxes per node in registers).
+#ifndef RC_EXTEND_WIDE_MIN_BLOCKS
+#define RC_EXTEND_WIDE_MIN_BLOCKS 8
+#endif
 
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
 
@@ -199,7 +203,8 @@ __device__ __forceinline__ void flush_extend_counts(const PassParams& p, unsigne
 }
 
 template <int ORDER, bool COUNT, int BLOCK>
-__global__ void __launch_bounds__(BLOCK, (RC_EXTEND_MIN_BLOCKS * 128) / BLOCK) k_extend(PassParams p, int segment)
+__global__ void __launch_bounds__(BLOCK, ((ORDER == ORDER_WIDE ? RC_EXTEND_WIDE_MIN_BLOCKS : RC_EXTEND_MIN_BLOCKS) * 128) /
+                                             BLOCK) k_extend(PassParams p, int segment)
 {
     const unsigned total = *reinterpret_cast<volatile unsigned*>(&p.counts[segment * 4 + 0]);
     const int* __restrict__ queue = (segment & 1) ? p.qb : p.qa;
@@ -220,7 +225,8 @@ __global__ void __launch_bounds__(BLOCK, (RC_EXTEND_MIN_BLOCKS * 128) / BLOCK) k
             float4 d = p.d[s];
             RayF ray = make_ray(v3(o.x, o.y, o.z), v3(d.x, d.y, d.z), 0.0f, FLT_MAX);
             HitF h{ -1, FLT_MAX, 0.0f, 0.0f, -1 };
-            bool found = traverse<false, ORDER, COUNT>(sc, ray, h, cnt, err, __float_as_int(o.w));
+            bool found = ORDER == ORDER_WIDE ? traverse_wide(sc, ray, h, err, __float_as_int(o.w))
+                                             : traverse<false, ORDER, COUNT>(sc, ray, h, cnt, err, __float_as_int(o.w));
             p.hit[s] = make_int4(found ? h.slot : -1, __float_as_int(h.t), __float_as_int(h.u), __float_as_int(h.v));
             done++;
         }
@@ -714,6 +720,7 @@ cudaError_t launch_path_segments(const PassParams& p, int order, int counting, c
             e = counting ? extend_inst<true>(p, seg, stream, numSMs) : extend_inst<false>(p, seg, stream, numSMs);
         else if (order == ORDER_NEAREST)
             e = counting ? extend_t<ORDER_NEAREST, true>(p, seg, shape.extendBlock, stream, numSMs)
+                : p.wide ? extend_t<ORDER_WIDE, false>(p, seg, shape.extendBlock, stream, numSMs)
                          : extend_t<ORDER_NEAREST, false>(p, seg, shape.extendBlock, stream, numSMs);
         else
             e = counting ? extend_t<ORDER_REF, true>(p, seg, shape.extendBlock, stream, numSMs)

@@ -100,6 +100,7 @@ struct PassParams
     DevControl* ctl;
     NrcPass nrc;
     int instanced;   // 1: the pass has two-level scenes (k_extend_instanced)
+    int wide;        // 1: every scene of the pass has its 4-wide BVH (uncounted nearest-first extend uses it)
 };
 
 // Bytes of path state per slot (o, d, thr, res, hit, two queue entries, chunk id).

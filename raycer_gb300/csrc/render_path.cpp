@@ -157,6 +157,8 @@ PathScene path_scene(const rc_tracer* h, uint64_t pixelStart)
     ps.sc.instances = h->dInstances;
     ps.sc.tlasRoot = h->tlasRoot;
     ps.sc.numInstances = int(h->nInstances);
+    ps.sc.wide = h->dWide;
+    ps.sc.wideRoot = h->wideRoot;
     for (int k = 0; k < 3; ++k)
     {
         ps.cam.pos[k] = h->camera.position[k];
@@ -269,6 +271,7 @@ rc_status render_path(rc_tracer* h, uint64_t pixelStart, uint64_t count, const v
     pp.numChunks = 1;
     pp.segments = g.max_path_length;
     pp.instanced = h->nInstances > 0 ? 1 : 0;
+    pp.wide = h->dWide != nullptr && h->nInstances == 0 ? 1 : 0;
     PassShape shape;
     const bool nrc = nrc_active(h);
     if (nrc)

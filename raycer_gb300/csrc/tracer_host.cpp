@@ -110,6 +110,9 @@ void release_scene(rc_tracer* h)
     dev_free(h, &h->dMats, size_t(h->nMats));
     dev_free(h, &h->dTlas, h->tlasCount);
     dev_free(h, &h->dInstances, size_t(h->nInstances));
+    dev_free(h, &h->dWide, h->wideCount);
+    h->wideCount = 0;
+    h->wideRoot = 0;
     h->tlasCount = 0;
     h->nInstances = 0;
     h->tlasRoot = 0;
@@ -361,6 +364,11 @@ rc_status upload_host_scene(rc_tracer* h, HostScene&& hs)
         h->bounds[k] = hs.flat[0].bmin[k];
         h->bounds[3 + k] = hs.flat[0].bmax[k];
     }
+    if ((s = upload_wide(h, dn, rootLink)) != RC_OK)
+    {
+        release_scene(h);
+        return s;
+    }
     h->hostNodes = std::move(hs.flat);
     h->hostOrder = std::move(hs.order);
     h->sceneReady = true;
@@ -431,6 +439,9 @@ DevScene dev_scene(const rc_tracer* h)
     s.instances = h->dInstances;
     s.tlasRoot = h->tlasRoot;
     s.numInstances = int(h->nInstances);
+    s.wide = h->dWide;
+    s.wideRoot = h->wideRoot;
+    s.widePad = 0;
     return s;
 }
 

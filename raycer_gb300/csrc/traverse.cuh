@@ -39,7 +39,8 @@ namespace rcx
 enum TraversalOrder
 {
     ORDER_REF = 0,
-    ORDER_NEAREST = 1
+    ORDER_NEAREST = 1,
+    ORDER_WIDE = 2  // kernels only: ORDER_NEAREST's closest hit through the 4-wide BVH (traverse_wide)
 };
 
 struct HitF
@@ -197,6 +198,140 @@ __device__ __forceinline__ bool traverse(const DevScene& sc, const RayF& ray, Hi
             sp--;
             cur = stack[sp];
             if (ORDER == ORDER_NEAREST && !ANY_HIT && sdist[sp] > hit.t)
+                continue;
+            break;
+        }
+    }
+}
+
+// Entry distance of one child box of a wide node, or +inf when the ray misses
+// it or enters it beyond `limit` (the current closest hit).
+__device__ __forceinline__ float wide_entry(const RayF& ray, float lox, float hix, float loy, float hiy, float loz,
+                                            float hiz, float limit)
+{
+    float e;
+    const bool h = ray.finite ? slab_finite(ray, lox, hix, loy, hiy, loz, hiz, e)
+                              : slab(ray, lox, hix, loy, hiy, loz, hiz, e);
+    return h && !(e > limit) ? e : __int_as_float(0x7f800000);
+}
+
+// Orders two (distance, link) pairs by distance.
+__device__ __forceinline__ void wide_cswap(float& da, int& la, float& db, int& lb)
+{
+    const bool s = db < da;
+    const float d = s ? db : da;
+    const int l = s ? lb : la;
+    db = s ? da : db;
+    lb = s ? la : lb;
+    da = d;
+    la = l;
+}
+
+// Closest hit through the 4-wide BVH (sc.wide; wide_bvh.cpp): one 128-B
+// node fetch tests up to four child boxes, the children hit within the
+// current closest distance are sorted by entry distance (a five-exchange
+// network), the nearest is entered and the others pushed farthest first with
+// their entry distances, and pops skip entries beyond the current hit. The
+// leaves and their triangle tests are the binary tree's, and the accepted
+// hit (minimum t, ties to the larger slot) does not depend on the order, so
+// it is traverse<false, ORDER_NEAREST>'s. No node or triangle counts: counted
+// frames use the binary traversal.
+__device__ __forceinline__ bool traverse_wide(const DevScene& sc, const RayF& ray, HitF& hit, int& err, int skip)
+{
+    const float kInf = __int_as_float(0x7f800000);
+    int stack[kMaxStack];
+    float sdist[kMaxStack];
+    int sp = 0;
+    int cur = sc.wideRoot;
+    bool found = false;
+    while (true)
+    {
+        if (cur >= 0)
+        {
+            const float4* p = reinterpret_cast<const float4*>(sc.wide + cur);
+            const float4 lox = __ldg(p + 0), hix = __ldg(p + 1), loy = __ldg(p + 2), hiy = __ldg(p + 3);
+            const float4 loz = __ldg(p + 4), hiz = __ldg(p + 5);
+            const int4 l = __ldg(reinterpret_cast<const int4*>(p + 6));
+            const int nc = __ldg(reinterpret_cast<const int*>(p + 7));
+            float d0 = wide_entry(ray, lox.x, hix.x, loy.x, hiy.x, loz.x, hiz.x, hit.t);
+            float d1 = wide_entry(ray, lox.y, hix.y, loy.y, hiy.y, loz.y, hiz.y, hit.t);
+            float d2 = nc > 2 ? wide_entry(ray, lox.z, hix.z, loy.z, hiy.z, loz.z, hiz.z, hit.t) : kInf;
+            float d3 = nc > 3 ? wide_entry(ray, lox.w, hix.w, loy.w, hiy.w, loz.w, hiz.w, hit.t) : kInf;
+            int l0 = l.x, l1 = l.y, l2 = l.z, l3 = l.w;
+            const int hits = (d0 < kInf ? 1 : 0) + (d1 < kInf ? 1 : 0) + (d2 < kInf ? 1 : 0) + (d3 < kInf ? 1 : 0);
+            if (hits == 1)
+            {
+                cur = d0 < kInf ? l0 : (d1 < kInf ? l1 : (d2 < kInf ? l2 : l3));
+                continue;
+            }
+            if (hits > 1)
+            {
+                wide_cswap(d0, l0, d1, l1);
+                wide_cswap(d2, l2, d3, l3);
+                wide_cswap(d0, l0, d2, l2);
+                wide_cswap(d1, l1, d3, l3);
+                wide_cswap(d1, l1, d2, l2);
+                if (sp + hits - 1 > kMaxStack)
+                {
+                    err = 1;
+                    return found;
+                }
+                if (d3 < kInf)
+                {
+                    stack[sp] = l3;
+                    sdist[sp] = d3;
+                    sp++;
+                }
+                if (d2 < kInf)
+                {
+                    stack[sp] = l2;
+                    sdist[sp] = d2;
+                    sp++;
+                }
+                if (d1 < kInf)
+                {
+                    stack[sp] = l1;
+                    sdist[sp] = d1;
+                    sp++;
+                }
+                cur = l0;
+                continue;
+            }
+        }
+        else
+        {
+            const int leaf = ~cur;
+            const int start = leaf >> kLeafCountBits;
+            const int count = leaf & ((1 << kLeafCountBits) - 1);
+            for (int i = 0; i < count; ++i)
+            {
+                const int slot = start + i;
+                if (slot == skip)
+                    continue;
+                const float4* tp = reinterpret_cast<const float4*>(sc.tris + slot);
+                const float4 ta = __ldg(tp + 0);
+                const float4 tb = __ldg(tp + 1);
+                const float4 tc = __ldg(tp + 2);
+                float t, u, v;
+                if (tri_hit(ray, v3(ta.x, ta.y, ta.z), v3(ta.w, tb.x, tb.y), v3(tb.z, tb.w, tc.x), t, u, v) &&
+                    (t < hit.t || (t == hit.t && slot > hit.slot)))
+                {
+                    hit.slot = slot;
+                    hit.t = t;
+                    hit.u = u;
+                    hit.v = v;
+                    found = true;
+                }
+            }
+        }
+        // pop
+        while (true)
+        {
+            if (sp == 0)
+                return found;
+            sp--;
+            cur = stack[sp];
+            if (sdist[sp] > hit.t)
                 continue;
             break;
         }
