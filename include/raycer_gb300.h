@@ -446,8 +446,8 @@ rc_status rc_sync(rc_tracer* h);
 /* Traced by rc_cast / rc_cast_device (hit prim = the flattened index:     */
 /* the triangles of instance 0, then of instance 1, ...), RAY frames and   */
 /* rc_cast_with_shadow (prim and occluder flattened the same way) and PATH */
-/* renders; scene files, rc_get_bvh and the allocation-free entry point    */
-/* take single-level scenes only.                                          */
+/* renders, and stored by scene files (version 2); rc_get_bvh and the      */
+/* allocation-free entry point take single-level scenes only.              */
 
 typedef struct rc_mesh
 {
@@ -475,18 +475,22 @@ rc_status rc_upload_instanced(rc_tracer* h, const rc_mesh* meshes, int32_t mesh_
 /* FlatBVH::restore, FlatBVH.h:98-105, for this path; the format is this     */
 /* build's own, not cereal's). A file holds the flat BVH in the reference's */
 /* form, the primitive order and the device triangle / shading / material   */
-/* records: loading builds nothing. Every load validates the file (magic,   */
-/* version, sizes, a 64-bit checksum, the BVH's structure and depth, the    */
-/* triangle records) before it allocates device memory; RC_IO + message on  */
-/* failure.                                                                  */
+/* records: loading builds nothing. A two-level scene's file holds each     */
+/* mesh's BVH and records and the instance descriptions; loading rebuilds   */
+/* only the BVH over the instances. Every load validates the file (magic,   */
+/* version, sizes, a 64-bit checksum, each BVH's structure and depth, the   */
+/* triangle records, the instances) before it allocates device memory;      */
+/* RC_IO + message on failure.                                               */
 
 typedef struct rc_scene_file_info
 {
     uint64_t triangles;
     uint64_t materials;
-    uint64_t bvh_nodes;   /* flat (reference-form) nodes */
-    uint64_t bvh_depth;
-    double bounds[6];     /* root box: min xyz, max xyz */
+    uint64_t bvh_nodes;   /* flat (reference-form) nodes (two-level: of all meshes) */
+    uint64_t bvh_depth;   /* (two-level: of the deepest mesh BVH) */
+    double bounds[6];     /* root box / scene box: min xyz, max xyz */
+    uint64_t meshes;      /* 0 for a single-level scene, else the mesh count */
+    uint64_t instances;   /* 0 for a single-level scene, else the instance count */
 } rc_scene_file_info;
 
 /* Writes the uploaded scene of a handle. */
@@ -498,6 +502,13 @@ rc_status rc_load_scene(rc_tracer* h, const char* path);
 rc_status rc_write_scene_file(const double* vertices, const uint32_t* material_index, int64_t n,
                               const rc_material* materials, int32_t material_count, uint32_t max_leaf_size,
                               const char* path, char* error, int64_t error_capacity);
+/* Host only (no GPU): builds the two-level scene rc_upload_instanced would
+ * upload (one SAH BVH per mesh) and writes it; rc_load_scene restores it
+ * (rebuilding only the top-level BVH over the instances). */
+rc_status rc_write_instanced_scene_file(const rc_mesh* meshes, int32_t mesh_count, const rc_instance* instances,
+                                        int64_t instance_count, const rc_material* materials, int32_t material_count,
+                                        uint32_t max_leaf_size, const char* path, char* error,
+                                        int64_t error_capacity);
 /* Host only: validates a file and reports its contents. */
 rc_status rc_inspect_scene_file(const char* path, rc_scene_file_info* out, char* error, int64_t error_capacity);
 

@@ -135,7 +135,8 @@ class rc_instance(C.Structure):
 
 class rc_scene_file_info(C.Structure):
     _fields_ = [("triangles", C.c_uint64), ("materials", C.c_uint64), ("bvh_nodes", C.c_uint64),
-                ("bvh_depth", C.c_uint64), ("bounds", C.c_double * 6)]
+                ("bvh_depth", C.c_uint64), ("bounds", C.c_double * 6), ("meshes", C.c_uint64),
+                ("instances", C.c_uint64)]
 
 
 RC_GENERAL_SKY = 1
@@ -216,6 +217,7 @@ PROTOTYPES = {
     "rc_load_scene": (i32, [P, C.c_char_p]),
     "rc_write_scene_file": (i32, [P, P, i64, P, i32, u32, C.c_char_p, C.c_char_p, i64]),
     "rc_inspect_scene_file": (i32, [C.c_char_p, C.POINTER(rc_scene_file_info), C.c_char_p, i64]),
+    "rc_write_instanced_scene_file": (i32, [P, i32, P, i64, P, i32, u32, C.c_char_p, C.c_char_p, i64]),
     "rc_film_rmse_f64": (i32, [P, P, C.POINTER(C.c_double)]),
 }
 

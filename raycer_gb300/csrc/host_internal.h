@@ -4,6 +4,7 @@
 
 #include <cuda_runtime.h>
 
+#include <chrono>
 #include <string>
 #include <vector>
 
@@ -27,6 +28,18 @@ struct HostScene
     std::vector<DevShade> shade;
     std::vector<DevMat> mats;
     uint32_t depth = 0;
+};
+
+// One mesh of an uploaded two-level scene, kept on the host for scene
+// files: its flat BVH and primitive order, and its range in the pooled
+// triangle arrays.
+struct InstancedMesh
+{
+    std::vector<BuildNode> flat;
+    std::vector<uint32_t> order;
+    uint32_t depth = 0;
+    int64_t firstTri = 0;
+    int64_t triangles = 0;
 };
 
 // Neural radiance cache state of a handle (nrc_host.cpp).
@@ -99,6 +112,8 @@ struct rc_tracer
     rcx::DevInstance* dInstances = nullptr;
     int64_t nInstances = 0;
     int32_t tlasRoot = 0;
+    std::vector<rcx::InstancedMesh> instMeshes;  // two-level scene: its meshes
+    std::vector<rc_instance> instDescs;          //   and instances, for rc_save_scene
     // 4-wide BVH of a single-level scene (wide_bvh.cpp), or none.
     rcx::DevNode4* dWide = nullptr;
     size_t wideCount = 0;
@@ -179,6 +194,21 @@ void release_scene_data(rc_tracer* h);
 // uploads it (h->dWide); leaves it out where its stack need exceeds the
 // traversal stack. Failure to allocate is an error.
 rc_status upload_wide(rc_tracer* h, const std::vector<DevNode>& nodes, int32_t rootLink);
+// Two-level scenes (instancing.cpp): argument checks, one SAH build per mesh
+// (host scenes in BVH order), and the pooled upload with instance transforms
+// and the top-level BVH (which also keeps the meshes and instances on the
+// handle for scene files). err gets the reason of a failure.
+rc_status check_instanced_args(const rc_mesh* meshes, int32_t mesh_count, const rc_instance* instances,
+                               int64_t instance_count, const rc_material* materials, int32_t material_count,
+                               uint32_t max_leaf_size, std::string& err);
+rc_status build_mesh_scenes(const rc_mesh* meshes, int32_t mesh_count, const rc_material* materials,
+                            int32_t material_count, uint32_t max_leaf_size, std::vector<HostScene>& out,
+                            std::string& err);
+// The scene box of instances of these meshes (the union of their world boxes).
+void instanced_scene_box(const std::vector<HostScene>& meshes, const rc_instance* instances, int64_t ni, double box[6]);
+rc_status upload_instanced_scenes(rc_tracer* h, std::vector<HostScene>&& meshScenes, const rc_instance* instances,
+                                  int64_t instance_count, int32_t material_count,
+                                  std::chrono::steady_clock::time_point t0);
 void device_nodes(const std::vector<BuildNode>& nodes, std::vector<DevNode>& dn, int32_t& rootLink, uint64_t& inner);
 // Upload through the GPU BVH builder (gpu_build_host.cpp).
 rc_status upload_gpu_built(rc_tracer* h, const double* v, const uint32_t* matIdx, int64_t n, const rc_material* mats,

@@ -151,29 +151,160 @@ bool invert(const M4& a, M4& out)
     return true;
 }
 
+// The reference's instance transform about the mesh box's centre c:
+// T(c + translate) * R_x(pitch) R_y(yaw) R_z(roll) * S(scale) * T(-c).
+M4 instance_transform(const double* meshBox, const rc_instance& r)
+{
+    double c[3];
+    for (int a = 0; a < 3; ++a)
+        c[a] = (meshBox[a] + meshBox[3 + a]) * 0.5;  // AABB::getCenter
+    return mul(mul(mul(translate(c[0] + r.translate[0], c[1] + r.translate[1], c[2] + r.translate[2]),
+                       mul(mul(rotate_axis(0, r.rotate[0]), rotate_axis(1, r.rotate[1])), rotate_axis(2, r.rotate[2]))),
+                   scale(r.scale[0], r.scale[1], r.scale[2])),
+               translate(-c[0], -c[1], -c[2]));
+}
+
+// World box of a mesh box under M: its 8 corners through M (AABB::transformed).
+void world_box(const double* mb, const M4& M, double* lo, double* hi)
+{
+    for (int a = 0; a < 3; ++a)
+    {
+        lo[a] = 1e300;
+        hi[a] = -1e300;
+    }
+    for (int corner = 0; corner < 8; ++corner)
+    {
+        const double p[3] = { (corner & 1) ? mb[3] : mb[0], (corner & 2) ? mb[4] : mb[1], (corner & 4) ? mb[5] : mb[2] };
+        for (int a = 0; a < 3; ++a)
+        {
+            const double w = M.m[a][0] * p[0] + M.m[a][1] * p[1] + M.m[a][2] * p[2] + M.m[a][3];
+            lo[a] = std::min(lo[a], w);
+            hi[a] = std::max(hi[a], w);
+        }
+    }
+}
+
 }  // namespace
 
-extern "C" rc_status rc_upload_instanced(rc_tracer* h, const rc_mesh* meshes, int32_t mesh_count,
-                                         const rc_instance* instances, int64_t instance_count,
-                                         const rc_material* materials, int32_t material_count,
-                                         uint32_t max_leaf_size)
+namespace rcx
 {
-    if (!h)
-        return RC_INVALID_ARG;
+
+void instanced_scene_box(const std::vector<HostScene>& meshes, const rc_instance* instances, int64_t ni, double box[6])
+{
+    for (int a = 0; a < 3; ++a)
+    {
+        box[a] = 1e300;
+        box[3 + a] = -1e300;
+    }
+    for (int64_t k = 0; k < ni; ++k)
+    {
+        const rc_instance& r = instances[k];
+        if (r.mesh < 0 || size_t(r.mesh) >= meshes.size())
+            continue;
+        const HostScene& hs = meshes[size_t(r.mesh)];
+        double mb[6];
+        for (int a = 0; a < 3; ++a)
+        {
+            mb[a] = hs.flat[0].bmin[a];
+            mb[3 + a] = hs.flat[0].bmax[a];
+        }
+        double lo[3], hi[3];
+        world_box(mb, instance_transform(mb, r), lo, hi);
+        for (int a = 0; a < 3; ++a)
+        {
+            box[a] = std::min(box[a], lo[a]);
+            box[3 + a] = std::max(box[3 + a], hi[a]);
+        }
+    }
+}
+
+rc_status check_instanced_args(const rc_mesh* meshes, int32_t mesh_count, const rc_instance* instances,
+                               int64_t instance_count, const rc_material* materials, int32_t material_count,
+                               uint32_t max_leaf_size, std::string& err)
+{
     if (!meshes || mesh_count <= 0 || !instances || instance_count <= 0 || !materials || material_count <= 0)
-        return fail(h, RC_INVALID_ARG, "upload_instanced: null array or empty scene");
+    {
+        err = "null array or empty scene";
+        return RC_INVALID_ARG;
+    }
     if (max_leaf_size < 1 || max_leaf_size > 15)
-        return fail(h, RC_UNSUPPORTED, "upload_instanced: max_leaf_size must be in 1..15");
+    {
+        err = "max_leaf_size must be in 1..15";
+        return RC_UNSUPPORTED;
+    }
     if (instance_count > (int64_t(1) << 24) || material_count > int32_t(kMetaMaterialMask))
-        return fail(h, RC_UNSUPPORTED, "upload_instanced: too many instances or materials");
+    {
+        err = "too many instances or materials";
+        return RC_UNSUPPORTED;
+    }
     for (int32_t i = 0; i < material_count; ++i)
         if ((materials[i].dielectric != 0 && materials[i].dielectric != 1) ||
             (materials[i].dielectric && !(materials[i].ior > 0.0f && std::isfinite(materials[i].ior))))
-            return fail(h, RC_INVALID_ARG, "upload_instanced: rc_material.dielectric must be 0 or 1 with ior > 0");
-    const auto t0 = std::chrono::steady_clock::now();
-    cudaSetDevice(h->device);
+        {
+            err = "rc_material.dielectric must be 0 or 1 with ior > 0";
+            return RC_INVALID_ARG;
+        }
+    return RC_OK;
+}
 
-    // Meshes: one SAH build each, pooled (node links and leaf starts offset).
+rc_status build_mesh_scenes(const rc_mesh* meshes, int32_t mesh_count, const rc_material* materials,
+                            int32_t material_count, uint32_t max_leaf_size, std::vector<HostScene>& out,
+                            std::string& err)
+{
+    out.clear();
+    out.resize(static_cast<size_t>(mesh_count));
+    int64_t total = 0;
+    for (int32_t m = 0; m < mesh_count; ++m)
+    {
+        const rc_mesh& me = meshes[m];
+        const int64_t n = me.triangle_count;
+        if (!me.vertices || !me.material_index || n <= 0)
+        {
+            err = "mesh " + std::to_string(m) + " is empty";
+            return RC_INVALID_ARG;
+        }
+        for (int64_t i = 0; i < n; ++i)
+            if (me.material_index[i] >= uint32_t(material_count))
+            {
+                err = "material index out of range in mesh " + std::to_string(m);
+                return RC_INVALID_ARG;
+            }
+        for (int64_t i = 0; i < n * 9; ++i)
+            if (!std::isfinite(me.vertices[i]))
+            {
+                err = "non-finite vertex in mesh " + std::to_string(m);
+                return RC_INVALID_ARG;
+            }
+        total += n;
+        if (total > (int64_t(1) << 27))
+        {
+            err = "more than 2^27 mesh triangles in total";
+            return RC_UNSUPPORTED;
+        }
+        BuildResult br;
+        if (!buildFlatBVH(me.vertices, n, max_leaf_size, 0, br, err))
+        {
+            err = "mesh " + std::to_string(m) + ": " + err;
+            return RC_INVALID_ARG;
+        }
+        if (br.depth > uint32_t(kMaxStack))
+        {
+            err = "a mesh BVH is deeper than the traversal stack";
+            return RC_UNSUPPORTED;
+        }
+        build_host_scene(me.vertices, me.material_index, n, materials, material_count, std::move(br.nodes),
+                         std::move(br.order), br.depth, out[size_t(m)]);
+    }
+    return RC_OK;
+}
+
+rc_status upload_instanced_scenes(rc_tracer* h, std::vector<HostScene>&& meshScenes, const rc_instance* instances,
+                                  int64_t instance_count, int32_t material_count,
+                                  std::chrono::steady_clock::time_point t0)
+{
+    const int32_t mesh_count = int32_t(meshScenes.size());
+    cudaSetDevice(h->device);
+    // Meshes, pooled (node links and leaf starts offset).
     std::vector<DevNode> nodes;
     std::vector<DevTri> tris;
     std::vector<DevShade> shade;
@@ -181,36 +312,17 @@ extern "C" rc_status rc_upload_instanced(rc_tracer* h, const rc_mesh* meshes, in
     std::vector<double> meshBox(static_cast<size_t>(mesh_count) * 6);
     std::vector<uint32_t> meshDepth(static_cast<size_t>(mesh_count));
     std::vector<int64_t> meshTris(static_cast<size_t>(mesh_count));
+    std::vector<int64_t> meshFirst(static_cast<size_t>(mesh_count));
     std::vector<DevMat> mats;
     for (int32_t m = 0; m < mesh_count; ++m)
     {
-        const rc_mesh& me = meshes[m];
-        const int64_t n = me.triangle_count;
-        if (!me.vertices || !me.material_index || n <= 0)
-            return fail(h, RC_INVALID_ARG, "upload_instanced: mesh " + std::to_string(m) + " is empty");
-        for (int64_t i = 0; i < n; ++i)
-            if (me.material_index[i] >= uint32_t(material_count))
-                return fail(h, RC_INVALID_ARG, "upload_instanced: material index out of range in mesh " +
-                                                   std::to_string(m));
-        for (int64_t i = 0; i < n * 9; ++i)
-            if (!std::isfinite(me.vertices[i]))
-                return fail(h, RC_INVALID_ARG, "upload_instanced: non-finite vertex in mesh " + std::to_string(m));
-        if (int64_t(tris.size()) + n > (int64_t(1) << 27))
-            return fail(h, RC_UNSUPPORTED, "upload_instanced: more than 2^27 mesh triangles in total");
-        BuildResult br;
-        std::string err;
-        if (!buildFlatBVH(me.vertices, n, max_leaf_size, 0, br, err))
-            return fail(h, RC_INVALID_ARG, "upload_instanced: mesh " + std::to_string(m) + ": " + err);
-        if (br.depth > uint32_t(kMaxStack))
-            return fail(h, RC_UNSUPPORTED, "upload_instanced: a mesh BVH is deeper than the traversal stack");
+        HostScene& hs = meshScenes[size_t(m)];
+        const int64_t n = int64_t(hs.tris.size());
         for (int k = 0; k < 3; ++k)
         {
-            meshBox[size_t(m) * 6 + k] = br.nodes[0].bmin[k];
-            meshBox[size_t(m) * 6 + 3 + k] = br.nodes[0].bmax[k];
+            meshBox[size_t(m) * 6 + k] = hs.flat[0].bmin[k];
+            meshBox[size_t(m) * 6 + 3 + k] = hs.flat[0].bmax[k];
         }
-        HostScene hs;
-        build_host_scene(me.vertices, me.material_index, n, materials, material_count, std::move(br.nodes),
-                         std::move(br.order), br.depth, hs);
         std::vector<DevNode> dn;
         int32_t root = 0;
         uint64_t inner = 0;
@@ -234,12 +346,12 @@ extern "C" rc_status rc_upload_instanced(rc_tracer* h, const rc_mesh* meshes, in
         meshRoot[size_t(m)] = relink(root);
         meshDepth[size_t(m)] = hs.depth;
         meshTris[size_t(m)] = n;
+        meshFirst[size_t(m)] = int64_t(triBase);
         tris.insert(tris.end(), hs.tris.begin(), hs.tris.end());
         shade.insert(shade.end(), hs.shade.begin(), hs.shade.end());
         if (m == 0)
             mats = hs.mats;
     }
-
     // Instances: transforms, world boxes, flattened primitive numbering.
     const int64_t ni = instance_count;
     std::vector<DevInstance> inst(static_cast<size_t>(ni));
@@ -257,14 +369,7 @@ extern "C" rc_status rc_upload_instanced(rc_tracer* h, const rc_mesh* meshes, in
                 r.scale[a] == 0.0)
                 return fail(h, RC_INVALID_ARG, "upload_instanced: non-finite or zero transform component");
         const double* mb = &meshBox[size_t(r.mesh) * 6];
-        double c[3];
-        for (int a = 0; a < 3; ++a)
-            c[a] = (mb[a] + mb[3 + a]) * 0.5;  // AABB::getCenter
-        const M4 M = mul(mul(mul(translate(c[0] + r.translate[0], c[1] + r.translate[1], c[2] + r.translate[2]),
-                                 mul(mul(rotate_axis(0, r.rotate[0]), rotate_axis(1, r.rotate[1])),
-                                     rotate_axis(2, r.rotate[2]))),
-                             scale(r.scale[0], r.scale[1], r.scale[2])),
-                         translate(-c[0], -c[1], -c[2]));
+        const M4 M = instance_transform(mb, r);
         M4 Mi;
         if (!invert(M, Mi))
             return fail(h, RC_INVALID_ARG, "upload_instanced: singular instance transform");
@@ -281,18 +386,8 @@ extern "C" rc_status rc_upload_instanced(rc_tracer* h, const rc_mesh* meshes, in
         d.identity = ident ? 1 : 0;
         primBase += meshTris[size_t(r.mesh)];
         // world box: the mesh box's corners through M
-        double lo[3] = { 1e300, 1e300, 1e300 }, hi[3] = { -1e300, -1e300, -1e300 };
-        for (int corner = 0; corner < 8; ++corner)
-        {
-            const double p[3] = { (corner & 1) ? mb[3] : mb[0], (corner & 2) ? mb[4] : mb[1],
-                                  (corner & 4) ? mb[5] : mb[2] };
-            for (int a = 0; a < 3; ++a)
-            {
-                const double w = M.m[a][0] * p[0] + M.m[a][1] * p[1] + M.m[a][2] * p[2] + M.m[a][3];
-                lo[a] = std::min(lo[a], w);
-                hi[a] = std::max(hi[a], w);
-            }
-        }
+        double lo[3], hi[3];
+        world_box(mb, M, lo, hi);
         // the SAH builder takes triangles: (lo, hi, hi) has this box and centre
         for (int a = 0; a < 3; ++a)
         {
@@ -391,9 +486,45 @@ extern "C" rc_status rc_upload_instanced(rc_tracer* h, const rc_mesh* meshes, in
                       mats.size() * sizeof(DevMat) + tn.size() * sizeof(DevNode) + ordered.size() * sizeof(DevInstance);
     h->hostNodes.clear();
     h->hostOrder.clear();
+    // kept for rc_save_scene: each mesh's flat BVH, order and place in the
+    // pooled triangle arrays, and the instance descriptions
+    h->instMeshes.clear();
+    h->instMeshes.resize(static_cast<size_t>(mesh_count));
+    for (int32_t m = 0; m < mesh_count; ++m)
+    {
+        InstancedMesh& im = h->instMeshes[size_t(m)];
+        im.flat = std::move(meshScenes[size_t(m)].flat);
+        im.order = std::move(meshScenes[size_t(m)].order);
+        im.depth = meshDepth[size_t(m)];
+        im.firstTri = meshFirst[size_t(m)];
+        im.triangles = meshTris[size_t(m)];
+    }
+    h->instDescs.assign(instances, instances + ni);
     for (int k = 0; k < 6; ++k)
         h->bounds[k] = sceneBox[k];
     h->sceneReady = true;
     h->stats.build_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     return RC_OK;
+}
+
+}  // namespace rcx
+
+extern "C" rc_status rc_upload_instanced(rc_tracer* h, const rc_mesh* meshes, int32_t mesh_count,
+                                         const rc_instance* instances, int64_t instance_count,
+                                         const rc_material* materials, int32_t material_count,
+                                         uint32_t max_leaf_size)
+{
+    if (!h)
+        return RC_INVALID_ARG;
+    std::string err;
+    rc_status s = check_instanced_args(meshes, mesh_count, instances, instance_count, materials, material_count,
+                                       max_leaf_size, err);
+    if (s != RC_OK)
+        return fail(h, s, "upload_instanced: " + err);
+    const auto t0 = std::chrono::steady_clock::now();
+    std::vector<HostScene> meshScenes;
+    if ((s = build_mesh_scenes(meshes, mesh_count, materials, material_count, max_leaf_size, meshScenes, err)) !=
+        RC_OK)
+        return fail(h, s, "upload_instanced: " + err);
+    return upload_instanced_scenes(h, std::move(meshScenes), instances, instance_count, material_count, t0);
 }

@@ -122,6 +122,8 @@ void release_scene(rc_tracer* h)
     h->innerCount = 0;
     h->hostNodes.clear();
     h->hostOrder.clear();
+    h->instMeshes.clear();
+    h->instDescs.clear();
 }
 
 void release_film(rc_tracer* h)

@@ -160,12 +160,45 @@ class Film:
         return self.toneMappedImage
 
 
-def write_scene_file(scene: SceneDesc, path) -> None:
-    """Host-only: builds the scene's BVH and device records and writes a scene file."""
+def _instanced_arrays(scene):
+    """rc_mesh / rc_instance arrays of a two-level scene (scenes.InstancedScene)
+    and the numpy arrays they point into (keep them alive during the call)."""
+    meshes = (N.rc_mesh * len(scene.meshes))()
+    keep = []
+    for i, (v, m) in enumerate(scene.meshes):
+        v = np.ascontiguousarray(v, np.float64)
+        m = np.ascontiguousarray(m, np.uint32)
+        keep += [v, m]
+        meshes[i].vertices = v.ctypes.data
+        meshes[i].material_index = m.ctypes.data
+        meshes[i].triangle_count = v.shape[0]
+    insts = (N.rc_instance * len(scene.instances))()
+    for i, d in enumerate(scene.instances):
+        insts[i].mesh = int(d.mesh)
+        insts[i].material = int(d.material)
+        insts[i].scale[:] = [float(x) for x in d.scale]
+        insts[i].rotate[:] = [float(x) for x in d.rotate]
+        insts[i].translate[:] = [float(x) for x in d.translate]
+    return meshes, insts, keep
+
+
+def write_scene_file(scene, path) -> None:
+    """Host-only: builds the scene's BVH(s) and device records and writes a
+    scene file (a SceneDesc, or a two-level scenes.InstancedScene)."""
+    err = C.create_string_buffer(512)
+    if hasattr(scene, "instances"):
+        meshes, insts, keep = _instanced_arrays(scene)
+        mats = materials_array(scene.materials)
+        st = N.lib().rc_write_instanced_scene_file(meshes, len(scene.meshes), insts, len(scene.instances), mats,
+                                                    len(scene.materials), int(scene.max_leaf_size),
+                                                    str(path).encode(), err, 512)
+        del keep
+        if st != N.RC_OK:
+            raise RaycerError(st, f"write_scene_file: {err.value.decode()}")
+        return
     v = np.ascontiguousarray(scene.vertices, np.float64)
     m = np.ascontiguousarray(scene.material_index, np.uint32)
     mats = materials_array(scene.materials)
-    err = C.create_string_buffer(512)
     st = N.lib().rc_write_scene_file(_ptr(v), _ptr(m), v.shape[0], mats, len(scene.materials),
                                       int(scene.max_leaf_size), str(path).encode(), err, 512)
     if st != N.RC_OK:
@@ -180,7 +213,8 @@ def inspect_scene_file(path) -> dict:
     if st != N.RC_OK:
         raise RaycerError(st, err.value.decode())
     return {"triangles": info.triangles, "materials": info.materials, "bvh_nodes": info.bvh_nodes,
-            "bvh_depth": info.bvh_depth, "bounds": list(info.bounds)}
+            "bvh_depth": info.bvh_depth, "bounds": list(info.bounds), "meshes": info.meshes,
+            "instances": info.instances}
 
 
 class CudaTracer:
@@ -275,22 +309,7 @@ class CudaTracer:
 
     def initializeInstanced(self, scene, seed: int = 1) -> None:
         """Uploads a two-level scene (scenes.InstancedScene) with rc_upload_instanced."""
-        meshes = (N.rc_mesh * len(scene.meshes))()
-        keep = []
-        for i, (v, m) in enumerate(scene.meshes):
-            v = np.ascontiguousarray(v, np.float64)
-            m = np.ascontiguousarray(m, np.uint32)
-            keep += [v, m]
-            meshes[i].vertices = v.ctypes.data
-            meshes[i].material_index = m.ctypes.data
-            meshes[i].triangle_count = v.shape[0]
-        insts = (N.rc_instance * len(scene.instances))()
-        for i, d in enumerate(scene.instances):
-            insts[i].mesh = int(d.mesh)
-            insts[i].material = int(d.material)
-            insts[i].scale[:] = [float(x) for x in d.scale]
-            insts[i].rotate[:] = [float(x) for x in d.rotate]
-            insts[i].translate[:] = [float(x) for x in d.translate]
+        meshes, insts, keep = _instanced_arrays(scene)
         mats = materials_array(scene.materials)
         self._check(self._lib.rc_upload_instanced(self._h, meshes, len(scene.meshes), insts, len(scene.instances),
                                                   mats, len(scene.materials), int(scene.max_leaf_size)),

@@ -56,3 +56,33 @@ def test_cache_argument_and_damaged_file(tmp_path):
             t.load_scene(bad, sc)
         assert e.value.status == N.RC_IO and "checksum" in str(e.value)
         assert np.array_equal(render(t, sc), first)    # the loaded scene is still there
+
+
+def test_instanced_scene_files(tmp_path):
+    """Two-level scenes through scene files: the file saved from a handle and
+    the host-written one load into scenes that render and cast exactly like
+    the uploaded one (the same mesh BVHs; the top level rebuilt the same)."""
+    import oracle
+    from raycer_gb300 import scenes
+    from raycer_gb300.tracer import RAY_DTYPE, camera_record
+
+    from helpers import camera_floats
+
+    sc = scenes.heightfield_blobs_instanced(instances=8, blob_level=2, hf_nx=32, hf_nz=16, width=48, height=27,
+                                            seed=5)
+    sc.settings.update(max_path_length=5)
+    n = sc.width * sc.height
+    rays = np.ascontiguousarray(oracle.camera_rays32(camera_floats(camera_record(sc)), sc.width, n))
+    rays = rays.view(RAY_DTYPE).reshape(-1)
+    with CudaTracer(0) as a:
+        a.initializeInstanced(sc, seed=4)
+        film = render(a, sc)
+        hits = a.cast(rays)
+        a.save_scene(tmp_path / "saved.rcgb")
+    assert (hits["prim"] >= 0).mean() > 0.1, (hits["prim"] >= 0).mean()
+    write_scene_file(sc, tmp_path / "written.rcgb")
+    for name in ("saved.rcgb", "written.rcgb"):
+        with CudaTracer(0) as b:
+            b.load_scene(tmp_path / name, sc, seed=4)
+            assert np.array_equal(render(b, sc), film), name
+            assert np.array_equal(b.cast(rays), hits), name

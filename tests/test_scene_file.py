@@ -67,3 +67,39 @@ def test_damaged_files_are_refused(tmp_path):
     refused(bytes(counts), "out of range")
     with pytest.raises(RaycerError):
         inspect_scene_file(tmp_path / "missing.rcgb")
+
+
+def test_instanced_scene_file(tmp_path):
+    """Two-level scenes (version 2): one BVH per mesh, the instances, the
+    scene box; a damaged payload is refused like a single-level one."""
+    from raycer_gb300 import scenes
+
+    sc = scenes.heightfield_blobs_instanced(instances=6, blob_level=2, hf_nx=32, hf_nz=16, width=32, height=18, seed=3)
+    path = tmp_path / "inst.rcgb"
+    write_scene_file(sc, path)
+    info = inspect_scene_file(path)
+    tris = sum(v.shape[0] for v, _ in sc.meshes)
+    assert info["meshes"] == len(sc.meshes) and info["instances"] == len(sc.instances)
+    assert info["triangles"] == tris and info["materials"] == len(sc.materials)
+    assert 1 <= info["bvh_depth"] <= 64
+    # the scene box holds every flattened vertex
+    flat = sc.flatten().vertices.reshape(-1, 3)
+    assert np.all(flat.min(axis=0) >= np.array(info["bounds"][:3]) - 1e-6)
+    assert np.all(flat.max(axis=0) <= np.array(info["bounds"][3:]) + 1e-6)
+    expect = (128 + len(sc.meshes) * 24 + info["bvh_nodes"] * 72 + tris * (4 + 48 + 48) + len(sc.materials) * 32 +
+              len(sc.instances) * 80)
+    assert path.stat().st_size == expect
+    raw = bytearray(path.read_bytes())
+    raw[-40] ^= 0x10  # inside the instance records
+    bad = tmp_path / "bad.rcgb"
+    bad.write_bytes(bytes(raw))
+    with pytest.raises(RaycerError) as e:
+        inspect_scene_file(bad)
+    assert e.value.status == N.RC_IO and "checksum" in str(e.value)
+
+
+def test_single_level_file_reports_no_instances(tmp_path):
+    path = tmp_path / "room.rcgb"
+    write_scene_file(small_room(clutter=50), path)
+    info = inspect_scene_file(path)
+    assert info["meshes"] == 0 and info["instances"] == 0
