@@ -234,7 +234,11 @@ rc_status upload_scene_table(rc_batch* b)
         return s;
     std::vector<PathScene> table(b->scenes.size());
     for (size_t i = 0; i < b->scenes.size(); ++i)
+    {
+        if ((s = ensure_wide(b->scenes[i])) != RC_OK)
+            return fail(b, s, "batch: scene " + std::to_string(i) + ": " + b->scenes[i]->err);
         table[i] = path_scene(b->scenes[i], 0);
+    }
     RB_TRY(b, cudaMemcpyAsync(b->dScenes, table.data(), table.size() * sizeof(PathScene), cudaMemcpyHostToDevice,
                               b->stream),
            "upload scene table");

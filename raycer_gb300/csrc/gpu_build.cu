@@ -7,6 +7,7 @@
 //   1. k_prep        float vertices, triangle boxes and centroids; per-block
 //                    centroid bounds (k_bounds_final reduces them)
 //   2. k_morton      30-bit Morton code of each centroid in the centroid box
+//                    (cubic cells: one scale, the box's largest extent)
 //   3. radix sort    (code, triangle) pairs, 4 stable passes of 8 bits:
 //                    per-tile digit histograms, one exclusive scan over
 //                    (digit, tile), stable scatter ranked with __match_any_sync
@@ -149,15 +150,16 @@ __global__ void k_morton(const float4* __restrict__ cen, int n, const float4* __
     if (i >= n)
         return;
     const float4 lo = box[0], hi = box[1], c = cen[i];
-    const float e[3] = { hi.x - lo.x, hi.y - lo.y, hi.z - lo.z };
+    // one scale for all axes (the largest extent): cells are cubes, so a flat
+    // scene's thin axis only splits where the cells have become that small
+    // (scaling each axis to its own extent would split a heightfield by
+    // height at the second level, into boxes that overlap everywhere)
+    const float ext = fmaxf(fmaxf(hi.x - lo.x, hi.y - lo.y), hi.z - lo.z);
+    const float inv = ext > 0.0f ? 1024.0f / ext : 0.0f;
     const float p[3] = { c.x - lo.x, c.y - lo.y, c.z - lo.z };
     uint32_t q[3];
     for (int a = 0; a < 3; ++a)
-    {
-        float u = e[a] > 0.0f ? p[a] / e[a] : 0.5f;
-        u = fminf(fmaxf(u * 1024.0f, 0.0f), 1023.0f);
-        q[a] = uint32_t(u);
-    }
+        q[a] = uint32_t(fminf(fmaxf(p[a] * inv, 0.0f), 1023.0f));
     keys[i] = (spread3(q[0]) << 2) | (spread3(q[1]) << 1) | spread3(q[2]);
     vals[i] = uint32_t(i);
 }

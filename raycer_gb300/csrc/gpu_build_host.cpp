@@ -236,12 +236,6 @@ rc_status upload_gpu_built(rc_tracer* h, const double* v, const uint32_t* matIdx
         release_scene_data(h);
         return fail(h, RC_DEVICE_ERROR, "gpu build: produced an invalid BVH: " + err);
     }
-    rc_status ws = upload_wide(h, hn, rootLink);
-    if (ws != RC_OK)
-    {
-        release_scene_data(h);
-        return ws;
-    }
     h->rootLink = rootLink;
     h->bvhDepth = flatDepth;
     for (int k = 0; k < 3; ++k)

@@ -210,6 +210,11 @@ PassParams pass_params(void* state, uint64_t slots, unsigned* counts, DevControl
 rc_status render_path(rc_tracer* h, uint64_t pixelStart, uint64_t count, const volatile int32_t* cancel)
 {
     const rc_general& g = h->general;
+    {
+        rc_status ws = ensure_wide(h);
+        if (ws != RC_OK)
+            return ws;
+    }
     const uint64_t spp = uint64_t(g.multi_sample_count_sqrt) * uint64_t(g.multi_sample_count_sqrt) *
                          uint64_t(g.path_sample_count);
     if (spp > kTargetSlots)

@@ -113,6 +113,7 @@ void release_scene(rc_tracer* h)
     dev_free(h, &h->dWide, h->wideCount);
     h->wideCount = 0;
     h->wideRoot = 0;
+    h->wideTried = false;
     h->tlasCount = 0;
     h->nInstances = 0;
     h->tlasRoot = 0;
@@ -365,11 +366,6 @@ rc_status upload_host_scene(rc_tracer* h, HostScene&& hs)
     {
         h->bounds[k] = hs.flat[0].bmin[k];
         h->bounds[3 + k] = hs.flat[0].bmax[k];
-    }
-    if ((s = upload_wide(h, dn, rootLink)) != RC_OK)
-    {
-        release_scene(h);
-        return s;
     }
     h->hostNodes = std::move(hs.flat);
     h->hostOrder = std::move(hs.order);

@@ -1,5 +1,6 @@
 // 4-wide BVH of a single-level scene, collapsed on the host from its binary
-// device nodes at upload time, for the path tracer's extend kernel (bounce
+// device nodes at the scene's first PATH render, for the path tracer's
+// extend kernel (bounce
 // rays: 5 % less extend time than the binary tree on a 5M-triangle scene;
 // for rc_cast's random rays it measured 3 % slower, so rc_cast keeps the
 // binary tree).
@@ -180,6 +181,25 @@ rc_status upload_wide(rc_tracer* h, const std::vector<DevNode>& nodes, int32_t r
     h->wideRoot = 0;
     h->deviceBytes += wide.size() * sizeof(DevNode4);
     return RC_OK;
+}
+
+rc_status ensure_wide(rc_tracer* h)
+{
+    if (h->wideTried || !h->sceneReady || h->nInstances > 0)
+        return RC_OK;
+    h->wideTried = true;
+    std::vector<DevNode> nodes(h->rootLink >= 0 ? h->innerCount : 0);
+    if (!nodes.empty())
+    {
+        cudaError_t e = cudaMemcpy(nodes.data(), h->dNodes, nodes.size() * sizeof(DevNode), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess)
+        {
+            cudaGetLastError();
+            h->err = std::string("wide BVH: download nodes: ") + cudaGetErrorString(e);
+            return RC_CUDA;
+        }
+    }
+    return upload_wide(h, nodes, h->rootLink);
 }
 
 }  // namespace rcx
