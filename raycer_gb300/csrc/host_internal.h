@@ -181,8 +181,10 @@ struct rc_tracer
 namespace rcx
 {
 
+// dOrigins (optional): per shadow-queue entry, the shadow ray's origin
+// (launch_raycast's shadowOrigins).
 rc_status raycast_into(rc_tracer* h, const rc_ray* dRays, uint64_t pixelStart, uint64_t count, int order,
-                       rc_cast_pixel* dOut, int* dQueue);
+                       rc_cast_pixel* dOut, int* dQueue, float4* dOrigins = nullptr);
 rc_status render_raycast(rc_tracer* h, uint64_t pixelStart, uint64_t count, const rc_ray* dRays);
 rc_status render_path(rc_tracer* h, uint64_t pixelStart, uint64_t count, const volatile int32_t* cancel);
 void release_render_buffers(rc_tracer* h);

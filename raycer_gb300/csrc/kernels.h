@@ -38,6 +38,11 @@ cudaError_t launch_cast(const LaunchInfo& li, const DevScene& sc, const rc_ray* 
 cudaError_t launch_raycast(const LaunchInfo& li, const DevScene& sc, const DevCamera& cam, const rc_ray* rays,
                            uint64_t pixelStart, int64_t count, int64_t width, int order, int castShadow,
                            float3 dirToLight, float rayStartOffset, rc_cast_pixel* out, int* shadowQueue,
-                           DevControl* ctl, cudaEvent_t between);
+                           DevControl* ctl, cudaEvent_t between, float4* shadowOrigins = nullptr);
+// shadowOrigins (optional, device memory, one float4 per queue entry): the
+// primary kernel stores each hit pixel's shadow-ray origin there (and, in a
+// two-level scene, the hit's instance in w), so the shadow kernel reads
+// neither the caller's rays nor the records again: for rays and records in
+// host memory, that is the host-link traffic of a second pass.
 
 }  // namespace rcx

@@ -133,7 +133,8 @@ __global__ void __launch_bounds__(kBlock, RC_TRACE_MIN_BLOCKS) k_raycast_primary
                                                             uint64_t pixelStart, int64_t count, int64_t width,
                                                             int64_t height, int64_t tilesX, int castShadow,
                                                             rc_cast_pixel* __restrict__ out, int* __restrict__ queue,
-                                                            DevControl* ctl)
+                                                            DevControl* ctl, float3 L, float rayStartOffset,
+                                                            float4* __restrict__ origins)
 {
     __shared__ PacketEntry wstack[PACKET ? kWarpsPerBlock : 1][PACKET ? kMaxStack : 1];
     TravCount cnt{ 0, 0 };
@@ -157,6 +158,7 @@ __global__ void __launch_bounds__(kBlock, RC_TRACE_MIN_BLOCKS) k_raycast_primary
         }
         bool hitAny = false;
         int hitSlot = -1;
+        float4 sorg = make_float4(0.0f, 0.0f, 0.0f, 0.0f);  // shadow-ray origin (+ instance) for `origins`
         if (PACKET)
         {
             // all lanes together, the ray of an invalid lane unused
@@ -173,6 +175,13 @@ __global__ void __launch_bounds__(kBlock, RC_TRACE_MIN_BLOCKS) k_raycast_primary
                 reinterpret_cast<int4*>(out)[i] = o;
                 hitAny = found && castShadow;
                 hitSlot = h.slot;
+                if (origins && hitAny)
+                {
+                    // the shadow kernel's own arithmetic (ip = o + t d, then + L * offset)
+                    const V3 dl = v3(L.x, L.y, L.z);
+                    const V3 so = vfma(dl, rayStartOffset, vfma(ray.d, h.t, ray.o));
+                    sorg = make_float4(so.x, so.y, so.z, __int_as_float(-1));
+                }
                 done++;
             }
         }
@@ -189,6 +198,12 @@ __global__ void __launch_bounds__(kBlock, RC_TRACE_MIN_BLOCKS) k_raycast_primary
             o.x = found ? caller_index(sc, h.slot) + (INST ? __ldg(&sc.instances[h.inst].primBase) : 0) : -1;
             o.y = __float_as_int(found ? h.t : -1.0f);
             o.z = INST && found && castShadow ? h.inst : -1;
+            if (origins && found && castShadow)
+            {
+                const V3 dl = v3(L.x, L.y, L.z);
+                const V3 so = vfma(dl, rayStartOffset, vfma(ray.d, h.t, ray.o));
+                sorg = make_float4(so.x, so.y, so.z, __int_as_float(INST ? h.inst : -1));
+            }
             o.w = found ? 1 : 0;
             reinterpret_cast<int4*>(out)[i] = o;
             hitAny = found && castShadow;
@@ -204,8 +219,12 @@ __global__ void __launch_bounds__(kBlock, RC_TRACE_MIN_BLOCKS) k_raycast_primary
                 qbase = atomicAdd(&ctl->head[1], unsigned(__popc(mask)));
             qbase = __shfl_sync(0xffffffffu, qbase, 0);
             if (hitAny)
-                reinterpret_cast<int2*>(queue)[qbase + __popc(mask & ((1u << lane_id()) - 1u))] =
-                    make_int2(int(i), hitSlot);
+            {
+                const unsigned qi = qbase + __popc(mask & ((1u << lane_id()) - 1u));
+                reinterpret_cast<int2*>(queue)[qi] = make_int2(int(i), hitSlot);
+                if (origins)
+                    origins[qi] = sorg;
+            }
         }
     }
     flush_counts(ctl, 0, done, cnt, err);
@@ -219,7 +238,8 @@ template <bool COUNT, bool INST>
 __global__ void __launch_bounds__(kBlock, RC_TRACE_MIN_BLOCKS) k_raycast_shadow(DevScene sc, DevCamera cam, const rc_ray* __restrict__ rays,
                                                            uint64_t pixelStart, int64_t width, float3 L,
                                                            float rayStartOffset, rc_cast_pixel* __restrict__ out,
-                                                           const int* __restrict__ queue, DevControl* ctl)
+                                                           const int* __restrict__ queue, DevControl* ctl,
+                                                           const float4* __restrict__ origins)
 {
     TravCount cnt{ 0, 0 };
     int err = 0;
@@ -235,19 +255,30 @@ __global__ void __launch_bounds__(kBlock, RC_TRACE_MIN_BLOCKS) k_raycast_shadow(
         {
             int2 e = reinterpret_cast<const int2*>(queue)[q];
             int i = e.x;
-            RayF pr = primary_ray(cam, rays, pixelStart + uint64_t(i), i, width);
-            float t = out[i].t;
-            // ip = origin + t * direction (intersections.cl:85)
-            V3 ip = vfma(pr.d, t, pr.o);
             V3 dl = v3(L.x, L.y, L.z);
-            RayF sr = make_ray(vfma(dl, rayStartOffset, ip), dl, 0.0f, FLT_MAX);
+            RayF sr;
+            int skipInst = -1;
+            if (origins)
+            {
+                // stored by the primary kernel with the arithmetic below
+                const float4 so = origins[q];
+                sr = make_ray(v3(so.x, so.y, so.z), dl, 0.0f, FLT_MAX);
+                skipInst = __float_as_int(so.w);
+            }
+            else
+            {
+                RayF pr = primary_ray(cam, rays, pixelStart + uint64_t(i), i, width);
+                float t = out[i].t;
+                // ip = origin + t * direction (intersections.cl:85)
+                V3 ip = vfma(pr.d, t, pr.o);
+                sr = make_ray(vfma(dl, rayStartOffset, ip), dl, 0.0f, FLT_MAX);
+                if (INST)
+                    skipInst = out[i].occluder;  // the primary stage left the hit's instance there
+            }
             HitF h{ -1, FLT_MAX, 0.0f, 0.0f, -1 };
             bool occ;
             if (INST)
-            {
-                // the primary stage left the hit's instance in the occluder field
-                occ = traverse_instanced<true, COUNT>(sc, sr, h, cnt, err, e.y, out[i].occluder);
-            }
+                occ = traverse_instanced<true, COUNT>(sc, sr, h, cnt, err, e.y, skipInst);
             else
                 occ = traverse<true, ORDER_REF, COUNT>(sc, sr, h, cnt, err, e.y);
             out[i].occluder = occ ? caller_index(sc, h.slot) + (INST ? __ldg(&sc.instances[h.inst].primBase) : 0) : -1;
@@ -307,7 +338,7 @@ bool whole_frame(uint64_t pixelStart, int64_t count, int64_t width)
 template <int ORDER, bool COUNT, bool PACKET, bool INST>
 cudaError_t raycast_t(const LaunchInfo& li, const DevScene& sc, const DevCamera& cam, const rc_ray* rays,
                       uint64_t pixelStart, int64_t count, int64_t width, int castShadow, float3 L, float off,
-                      rc_cast_pixel* out, int* queue, DevControl* ctl, cudaEvent_t between)
+                      rc_cast_pixel* out, int* queue, DevControl* ctl, cudaEvent_t between, float4* origins)
 {
     auto kp = k_raycast_primary<ORDER, COUNT, PACKET, INST>;
     auto ks = k_raycast_shadow<COUNT, INST>;
@@ -321,13 +352,13 @@ cudaError_t raycast_t(const LaunchInfo& li, const DevScene& sc, const DevCamera&
     const int64_t height = width > 0 ? count / width : 0;
     const int64_t tilesX = whole_frame(pixelStart, count, width) ? (width + 7) / 8 : 0;
     kp<<<gp, kBlock, 0, li.stream>>>(sc, cam, rays, pixelStart, count, width, height, tilesX, castShadow, out, queue,
-                                     ctl);
+                                     ctl, L, off, castShadow ? origins : nullptr);
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess && between)
         e = cudaEventRecord(between, li.stream);
     if (e != cudaSuccess || !castShadow)
         return e;
-    ks<<<gs, kBlock, 0, li.stream>>>(sc, cam, rays, pixelStart, width, L, off, out, queue, ctl);
+    ks<<<gs, kBlock, 0, li.stream>>>(sc, cam, rays, pixelStart, width, L, off, out, queue, ctl, origins);
     return cudaGetLastError();
 }
 
@@ -351,12 +382,12 @@ cudaError_t launch_cast(const LaunchInfo& li, const DevScene& sc, const rc_ray* 
 cudaError_t launch_raycast(const LaunchInfo& li, const DevScene& sc, const DevCamera& cam, const rc_ray* rays,
                            uint64_t pixelStart, int64_t count, int64_t width, int order, int castShadow,
                            float3 dirToLight, float rayStartOffset, rc_cast_pixel* out, int* shadowQueue,
-                           DevControl* ctl, cudaEvent_t between)
+                           DevControl* ctl, cudaEvent_t between, float4* shadowOrigins)
 {
     if (count <= 0)
         return cudaSuccess;
 #define RC_RAYCAST_ARGS li, sc, cam, rays, pixelStart, count, width, castShadow, dirToLight, rayStartOffset, out, \
-                        shadowQueue, ctl, between
+                        shadowQueue, ctl, between, shadowOrigins
     // two-level scenes: the top level nearest-first, like rc_cast's
     if (sc.numInstances > 0)
         return li.counting ? raycast_t<ORDER_NEAREST, true, false, true>(RC_RAYCAST_ARGS)

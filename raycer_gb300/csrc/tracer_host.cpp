@@ -1083,11 +1083,15 @@ rc_status rc_cast_with_shadow(rc_tracer* h, const rc_ray* rays, int64_t n, int32
         void* vo = vr ? device_view(h, out) : nullptr;
         if (vr && vo && ((reinterpret_cast<uintptr_t>(vr) | reinterpret_cast<uintptr_t>(vo)) & 15u) == 0)
         {
-            if ((s = ensure_bytes(h, &h->dTmpB, &h->capTmpB, size_t(n) * 2 * sizeof(int), "allocate shadow queue")) !=
-                RC_OK)
+            // shadow queue (8 B per entry) + the shadow rays' origins (16 B, device
+            // memory): the shadow kernel then reads nothing over the host link
+            const size_t queueBytes = (size_t(n) * 2 * sizeof(int) + 15) & ~size_t(15);
+            if ((s = ensure_bytes(h, &h->dTmpB, &h->capTmpB, queueBytes + size_t(n) * sizeof(float4),
+                                  "allocate shadow queue")) != RC_OK)
                 return s;
             s = raycast_into(h, static_cast<const rc_ray*>(vr), 0, uint64_t(n), order, static_cast<rc_cast_pixel*>(vo),
-                             static_cast<int*>(h->dTmpB));
+                             static_cast<int*>(h->dTmpB),
+                             reinterpret_cast<float4*>(static_cast<char*>(h->dTmpB) + queueBytes));
             h->stats.stage_ms[0] = h->stats.stage_ms[1] = 0.0;
             return s;
         }
@@ -1240,7 +1244,7 @@ namespace rcx
 {
 
 rc_status raycast_into(rc_tracer* h, const rc_ray* dRays, uint64_t pixelStart, uint64_t count, int order,
-                       rc_cast_pixel* dOut, int* dQueue)
+                       rc_cast_pixel* dOut, int* dQueue, float4* dOrigins)
 {
     float3 L = make_float3(0.0f, 0.0f, 0.0f);
     int castShadow = h->lights.empty() ? 0 : 1;
@@ -1256,7 +1260,8 @@ rc_status raycast_into(rc_tracer* h, const rc_ray* dRays, uint64_t pixelStart, u
         return s;
     RC_CUDA_TRY(h,
                 launch_raycast(launch_info(h), dev_scene(h), cam, dRays, pixelStart, int64_t(count), width, order,
-                               castShadow, L, h->general.ray_start_offset, dOut, dQueue, h->dCtl, h->evMid),
+                               castShadow, L, h->general.ray_start_offset, dOut, dQueue, h->dCtl, h->evMid,
+                               dOrigins),
                 "launch ray-cast kernels");
     return end_launch(h, "ray cast", true);
 }
