@@ -333,16 +333,19 @@ def run_ours(args, rank, local_rank, world):
     order = N.RC_ORDER_NEAREST if args.order == "nearest" else N.RC_ORDER_REFERENCE
     for _ in range(max(1, args.warmup)):
         assert N.lib().rc_cast_with_shadow(tracer.handle, rp, n_pix, order, op) == N.RC_OK
-    e2e_rays = 0
+    # the same rays every step: primary + shadow rays counted once, outside the timed loop
+    rays_per_call = tracer.stats()["rays_traced"]
+    cast_with_shadow = N.lib().rc_cast_with_shadow
+    handle = tracer.handle
     barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        st = N.lib().rc_cast_with_shadow(tracer.handle, rp, n_pix, order, op)
+        st = cast_with_shadow(handle, rp, n_pix, order, op)
         if st != N.RC_OK:
             raise RuntimeError(N.lib().rc_last_error(tracer.handle).decode())
-        e2e_rays += tracer.stats()["rays_traced"]
     barrier()
     e2e_sec = time.perf_counter() - t0
+    e2e_rays = rays_per_call * args.steps
 
     bvh = tracer.get_bvh() if rank == 0 else None
 
