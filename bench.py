@@ -55,6 +55,8 @@ def parse_args():
     ap.add_argument("--workload", choices=["raycast", "batch", "nrc", "build", "large", "path"], default="raycast",
                     help="raycast: the 1080p heightfield frame (default); batch: 64 rooms in one graph launch; "
                          "nrc: time to display RMSE 0.01, radiance cache vs plain path tracing")
+    ap.add_argument("--enclosed", action="store_true",
+                    help="nrc workload: the same geometry inside a closed box lit by an emissive panel, no sky")
     ap.add_argument("--gt-spp", type=int, default=4096, help="nrc / large: ground-truth samples per pixel")
     ap.add_argument("--scale", type=float, default=1.0, help="nrc: film scale (1 = 1920x1080)")
     ap.add_argument("--terminate-segment", type=int, default=2,
@@ -466,7 +468,7 @@ def run_nrc(args, rank, world):
 
     w, h = int(round(1920 * args.scale)), int(round(1080 * args.scale))
     t0 = time.perf_counter()
-    sc = scenes.heightfield_blobs_scene(width=w, height=h)
+    sc = scenes.heightfield_blobs_scene(width=w, height=h, enclosed=args.enclosed)
     build_s = time.perf_counter() - t0
     res = time_to_rmse(sc, target=0.01, gt_spp=args.gt_spp, max_frames=4096, max_seconds=90.0,
                        cache_config=dict(terminate_segment=args.terminate_segment),
@@ -484,7 +486,8 @@ def run_nrc(args, rank, world):
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "bf16 (MLP) / f32 (paths)",
         "data": "synthetic (seeded heightfield + blob instances)",
         "config": {"workload": f"radiance cache: heightfield + 200 blobs, {sc.triangle_count} tris, {w}x{h}, "
-                               "1 spp/frame, depth 12, sky-lit",
+                               "1 spp/frame, depth 12, " + ("inside a closed box lit by an emissive panel, no sky"
+                                                            if args.enclosed else "sky-lit"),
                    "gt_spp": res.gt_spp, "gt_seconds": round(res.gt_seconds, 1), "scene_build_s": round(build_s, 1),
                    "terminate_segment": args.terminate_segment},
         "plain": run_dict(res.plain), "cache": run_dict(res.cache),

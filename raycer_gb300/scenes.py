@@ -395,12 +395,17 @@ def _random_rotations(rng, count):
 
 def heightfield_blobs_scene(instances: int = 200, blob_level: int = 5, seed: int = 4, hf_nx: int = 1024,
                             hf_nz: int = 512, width: int = 1920, height: int = 1080,
-                            sky=(1.0, 1.0, 1.0)) -> SceneDesc:
+                            sky=(1.0, 1.0, 1.0), enclosed: bool = False) -> SceneDesc:
     """The radiance-cache workload: the 1,045,506-triangle heightfield (value
     noise seed 2) plus `instances` copies of one 20,480-triangle random blob at
     uniform random positions over the terrain, uniform random rotations,
     scale U(0.25, 0.6) and albedo U(0.1, 0.9)^3, flattened to world-space
-    triangles. Lit by a uniform sky: a path that escapes returns `sky`."""
+    triangles. Lit by a uniform sky: a path that escapes returns `sky`.
+
+    enclosed=True: the same geometry inside a closed box (x -14..14, y -1..8,
+    z -8..14, inward-facing walls of albedo 0.75, the camera inside) lit by an
+    emissive 10 x 5 panel of radiance 12 just under the ceiling, and no sky:
+    every path runs to the depth limit unless it reaches the panel."""
     hf = heightfield_scene(seed=2, nx=hf_nx, nz=hf_nz, width=width, height=height)
     blob = blob_mesh(seed=seed, level=blob_level).reshape(-1, 3, 3)
     rng = np.random.Generator(np.random.PCG64(seed))
@@ -420,9 +425,31 @@ def heightfield_blobs_scene(instances: int = 200, blob_level: int = 5, seed: int
     mats = [Material(diffuse=(0.6, 0.6, 0.6))] + [Material(diffuse=tuple(float(c) for c in a)) for a in albedo]
     midx = np.concatenate([np.zeros(hf.triangle_count, np.uint32),
                            np.repeat(np.arange(1, instances + 1, dtype=np.uint32), blob.shape[0])])
+    verts = np.concatenate([hf.vertices, bv])
+    name = f"heightfield + {instances} blobs x {blob.shape[0]} tris"
+    if enclosed:
+        x0, x1, y0, y1, z0, z1 = -14.0, 14.0, -1.0, 8.0, -8.0, 14.0
+        # (p0, u, v) with u x v pointing into the box, as room_scene's walls
+        dx, dy, dz = x1 - x0, y1 - y0, z1 - z0
+        walls = np.concatenate([
+            _quad((x0, y0, z0), (0, 0, dz), (dx, 0, 0)),   # floor, +y
+            _quad((x0, y1, z0), (dx, 0, 0), (0, 0, dz)),   # ceiling, -y
+            _quad((x0, y0, z0), (dx, 0, 0), (0, dy, 0)),   # back, +z
+            _quad((x0, y0, z1), (0, dy, 0), (dx, 0, 0)),   # front (behind the camera), -z
+            _quad((x0, y0, z0), (0, dy, 0), (0, 0, dz)),   # left, +x
+            _quad((x1, y0, z0), (0, 0, dz), (0, dy, 0)),   # right, -x
+        ])
+        panel = np.array(_quad((-5.0, y1 - 0.01, -2.5), (10.0, 0, 0), (0, 0, 5.0)))  # facing down, -y
+        mats = mats + [Material(diffuse=(0.75, 0.75, 0.75)),
+                       Material(diffuse=(0.0, 0.0, 0.0), emittance=(12.0, 12.0, 12.0), is_emissive=True)]
+        wall_id, light_id = len(mats) - 2, len(mats) - 1
+        verts = np.concatenate([verts, _f32(walls), _f32(panel)])
+        midx = np.concatenate([midx, np.full(walls.shape[0], wall_id, np.uint32),
+                               np.full(panel.shape[0], light_id, np.uint32)])
+        name += ", enclosed, emissive panel"
     return SceneDesc(
-        name=f"heightfield + {instances} blobs x {blob.shape[0]} tris",
-        vertices=np.concatenate([hf.vertices, bv]),
+        name=name,
+        vertices=verts,
         material_index=midx,
         materials=mats,
         camera=hf.camera,
@@ -431,7 +458,7 @@ def heightfield_blobs_scene(instances: int = 200, blob_level: int = 5, seed: int
         light_direction=None,
         max_leaf_size=4,
         settings=dict(tracer="path", max_path_length=12, multi_sample_count_sqrt=1, path_sample_count=1,
-                      sampler="cmj", miss_radiance=tuple(sky)),
+                      sampler="cmj", miss_radiance=None if enclosed else tuple(sky)),
     )
 
 
