@@ -40,7 +40,10 @@ struct __align__(16) DevNode
     float4 xy0;  // child 0: lo.x, hi.x, lo.y, hi.y
     float4 xy1;  // child 1: lo.x, hi.x, lo.y, hi.y
     float4 z01;  // child 0 lo.z, hi.z; child 1 lo.z, hi.z
-    int4 link;   // child 0 (left), child 1 (right), depth-first subtree end, reserved
+    int4 link;   // child 0 (left), child 1 (right), next, reserved. next: the node whose right
+                 // child the reference's preorder visits after this node's subtree (the
+                 // lowest ancestor with this node in its left subtree), -1 after the last
+                 // (thread_nodes; the stackless walk of traverse_stackless)
 };
 
 struct __align__(16) DevNode4

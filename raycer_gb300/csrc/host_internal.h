@@ -197,6 +197,9 @@ void release_scene_data(rc_tracer* h);
 // uploads it (h->dWide); leaves it out where its stack need exceeds the
 // traversal stack. Failure to allocate is an error.
 rc_status upload_wide(rc_tracer* h, const std::vector<DevNode>& nodes, int32_t rootLink);
+// Sets each inner node's next link (DevNode::link.z) for the stackless
+// reference-order walk.
+void thread_nodes(std::vector<DevNode>& dn, int32_t rootLink);
 // Builds the 4-wide BVH of the handle's single-level scene on first use (the
 // first PATH or batch render of a scene): downloads the binary nodes once,
 // collapses and uploads them. Uploads and RAY frames do not pay for it.

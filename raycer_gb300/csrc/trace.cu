@@ -68,7 +68,7 @@ __device__ __forceinline__ int caller_index(const DevScene& sc, int slot)
     return __float_as_int(__ldg(&sc.tris[slot].c.z));
 }
 
-template <bool ANY, int ORDER, bool COUNT>
+template <bool ANY, int ORDER, bool COUNT, bool SL>
 __global__ void __launch_bounds__(kBlock, RC_TRACE_MIN_BLOCKS) k_cast(DevScene sc, const rc_ray* __restrict__ rays, int n,
                                                  rc_hit* __restrict__ hits, DevControl* ctl)
 {
@@ -88,7 +88,9 @@ __global__ void __launch_bounds__(kBlock, RC_TRACE_MIN_BLOCKS) k_cast(DevScene s
             float4 r1 = __ldg(rp + 1);
             RayF ray = make_ray(v3(r0.x, r0.y, r0.z), v3(r1.x, r1.y, r1.z), r0.w, r1.w);
             HitF h{ -1, FLT_MAX, 0.0f, 0.0f, -1 };
-            bool found = traverse_scene<ANY, ORDER, COUNT>(sc, ray, h, cnt, err, -1, -1);
+            // SL: the reference order of a single-level scene on the threaded tree
+            bool found = SL ? traverse_stackless<ANY>(sc, ray, h, -1)
+                            : traverse_scene<ANY, ORDER, COUNT>(sc, ray, h, cnt, err, -1, -1);
             int4 out;
             // two-level scenes: the flattened index (instance's first + mesh-local)
             out.x = found ? caller_index(sc, h.slot) + (h.inst >= 0 ? __ldg(&sc.instances[h.inst].primBase) : 0) : -1;
@@ -234,7 +236,7 @@ __global__ void __launch_bounds__(kBlock, RC_TRACE_MIN_BLOCKS) k_raycast_primary
 // (Raytracer::calculateShadowAmount, Raytracer.cpp:497-522 /
 // lighting.cl:28-48): origin = hit position + dirToLight * rayStartOffset;
 // the primary hit's own triangle is skipped (see traverse.cuh).
-template <bool COUNT, bool INST>
+template <bool COUNT, bool INST, bool SL>
 __global__ void __launch_bounds__(kBlock, RC_TRACE_MIN_BLOCKS) k_raycast_shadow(DevScene sc, DevCamera cam, const rc_ray* __restrict__ rays,
                                                            uint64_t pixelStart, int64_t width, float3 L,
                                                            float rayStartOffset, rc_cast_pixel* __restrict__ out,
@@ -279,6 +281,8 @@ __global__ void __launch_bounds__(kBlock, RC_TRACE_MIN_BLOCKS) k_raycast_shadow(
             bool occ;
             if (INST)
                 occ = traverse_instanced<true, COUNT>(sc, sr, h, cnt, err, e.y, skipInst);
+            else if (SL)
+                occ = traverse_stackless<true>(sc, sr, h, e.y);  // the same first occluder, no stack
             else
                 occ = traverse<true, ORDER_REF, COUNT>(sc, sr, h, cnt, err, e.y);
             out[i].occluder = occ ? caller_index(sc, h.slot) + (INST ? __ldg(&sc.instances[h.inst].primBase) : 0) : -1;
@@ -298,11 +302,11 @@ int persistent_blocks(K kernel, int numSMs)
     return perSM * numSMs;
 }
 
-template <bool ANY, int ORDER, bool COUNT>
+template <bool ANY, int ORDER, bool COUNT, bool SL = false>
 cudaError_t cast_t(const LaunchInfo& li, const DevScene& sc, const rc_ray* rays, int64_t n, rc_hit* hits,
                    DevControl* ctl)
 {
-    auto k = k_cast<ANY, ORDER, COUNT>;
+    auto k = k_cast<ANY, ORDER, COUNT, SL>;
     static int grid = 0;
     if (grid == 0)
         grid = persistent_blocks(k, li.numSMs);
@@ -335,13 +339,26 @@ bool whole_frame(uint64_t pixelStart, int64_t count, int64_t width)
     return RC_TRACE_TILES && pixelStart == 0 && width >= 8 && count / width >= 4 && (count / width) * width == count;
 }
 
-template <int ORDER, bool COUNT, bool PACKET, bool INST>
+// Whether the reference-order queries of uncounted frames (the RAY frame's
+// shadow rays, rc_cast in RC_ORDER_REFERENCE) walk the threaded tree without
+// a stack (RC_STACKLESS=1; read once). The same hits; measured slower on the
+// 1080p heightfield's shadow rays (0.279 vs 0.169 ms), so off by default.
+bool stackless()
+{
+    static const bool on = [] {
+        const char* v = std::getenv("RC_STACKLESS");
+        return v && v[0] == '1';
+    }();
+    return on;
+}
+
+template <int ORDER, bool COUNT, bool PACKET, bool INST, bool SL = false>
 cudaError_t raycast_t(const LaunchInfo& li, const DevScene& sc, const DevCamera& cam, const rc_ray* rays,
                       uint64_t pixelStart, int64_t count, int64_t width, int castShadow, float3 L, float off,
                       rc_cast_pixel* out, int* queue, DevControl* ctl, cudaEvent_t between, float4* origins)
 {
     auto kp = k_raycast_primary<ORDER, COUNT, PACKET, INST>;
-    auto ks = k_raycast_shadow<COUNT, INST>;
+    auto ks = k_raycast_shadow<COUNT, INST, SL>;
     static int gp = 0, gs = 0;
     if (gp == 0)
         gp = persistent_blocks(kp, li.numSMs);
@@ -369,13 +386,16 @@ cudaError_t launch_cast(const LaunchInfo& li, const DevScene& sc, const rc_ray* 
 {
     if (n <= 0)
         return cudaSuccess;
+    const bool sl = !li.counting && sc.numInstances == 0 && stackless();
     if (anyHit)
         return li.counting ? cast_t<true, ORDER_REF, true>(li, sc, rays, n, hits, ctl)
+               : sl        ? cast_t<true, ORDER_REF, false, true>(li, sc, rays, n, hits, ctl)
                            : cast_t<true, ORDER_REF, false>(li, sc, rays, n, hits, ctl);
     if (order == ORDER_NEAREST)
         return li.counting ? cast_t<false, ORDER_NEAREST, true>(li, sc, rays, n, hits, ctl)
                            : cast_t<false, ORDER_NEAREST, false>(li, sc, rays, n, hits, ctl);
     return li.counting ? cast_t<false, ORDER_REF, true>(li, sc, rays, n, hits, ctl)
+           : sl        ? cast_t<false, ORDER_REF, false, true>(li, sc, rays, n, hits, ctl)
                        : cast_t<false, ORDER_REF, false>(li, sc, rays, n, hits, ctl);
 }
 
@@ -396,6 +416,14 @@ cudaError_t launch_raycast(const LaunchInfo& li, const DevScene& sc, const DevCa
         return order == ORDER_NEAREST ? raycast_t<ORDER_NEAREST, true, false, false>(RC_RAYCAST_ARGS)
                                       : raycast_t<ORDER_REF, true, false, false>(RC_RAYCAST_ARGS);
     const int packets = trace_packets();
+    if (stackless())
+    {
+        if (whole_frame(pixelStart, count, width) && (packets == 2 || (packets == 1 && !rays)))
+            return order == ORDER_NEAREST ? raycast_t<ORDER_NEAREST, false, true, false, true>(RC_RAYCAST_ARGS)
+                                          : raycast_t<ORDER_REF, false, true, false, true>(RC_RAYCAST_ARGS);
+        return order == ORDER_NEAREST ? raycast_t<ORDER_NEAREST, false, false, false, true>(RC_RAYCAST_ARGS)
+                                      : raycast_t<ORDER_REF, false, false, false, true>(RC_RAYCAST_ARGS);
+    }
     if (whole_frame(pixelStart, count, width) && (packets == 2 || (packets == 1 && !rays)))
         return order == ORDER_NEAREST ? raycast_t<ORDER_NEAREST, false, true, false>(RC_RAYCAST_ARGS)
                                       : raycast_t<ORDER_REF, false, true, false>(RC_RAYCAST_ARGS);

@@ -266,6 +266,25 @@ void device_nodes(const std::vector<BuildNode>& nodes, std::vector<DevNode>& dn,
     }
     rootLink = nodes[0].rightOffset != 0 ? 0 : link(0);
     inner = uint64_t(count);
+    thread_nodes(dn, rootLink);
+}
+
+void thread_nodes(std::vector<DevNode>& dn, int32_t rootLink)
+{
+    if (rootLink < 0 || dn.empty())
+        return;
+    std::vector<std::pair<int32_t, int32_t>> work{ { rootLink, -1 } };  // (node, its next)
+    while (!work.empty())
+    {
+        const auto [p, next] = work.back();
+        work.pop_back();
+        DevNode& d = dn[size_t(p)];
+        d.link.z = next;
+        if (d.link.y >= 0)
+            work.push_back({ d.link.y, next });  // after the right subtree: p's own next
+        if (d.link.x >= 0)
+            work.push_back({ d.link.x, p });     // after the left subtree: p's right child
+    }
 }
 
 // Triangle, shading and material records of a scene in BVH order.

@@ -204,6 +204,100 @@ __device__ __forceinline__ bool traverse(const DevScene& sc, const RayF& ray, Hi
     }
 }
 
+// The reference's order without a stack: the tree is threaded (each inner
+// node's link.z names the node whose right child follows its subtree in the
+// preorder; tracer_host.cpp thread_nodes). At (node p, side s) the walk tests
+// child s's box; a hit inner child is entered at its left side, a hit leaf's
+// triangles are tested in order; then the walk moves to p's right side, or,
+// after the right side, to (next of p, right side). Each ray meets the
+// boxes and triangles of traverse<ANY_HIT, ORDER_REF> in the same order, so
+// it returns the same closest hit (ties to the later triangle) or the same
+// first any-hit; a node is fetched when entered and again when the walk
+// returns to its right side, instead of being pushed and popped.
+template <bool ANY_HIT>
+__device__ __forceinline__ bool traverse_stackless(const DevScene& sc, const RayF& ray, HitF& hit, int skip)
+{
+    bool found = false;
+    int p = sc.rootLink;
+    int side = 0;
+    if (p < 0)
+    {
+        // a leaf root: its triangles only
+        side = 2;
+    }
+    float4 a, b, c;
+    int4 l;
+    if (p >= 0)
+        load_node(sc.nodes, p, a, b, c, l);
+    while (true)
+    {
+        int child;
+        bool hitBox;
+        if (side == 2)
+        {
+            child = p;  // the leaf root
+            hitBox = true;
+        }
+        else
+        {
+            float e;
+            const float lox = side ? b.x : a.x, hix = side ? b.y : a.y, loy = side ? b.z : a.z, hiy = side ? b.w : a.w;
+            const float loz = side ? c.z : c.x, hiz = side ? c.w : c.y;
+            hitBox = ray.finite ? slab_finite(ray, lox, hix, loy, hiy, loz, hiz, e) : slab(ray, lox, hix, loy, hiy, loz, hiz, e);
+            child = side ? l.y : l.x;
+        }
+        if (hitBox)
+        {
+            if (child >= 0)
+            {
+                p = child;
+                side = 0;
+                load_node(sc.nodes, p, a, b, c, l);
+                continue;
+            }
+            const int leaf = ~child;
+            const int start = leaf >> kLeafCountBits;
+            const int count = leaf & ((1 << kLeafCountBits) - 1);
+            for (int i = 0; i < count; ++i)
+            {
+                const int slot = start + i;
+                if (slot == skip)
+                    continue;
+                const float4* tp = reinterpret_cast<const float4*>(sc.tris + slot);
+                const float4 ta = __ldg(tp + 0);
+                const float4 tb = __ldg(tp + 1);
+                const float4 tc = __ldg(tp + 2);
+                if (ANY_HIT && (__float_as_uint(tc.y) & kMetaNonShadowing))
+                    continue;
+                float t, u, v;
+                if (tri_hit(ray, v3(ta.x, ta.y, ta.z), v3(ta.w, tb.x, tb.y), v3(tb.z, tb.w, tc.x), t, u, v) &&
+                    (ANY_HIT || !(t > hit.t)))
+                {
+                    hit.slot = slot;
+                    hit.t = t;
+                    hit.u = u;
+                    hit.v = v;
+                    found = true;
+                    if (ANY_HIT)
+                        return true;
+                }
+            }
+        }
+        // advance: the right side of p, or the right side of p's next
+        if (side == 0)
+        {
+            side = 1;
+            continue;
+        }
+        if (side == 2)
+            return found;
+        p = l.z;
+        if (p < 0)
+            return found;
+        load_node(sc.nodes, p, a, b, c, l);
+    }
+}
+
 // Entry distance of one child box of a wide node, or +inf when the ray misses
 // it or enters it beyond `limit` (the current closest hit).
 __device__ __forceinline__ float wide_entry(const RayF& ray, float lox, float hix, float loy, float hiy, float loz,
