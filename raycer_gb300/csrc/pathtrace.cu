@@ -47,7 +47,7 @@ namespace
 #endif
 // The same for the 4-wide traversal (four boxes per node in registers).
 #ifndef RC_EXTEND_WIDE_MIN_BLOCKS
-#define RC_EXTEND_WIDE_MIN_BLOCKS 8
+#define RC_EXTEND_WIDE_MIN_BLOCKS 9
 #endif
 
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
