@@ -45,6 +45,10 @@ namespace
 #ifndef RC_EXTEND_MIN_BLOCKS
 #define RC_EXTEND_MIN_BLOCKS 10
 #endif
+// The same for the two-level extend kernel.
+#ifndef RC_EXTEND_INST_MIN_BLOCKS
+#define RC_EXTEND_INST_MIN_BLOCKS 8
+#endif
 // The same for the 4-wide traversal (four boxes per node in registers).
 #ifndef RC_EXTEND_WIDE_MIN_BLOCKS
 #define RC_EXTEND_WIDE_MIN_BLOCKS 9
@@ -237,7 +241,7 @@ __global__ void __launch_bounds__(BLOCK, ((ORDER == ORDER_WIDE ? RC_EXTEND_WIDE_
 // Extend for passes with two-level scenes: 32 queue entries per warp fetch,
 // each ray traced in one go.
 template <bool COUNT>
-__global__ void __launch_bounds__(128) k_extend_instanced(PassParams p, int segment)
+__global__ void __launch_bounds__(128, RC_EXTEND_INST_MIN_BLOCKS) k_extend_instanced(PassParams p, int segment)
 {
     const unsigned total = *reinterpret_cast<volatile unsigned*>(&p.counts[segment * 4 + 0]);
     const int* __restrict__ queue = (segment & 1) ? p.qb : p.qa;
