@@ -87,3 +87,76 @@ def test_cast_with_shadow_host_buffers_equal_frame(copy, monkeypatch):
         stats = t.stats()
     assert np.array_equal(out, frame)
     assert stats["rays_traced"] == n + int((frame["prim"] >= 0).sum())
+
+
+def _edge_rays():
+    """Rays at the slab and triangle tests' edge cases: axis-aligned
+    directions (two zero components: infinite inverse components of both
+    signs, including -0.0), one zero component, origins on the room's wall
+    planes and inside the walls, rays lying in a wall's plane (det = 0),
+    directions aimed at triangle vertices, empty and reversed t windows,
+    and NaN components."""
+    rng = np.random.default_rng(11)
+    rays = []
+    axes = np.eye(3, dtype=np.float32)
+    for s in (1.0, -1.0):
+        for a in range(3):
+            d = s * axes[a]
+            for _ in range(400):
+                o = rng.uniform(-0.9, 0.9, 3).astype(np.float32)
+                rays.append((o, d, 0.0, 3.0e38))
+            dz = d.copy()
+            dz[dz == 0] = -0.0  # zero components of the other sign
+            for _ in range(100):
+                rays.append((rng.uniform(-0.9, 0.9, 3).astype(np.float32), dz, 0.0, 3.0e38))
+    for _ in range(600):  # one zero component
+        d = rng.normal(size=3).astype(np.float32)
+        d[rng.integers(0, 3)] = 0.0
+        rays.append((rng.uniform(-0.9, 0.9, 3).astype(np.float32), d / np.linalg.norm(d), 0.0, 3.0e38))
+    for _ in range(600):  # origins on the wall planes x, y, z = -1 / +1
+        o = rng.uniform(-0.9, 0.9, 3).astype(np.float32)
+        o[rng.integers(0, 3)] = np.float32(rng.choice([-1.0, 1.0]))
+        d = rng.normal(size=3).astype(np.float32)
+        rays.append((o, d / np.linalg.norm(d), 0.0, 3.0e38))
+    for _ in range(300):  # in the plane of the floor (y = -1) and of the back wall (z = -1)
+        o = np.array([rng.uniform(-0.9, 0.9), -1.0, rng.uniform(-0.9, 0.9)], np.float32)
+        d = np.array([rng.normal(), 0.0, rng.normal()], np.float32)
+        rays.append((o, d / np.linalg.norm(d), 0.0, 3.0e38))
+        o = np.array([rng.uniform(-0.9, 0.9), rng.uniform(-0.9, 0.9), -1.0], np.float32)
+        d = np.array([rng.normal(), rng.normal(), 0.0], np.float32)
+        rays.append((o, d / np.linalg.norm(d), 0.0, 3.0e38))
+    corners = np.array([[-1, -1, -1], [1, -1, -1], [-1, 1, -1], [1, 1, -1], [-1, -1, 1], [1, -1, 1]], np.float32)
+    for c in corners:  # at wall corners (triangle vertices)
+        for _ in range(50):
+            o = rng.uniform(-0.5, 0.5, 3).astype(np.float32)
+            d = c - o
+            rays.append((o, d / np.linalg.norm(d), 0.0, 3.0e38))
+    for _ in range(200):  # empty / reversed windows
+        d = rng.normal(size=3).astype(np.float32)
+        t0 = np.float32(rng.uniform(0.0, 2.0))
+        rays.append((rng.uniform(-0.9, 0.9, 3).astype(np.float32), d / np.linalg.norm(d), t0, t0 * np.float32(0.5)))
+    nan = np.float32(np.nan)
+    for o, d in (((nan, 0, 0), (0, 0, -1)), ((0, 0, 0), (nan, 0, -1)), ((0, 0, 0), (nan, nan, nan))):
+        rays.append((np.array(o, np.float32), np.array(d, np.float32), 0.0, 3.0e38))
+    out = np.zeros(len(rays), dtype=[("origin", "<f4", 3), ("t_min", "<f4"), ("direction", "<f4", 3),
+                                     ("t_max", "<f4")])
+    for i, (o, d, t0, t1) in enumerate(rays):
+        out[i] = (o, t0, d, t1)
+    return out
+
+
+@pytest.mark.parametrize("any_hit", [False, True])
+@pytest.mark.parametrize("order", [N.RC_ORDER_REFERENCE, N.RC_ORDER_NEAREST])
+def test_cast_edge_rays_bit_exact(any_hit, order):
+    sc = small_room(clutter=500)
+    rays = _edge_rays()
+    with CudaTracer(0) as t:
+        t.initializeBuffers(sc)
+        hits = t.cast(rays, any_hit=any_hit, order=order)
+    prim, tt, u, v, _ = oracle.Oracle(sc).cast32(rays, any_hit=any_hit, order=order)
+    assert (prim >= 0).mean() > 0.5
+    assert np.array_equal(hits["prim"], prim), int((hits["prim"] != prim).sum())
+    same_t = (hits["t"] == tt) | (np.isnan(hits["t"]) & np.isnan(tt))
+    assert same_t.all()
+    for g, r in ((hits["u"], u), (hits["v"], v)):
+        assert ((g == r) | (np.isnan(g) & np.isnan(r))).all()
