@@ -386,7 +386,9 @@ def run_ours(args, rank, local_rank, world):
                          "algorithmic_bytes_per_launch": int(prim_bytes),
                          "avg_launch_ms": round(prim_avg * 1e3, 4),
                          "traffic": traffic,
-                         "node_fetches": int(s0_nodes), "triangle_tests": int(s0_tris)},
+                         "node_fetches": int(s0_nodes), "triangle_tests": int(s0_tris),
+                         # BVH-node bytes (64 B per inner-node fetch) per second of the primary kernel
+                         "bvh_node_gbs": round(s0_nodes * 64 / prim_avg / 1e9, 1)},
             "stages_ms": {"primary": round(statistics.mean(prim_ms), 4), "shadow": round(statistics.mean(shadow_ms), 4)},
             "wall_s": round(t_wall, 3),
             "clocks": clocks.summary(),
