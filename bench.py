@@ -48,8 +48,9 @@ WORKLOAD = "heightfield ray cast 1920x1080: primary closest hit + directional sh
 def parse_args():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
-    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default 200; batch: 5, each step one 64-scene frame of about 4 s)")
+    ap.add_argument("--warmup", type=int, default=None, help="untimed warm-up steps (default 10; batch: 3)")
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--order", choices=["nearest", "reference"], default="nearest")
     ap.add_argument("--workload", choices=["raycast", "batch", "nrc", "build", "large", "path", "cpu"], default="raycast",
@@ -61,7 +62,12 @@ def parse_args():
     ap.add_argument("--scale", type=float, default=1.0, help="nrc: film scale (1 = 1920x1080)")
     ap.add_argument("--terminate-segment", type=int, default=2,
                     help="nrc: paths end into the cache at the hit of this segment")
-    return ap.parse_args()
+    args = ap.parse_args()
+    if args.steps is None:
+        args.steps = 5 if args.workload == "batch" else 200
+    if args.warmup is None:
+        args.warmup = 3 if args.workload == "batch" else 10
+    return args
 
 
 def dist_env():
