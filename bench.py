@@ -158,9 +158,12 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def profiled_traffic():
-    """DRAM bytes per launch of the primary kernel from the committed ncu summary."""
-    f = ROOT / "profiles" / "raycast_primary_heightfield_1080p.md"
+def profiled_traffic(fused=False):
+    """DRAM bytes per launch of the frame's dominant kernel (the one-kernel
+    frame of primary + shadow rays, or the two-stage frame's primary kernel)
+    from the committed ncu summary, or None."""
+    f = ROOT / "profiles" / ("raycast_frame_fused_heightfield_1080p.md" if fused
+                             else "raycast_primary_heightfield_1080p.md")
     if not f.exists():
         return None
     m = re.search(r"dram_bytes_per_launch:\s*([0-9.eE+]+)", f.read_text())
@@ -372,10 +375,20 @@ def run_ours(args, rank, local_rank, world):
         peak, peak_kind = measured_peaks()
         s0_nodes, s0_tris = counted["stage_nodes"][0], counted["stage_tris"][0]
         hits = counted["stage_rays"][1]
-        prim_bytes = 64 * s0_nodes + 48 * s0_tris + 16 * n_pix + 8 * hits
+        # One kernel per frame (shadow rays traced where the primary hit was
+        # found; the shadow stage's time is then 0): its bytes are both
+        # stages' node and triangle fetches + the records, written once.
+        fused = statistics.mean(shadow_ms) == 0.0
+        if fused:
+            k_nodes = s0_nodes + counted["stage_nodes"][1]
+            k_tris = s0_tris + counted["stage_tris"][1]
+            prim_bytes = 64 * k_nodes + 48 * k_tris + 16 * n_pix
+        else:
+            k_nodes, k_tris = s0_nodes, s0_tris
+            prim_bytes = 64 * s0_nodes + 48 * s0_tris + 16 * n_pix + 8 * hits
         prim_avg = statistics.mean(prim_ms) / 1e3
         achieved = prim_bytes / prim_avg / 1e9
-        traffic = profiled_traffic()
+        traffic = profiled_traffic(fused)
         line = {
             "metric": METRIC, "value": round(total_rays / dev_sec / 1e6, 2), "unit": METRIC,
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -386,15 +399,18 @@ def run_ours(args, rank, local_rank, world):
                        "parallelism": f"replicas x{world}"},
             "e2e": {"value": round(e2e_rays / e2e_sec / 1e6, 2), "unit": METRIC,
                     "h2d_bytes_per_step": n_pix * 32, "d2h_bytes_per_step": n_pix * 16},
-            "gpu_launches": 2 * args.steps,
-            "roofline": {"bound": "hbm", "kernel": "k_raycast_primary (closest hit)", "achieved": round(achieved, 1),
+            "gpu_launches": (1 if fused else 2) * args.steps,
+            "roofline": {"bound": "hbm",
+                         "kernel": "k_raycast_primary (closest hit + shadow any-hit, one kernel)" if fused
+                         else "k_raycast_primary (closest hit)",
+                         "achieved": round(achieved, 1),
                          "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
                          "algorithmic_bytes_per_launch": int(prim_bytes),
                          "avg_launch_ms": round(prim_avg * 1e3, 4),
                          "traffic": traffic,
-                         "node_fetches": int(s0_nodes), "triangle_tests": int(s0_tris),
-                         # BVH-node bytes (64 B per inner-node fetch) per second of the primary kernel
-                         "bvh_node_gbs": round(s0_nodes * 64 / prim_avg / 1e9, 1)},
+                         "node_fetches": int(k_nodes), "triangle_tests": int(k_tris),
+                         # BVH-node bytes (64 B per inner-node fetch) per second of the kernel
+                         "bvh_node_gbs": round(k_nodes * 64 / prim_avg / 1e9, 1)},
             "stages_ms": {"primary": round(statistics.mean(prim_ms), 4), "shadow": round(statistics.mean(shadow_ms), 4)},
             "wall_s": round(t_wall, 3),
             "clocks": clocks.summary(),

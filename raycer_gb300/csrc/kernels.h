@@ -35,14 +35,21 @@ cudaError_t launch_cast(const LaunchInfo& li, const DevScene& sc, const rc_ray* 
 // Primary rays come from the camera (rays == nullptr) or from `rays`
 // (one per pixel, caller order). Writes out[0..count); shadowQueue needs
 // 2 * `count` ints (pixel, hit slot). ctl->head[0], head[1], head[2] must be zero on entry.
+// Uncounted frames with a light run as one kernel by default (each shadow
+// ray traced where its primary hit was found; no queue); counted frames and
+// RC_TRACE_FUSED=0 run the primary and the shadow kernel, with `between`
+// recorded between them. *kernels (optional) receives the number of kernels
+// launched (0 for an empty frame).
 cudaError_t launch_raycast(const LaunchInfo& li, const DevScene& sc, const DevCamera& cam, const rc_ray* rays,
                            uint64_t pixelStart, int64_t count, int64_t width, int order, int castShadow,
                            float3 dirToLight, float rayStartOffset, rc_cast_pixel* out, int* shadowQueue,
-                           DevControl* ctl, cudaEvent_t between, float4* shadowOrigins = nullptr);
-// shadowOrigins (optional, device memory, one float4 per queue entry): the
-// primary kernel stores each hit pixel's shadow-ray origin there (and, in a
-// two-level scene, the hit's instance in w), so the shadow kernel reads
-// neither the caller's rays nor the records again: for rays and records in
-// host memory, that is the host-link traffic of a second pass.
+                           DevControl* ctl, cudaEvent_t between, float4* shadowOrigins = nullptr,
+                           int* kernels = nullptr);
+// shadowOrigins (optional, device memory, one float4 per queue entry): in
+// the two-kernel form the primary kernel stores each hit pixel's shadow-ray
+// origin there (and, in a two-level scene, the hit's instance in w), so the
+// shadow kernel reads neither the caller's rays nor the records again: for
+// rays and records in host memory, that is the host-link traffic of a
+// second pass.
 
 }  // namespace rcx

@@ -120,6 +120,28 @@ __device__ __forceinline__ RayF primary_ray(const DevCamera& cam, const rc_ray* 
     return make_ray(v3(cam.pos[0], cam.pos[1], cam.pos[2]), d, 0.0f, FLT_MAX);
 }
 
+// The shadow ray of a primary hit, traced where the hit was found: the
+// arithmetic of stage 2 below (origin = o + t d, then + L * rayStartOffset;
+// the hit's own triangle, of its instance, skipped). Completes the record:
+// occluder and flags.
+template <bool INST, bool SL>
+__device__ __forceinline__ void shadow_of(const DevScene& sc, const RayF& ray, const HitF& h, float3 L,
+                                          float rayStartOffset, int4& o, TravCount& cnt, int& err)
+{
+    const V3 dl = v3(L.x, L.y, L.z);
+    const RayF sr = make_ray(vfma(dl, rayStartOffset, vfma(ray.d, h.t, ray.o)), dl, 0.0f, FLT_MAX);
+    HitF s{ -1, FLT_MAX, 0.0f, 0.0f, -1 };
+    bool occ;
+    if (INST)
+        occ = traverse_instanced<true, false>(sc, sr, s, cnt, err, h.slot, h.inst);
+    else if (SL)
+        occ = traverse_stackless<true>(sc, sr, s, h.slot);
+    else
+        occ = traverse<true, ORDER_REF, false>(sc, sr, s, cnt, err, h.slot);
+    o.z = occ ? caller_index(sc, s.slot) + (INST ? __ldg(&sc.instances[s.inst].primBase) : 0) : -1;
+    o.w = 1 | 2 | (occ ? 4 : 0);
+}
+
 // Stage 1 of the RAY frame: closest hit of every pixel's primary ray.
 // Whole frames (tilesX > 0: camera rays, or caller rays one per pixel) are
 // walked in 8x4-pixel tiles, one tile per warp fetch, so a warp's rays are
@@ -130,7 +152,14 @@ __device__ __forceinline__ RayF primary_ray(const DevCamera& cam, const rc_ray* 
 // record's prim is the flattened index, instance's first + mesh-local, and
 // while a shadow ray is to follow its occluder field holds the hit's
 // instance, for the shadow ray to skip the hit triangle of that instance).
-template <int ORDER, bool COUNT, bool PACKET, bool INST>
+// FUSED (uncounted frames with a light): each lane whose ray hit traces its
+// shadow ray right after the tile's primary rays, with the shadow kernel's
+// arithmetic (stage 2 below; SL: the threaded walk), and the pixel's record
+// is written once, complete; no queue. The shadow rays of a tile whose
+// pixels all hit (or all miss) keep the warp full (or cost nothing); only
+// tiles on a silhouette leave lanes idle. With the caller's rays in host
+// memory the shadow work then overlaps the ray reads over the host link.
+template <int ORDER, bool COUNT, bool PACKET, bool INST, bool FUSED = false, bool SL = false>
 __global__ void __launch_bounds__(kBlock, RC_TRACE_MIN_BLOCKS) k_raycast_primary(DevScene sc, DevCamera cam, const rc_ray* __restrict__ rays,
                                                             uint64_t pixelStart, int64_t count, int64_t width,
                                                             int64_t height, int64_t tilesX, int castShadow,
@@ -138,6 +167,9 @@ __global__ void __launch_bounds__(kBlock, RC_TRACE_MIN_BLOCKS) k_raycast_primary
                                                             DevControl* ctl, float3 L, float rayStartOffset,
                                                             float4* __restrict__ origins)
 {
+    static_assert(!(FUSED && COUNT), "counted frames keep the two stages");
+    TravCount cnt1{ 0, 0 };  // FUSED: the shadow rays' counts
+    unsigned long long done1 = 0;
     __shared__ PacketEntry wstack[PACKET ? kWarpsPerBlock : 1][PACKET ? kMaxStack : 1];
     TravCount cnt{ 0, 0 };
     int err = 0;
@@ -167,7 +199,23 @@ __global__ void __launch_bounds__(kBlock, RC_TRACE_MIN_BLOCKS) k_raycast_primary
             RayF ray = primary_ray(cam, rays, valid ? pixelStart + uint64_t(i) : pixelStart, valid ? i : 0, width);
             HitF h{ -1, FLT_MAX, 0.0f, 0.0f, -1 };
             bool found = traverse_packet<ORDER>(sc, ray, h, err, -1, valid, wstack[threadIdx.x >> 5]);
-            if (valid)
+            if (FUSED)
+            {
+                int4 o;
+                o.x = found ? caller_index(sc, h.slot) : -1;
+                o.y = __float_as_int(found ? h.t : -1.0f);
+                o.z = -1;
+                o.w = found ? 1 : 0;
+                if (valid && found)
+                    shadow_of<false, SL>(sc, ray, h, L, rayStartOffset, o, cnt1, err);
+                if (valid)
+                {
+                    reinterpret_cast<int4*>(out)[i] = o;
+                    done++;
+                    done1 += found ? 1 : 0;
+                }
+            }
+            else if (valid)
             {
                 int4 o;
                 o.x = found ? caller_index(sc, h.slot) : -1;
@@ -199,21 +247,29 @@ __global__ void __launch_bounds__(kBlock, RC_TRACE_MIN_BLOCKS) k_raycast_primary
             int4 o;
             o.x = found ? caller_index(sc, h.slot) + (INST ? __ldg(&sc.instances[h.inst].primBase) : 0) : -1;
             o.y = __float_as_int(found ? h.t : -1.0f);
-            o.z = INST && found && castShadow ? h.inst : -1;
-            if (origins && found && castShadow)
+            o.z = INST && found && castShadow && !FUSED ? h.inst : -1;
+            o.w = found ? 1 : 0;
+            if (FUSED)
+            {
+                if (found)
+                {
+                    shadow_of<INST, SL>(sc, ray, h, L, rayStartOffset, o, cnt1, err);
+                    done1++;
+                }
+            }
+            else if (origins && found && castShadow)
             {
                 const V3 dl = v3(L.x, L.y, L.z);
                 const V3 so = vfma(dl, rayStartOffset, vfma(ray.d, h.t, ray.o));
                 sorg = make_float4(so.x, so.y, so.z, __int_as_float(INST ? h.inst : -1));
             }
-            o.w = found ? 1 : 0;
             reinterpret_cast<int4*>(out)[i] = o;
-            hitAny = found && castShadow;
+            hitAny = found && castShadow && !FUSED;
             hitSlot = h.slot;
             done++;
         }
         // Warp-aggregated compaction of the hit pixels into the shadow queue.
-        unsigned mask = __ballot_sync(0xffffffffu, hitAny);
+        unsigned mask = FUSED ? 0u : __ballot_sync(0xffffffffu, hitAny);
         if (mask)
         {
             unsigned qbase = 0;
@@ -230,6 +286,8 @@ __global__ void __launch_bounds__(kBlock, RC_TRACE_MIN_BLOCKS) k_raycast_primary
         }
     }
     flush_counts(ctl, 0, done, cnt, err);
+    if (FUSED)
+        flush_counts(ctl, 1, done1, cnt1, 0);
 }
 
 // Stage 2: one any-hit shadow ray toward the light per queued pixel
@@ -352,11 +410,27 @@ bool stackless()
     return on;
 }
 
-template <int ORDER, bool COUNT, bool PACKET, bool INST, bool SL = false>
+template <int ORDER, bool COUNT, bool PACKET, bool INST, bool SL = false, bool FUSED = false>
 cudaError_t raycast_t(const LaunchInfo& li, const DevScene& sc, const DevCamera& cam, const rc_ray* rays,
                       uint64_t pixelStart, int64_t count, int64_t width, int castShadow, float3 L, float off,
-                      rc_cast_pixel* out, int* queue, DevControl* ctl, cudaEvent_t between, float4* origins)
+                      rc_cast_pixel* out, int* queue, DevControl* ctl, cudaEvent_t between, float4* origins,
+                      int& kernels)
 {
+    // Tile a whole frame (pixel range = the full image; camera rays or one
+    // caller ray per pixel): only the order the warps take the pixels in.
+    const int64_t height = width > 0 ? count / width : 0;
+    const int64_t tilesX = whole_frame(pixelStart, count, width) ? (width + 7) / 8 : 0;
+    if (FUSED && castShadow)
+    {
+        auto kf = k_raycast_primary<ORDER, false, PACKET, INST, true, SL>;
+        static int gf = 0;
+        if (gf == 0)
+            gf = persistent_blocks(kf, li.numSMs);
+        kf<<<gf, kBlock, 0, li.stream>>>(sc, cam, rays, pixelStart, count, width, height, tilesX, castShadow, out,
+                                         queue, ctl, L, off, nullptr);
+        kernels = 1;
+        return cudaGetLastError();
+    }
     auto kp = k_raycast_primary<ORDER, COUNT, PACKET, INST>;
     auto ks = k_raycast_shadow<COUNT, INST, SL>;
     static int gp = 0, gs = 0;
@@ -364,19 +438,46 @@ cudaError_t raycast_t(const LaunchInfo& li, const DevScene& sc, const DevCamera&
         gp = persistent_blocks(kp, li.numSMs);
     if (gs == 0)
         gs = persistent_blocks(ks, li.numSMs);
-    // Tile a whole frame (pixel range = the full image; camera rays or one
-    // caller ray per pixel): only the order the warps take the pixels in.
-    const int64_t height = width > 0 ? count / width : 0;
-    const int64_t tilesX = whole_frame(pixelStart, count, width) ? (width + 7) / 8 : 0;
     kp<<<gp, kBlock, 0, li.stream>>>(sc, cam, rays, pixelStart, count, width, height, tilesX, castShadow, out, queue,
                                      ctl, L, off, castShadow ? origins : nullptr);
+    kernels = 1;
     cudaError_t e = cudaGetLastError();
-    if (e == cudaSuccess && between)
-        e = cudaEventRecord(between, li.stream);
     if (e != cudaSuccess || !castShadow)
         return e;
+    if (between)
+        e = cudaEventRecord(between, li.stream);
+    if (e != cudaSuccess)
+        return e;
     ks<<<gs, kBlock, 0, li.stream>>>(sc, cam, rays, pixelStart, width, L, off, out, queue, ctl, origins);
+    kernels = 2;
     return cudaGetLastError();
+}
+
+// Whether uncounted RAY frames trace each shadow ray in the primary kernel
+// (k_raycast_primary FUSED); RC_TRACE_FUSED=0 keeps the two kernels with the
+// compacted shadow queue (read once).
+bool fused_frames()
+{
+    static const bool on = [] {
+        const char* v = std::getenv("RC_TRACE_FUSED");
+        return !(v && v[0] == '0');
+    }();
+    return on;
+}
+
+// Uncounted frames: the fused or the two-kernel form.
+template <int ORDER, bool PACKET, bool INST, bool SL = false>
+cudaError_t raycast_u(const LaunchInfo& li, const DevScene& sc, const DevCamera& cam, const rc_ray* rays,
+                      uint64_t pixelStart, int64_t count, int64_t width, int castShadow, float3 L, float off,
+                      rc_cast_pixel* out, int* queue, DevControl* ctl, cudaEvent_t between, float4* origins,
+                      int& kernels)
+{
+    return fused_frames() ? raycast_t<ORDER, false, PACKET, INST, SL, true>(li, sc, cam, rays, pixelStart, count,
+                                                                             width, castShadow, L, off, out, queue,
+                                                                             ctl, between, origins, kernels)
+                          : raycast_t<ORDER, false, PACKET, INST, SL, false>(li, sc, cam, rays, pixelStart, count,
+                                                                              width, castShadow, L, off, out, queue,
+                                                                              ctl, between, origins, kernels);
 }
 
 }  // namespace
@@ -402,33 +503,38 @@ cudaError_t launch_cast(const LaunchInfo& li, const DevScene& sc, const rc_ray* 
 cudaError_t launch_raycast(const LaunchInfo& li, const DevScene& sc, const DevCamera& cam, const rc_ray* rays,
                            uint64_t pixelStart, int64_t count, int64_t width, int order, int castShadow,
                            float3 dirToLight, float rayStartOffset, rc_cast_pixel* out, int* shadowQueue,
-                           DevControl* ctl, cudaEvent_t between, float4* shadowOrigins)
+                           DevControl* ctl, cudaEvent_t between, float4* shadowOrigins, int* kernels)
 {
+    int launched = 0;
+    if (!kernels)
+        kernels = &launched;
+    *kernels = 0;
     if (count <= 0)
         return cudaSuccess;
 #define RC_RAYCAST_ARGS li, sc, cam, rays, pixelStart, count, width, castShadow, dirToLight, rayStartOffset, out, \
-                        shadowQueue, ctl, between, shadowOrigins
+                        shadowQueue, ctl, between, shadowOrigins, *kernels
     // two-level scenes: the top level nearest-first, like rc_cast's
     if (sc.numInstances > 0)
         return li.counting ? raycast_t<ORDER_NEAREST, true, false, true>(RC_RAYCAST_ARGS)
-                           : raycast_t<ORDER_NEAREST, false, false, true>(RC_RAYCAST_ARGS);
+                           : raycast_u<ORDER_NEAREST, false, true>(RC_RAYCAST_ARGS);
     if (li.counting)
         return order == ORDER_NEAREST ? raycast_t<ORDER_NEAREST, true, false, false>(RC_RAYCAST_ARGS)
                                       : raycast_t<ORDER_REF, true, false, false>(RC_RAYCAST_ARGS);
     const int packets = trace_packets();
+    const bool packet = whole_frame(pixelStart, count, width) && (packets == 2 || (packets == 1 && !rays));
     if (stackless())
     {
-        if (whole_frame(pixelStart, count, width) && (packets == 2 || (packets == 1 && !rays)))
-            return order == ORDER_NEAREST ? raycast_t<ORDER_NEAREST, false, true, false, true>(RC_RAYCAST_ARGS)
-                                          : raycast_t<ORDER_REF, false, true, false, true>(RC_RAYCAST_ARGS);
-        return order == ORDER_NEAREST ? raycast_t<ORDER_NEAREST, false, false, false, true>(RC_RAYCAST_ARGS)
-                                      : raycast_t<ORDER_REF, false, false, false, true>(RC_RAYCAST_ARGS);
+        if (packet)
+            return order == ORDER_NEAREST ? raycast_u<ORDER_NEAREST, true, false, true>(RC_RAYCAST_ARGS)
+                                          : raycast_u<ORDER_REF, true, false, true>(RC_RAYCAST_ARGS);
+        return order == ORDER_NEAREST ? raycast_u<ORDER_NEAREST, false, false, true>(RC_RAYCAST_ARGS)
+                                      : raycast_u<ORDER_REF, false, false, true>(RC_RAYCAST_ARGS);
     }
-    if (whole_frame(pixelStart, count, width) && (packets == 2 || (packets == 1 && !rays)))
-        return order == ORDER_NEAREST ? raycast_t<ORDER_NEAREST, false, true, false>(RC_RAYCAST_ARGS)
-                                      : raycast_t<ORDER_REF, false, true, false>(RC_RAYCAST_ARGS);
-    return order == ORDER_NEAREST ? raycast_t<ORDER_NEAREST, false, false, false>(RC_RAYCAST_ARGS)
-                                  : raycast_t<ORDER_REF, false, false, false>(RC_RAYCAST_ARGS);
+    if (packet)
+        return order == ORDER_NEAREST ? raycast_u<ORDER_NEAREST, true, false>(RC_RAYCAST_ARGS)
+                                      : raycast_u<ORDER_REF, true, false>(RC_RAYCAST_ARGS);
+    return order == ORDER_NEAREST ? raycast_u<ORDER_NEAREST, false, false>(RC_RAYCAST_ARGS)
+                                  : raycast_u<ORDER_REF, false, false>(RC_RAYCAST_ARGS);
 #undef RC_RAYCAST_ARGS
 }
 

@@ -1277,12 +1277,13 @@ rc_status raycast_into(rc_tracer* h, const rc_ray* dRays, uint64_t pixelStart, u
     rc_status s = begin_launch(h);
     if (s != RC_OK)
         return s;
+    int kernels = 0;
     RC_CUDA_TRY(h,
                 launch_raycast(launch_info(h), dev_scene(h), cam, dRays, pixelStart, int64_t(count), width, order,
                                castShadow, L, h->general.ray_start_offset, dOut, dQueue, h->dCtl, h->evMid,
-                               dOrigins),
+                               dOrigins, &kernels),
                 "launch ray-cast kernels");
-    return end_launch(h, "ray cast", true);
+    return end_launch(h, "ray cast", kernels == 2);
 }
 
 rc_status render_raycast(rc_tracer* h, uint64_t pixelStart, uint64_t count, const rc_ray* dRays)
