@@ -40,10 +40,21 @@ struct __align__(16) DevNode
     float4 xy0;  // child 0: lo.x, hi.x, lo.y, hi.y
     float4 xy1;  // child 1: lo.x, hi.x, lo.y, hi.y
     float4 z01;  // child 0 lo.z, hi.z; child 1 lo.z, hi.z
-    int4 link;   // child 0 (left), child 1 (right), next, reserved. next: the node whose right
-                 // child the reference's preorder visits after this node's subtree (the
-                 // lowest ancestor with this node in its left subtree), -1 after the last
-                 // (thread_nodes; the stackless walk of traverse_stackless)
+    int4 link;   // child 0 (left), child 1 (right), reserved, reserved
+};
+
+// One child box of the binary tree in the reference's preorder (the
+// stackless walk, traverse_stackless): a box that is hit leads to the next
+// record (its first child) if it is an inner node's, else its leaf's
+// triangles are tested; then, or on a miss, the walk jumps to `miss`, the
+// first record after the box's subtree (= the record count after the last).
+struct __align__(32) DevRope
+{
+    float4 a;    // lo.x, lo.y, lo.z, hi.x
+    float hi_y;
+    float hi_z;
+    int link;    // >= 0: inner node (its children follow); < 0: leaf code ~((start << 4) | count)
+    int miss;
 };
 
 struct __align__(16) DevNode4
@@ -119,7 +130,8 @@ struct DevScene
     int numInstances;  // 0: single-level scene
     const DevNode4* wide;  // 4-wide BVH of a single-level scene, or null
     int wideRoot;          // >= 0: DevNode4 0; < 0: the root is a leaf
-    int widePad;
+    int ropeCount;         // records in `ropes`
+    const DevRope* ropes;  // the stackless walk's records of a single-level scene, or null
 };
 
 // Float32 camera record used by the kernels (same fields as rc_camera).

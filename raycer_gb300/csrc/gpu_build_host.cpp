@@ -211,12 +211,6 @@ rc_status upload_gpu_built(rc_tracer* h, const double* v, const uint32_t* matIdx
     GB_TRY(cudaStreamSynchronize(h->stream), "emit");
 
     const int32_t rootLink = kept > 0 ? 0 : ~int32_t((0u << kLeafCountBits) | uint32_t(n));
-    if (kept > 0)
-    {
-        // next links for the stackless walk, computed here and uploaded with the nodes
-        thread_nodes(hn, rootLink);
-        GB_TRY(cudaMemcpy(dNodes, hn.data(), nodeCount * sizeof(DevNode), cudaMemcpyHostToDevice), "upload next links");
-    }
     std::vector<BuildNode> flat;
     flat_from_device(hn, hr, rootLink, n, flat);
     if (rootLink < 0)

@@ -119,6 +119,10 @@ struct rc_tracer
     size_t wideCount = 0;
     int32_t wideRoot = 0;
     bool wideTried = false;  // ensure_wide ran for the current scene
+    // Rope records of a single-level scene for the stackless walk (wide_bvh.cpp), or none.
+    rcx::DevRope* dRopes = nullptr;
+    size_t ropeCount = 0;
+    bool ropesTried = false;  // ensure_ropes ran for the current scene
 
     // Per-frame records.
     rc_camera camera{};
@@ -197,13 +201,14 @@ void release_scene_data(rc_tracer* h);
 // uploads it (h->dWide); leaves it out where its stack need exceeds the
 // traversal stack. Failure to allocate is an error.
 rc_status upload_wide(rc_tracer* h, const std::vector<DevNode>& nodes, int32_t rootLink);
-// Sets each inner node's next link (DevNode::link.z) for the stackless
-// reference-order walk.
-void thread_nodes(std::vector<DevNode>& dn, int32_t rootLink);
 // Builds the 4-wide BVH of the handle's single-level scene on first use (the
 // first PATH or batch render of a scene): downloads the binary nodes once,
 // collapses and uploads them. Uploads and RAY frames do not pay for it.
 rc_status ensure_wide(rc_tracer* h);
+// Builds the rope records of the handle's single-level scene on first use
+// (the first RAY frame or rc_cast while the stackless walk is on): one
+// download of the binary nodes, one upload of the records.
+rc_status ensure_ropes(rc_tracer* h);
 // Two-level scenes (instancing.cpp): argument checks, one SAH build per mesh
 // (host scenes in BVH order), and the pooled upload with instance transforms
 // and the top-level BVH (which also keeps the meshes and instances on the

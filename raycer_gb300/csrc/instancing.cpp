@@ -341,7 +341,6 @@ rc_status upload_instanced_scenes(rc_tracer* h, std::vector<HostScene>&& meshSce
             {
                 d.link.x = relink(d.link.x);
                 d.link.y = relink(d.link.y);
-                d.link.z = d.link.z >= 0 ? d.link.z + nodeBase : -1;
                 nodes.push_back(d);
             }
         meshRoot[size_t(m)] = relink(root);

@@ -27,6 +27,12 @@ struct LaunchInfo
     int counting;  // count node / triangle tests
 };
 
+// Whether uncounted reference-order queries (RAY-frame shadow rays, rc_cast
+// in RC_ORDER_REFERENCE) take the stackless walk (traverse_stackless) where
+// the scene has rope records (DevScene::ropes; the host builds them on first
+// use while this is on).
+bool stackless_walk();
+
 // Generic ray queries (rc_ray -> rc_hit).
 cudaError_t launch_cast(const LaunchInfo& li, const DevScene& sc, const rc_ray* rays, int64_t n, int anyHit,
                         int order, rc_hit* hits, DevControl* ctl);

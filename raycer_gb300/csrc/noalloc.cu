@@ -109,6 +109,8 @@ extern "C" rc_status rc_cast_with_shadow_device_noalloc(rc_tracer* h, const rc_r
     sc.numTris = int(h->nTris);
     sc.numMats = int(h->nMats);
     sc.pad = 0;
+    sc.ropes = h->dRopes;  // built by an earlier call, if any (nothing is allocated here)
+    sc.ropeCount = int(h->ropeCount);
     rcx::DevCamera cam{};
     rcx::LaunchInfo li;
     li.stream = h->stream;

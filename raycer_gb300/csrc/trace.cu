@@ -88,7 +88,7 @@ __global__ void __launch_bounds__(kBlock, RC_TRACE_MIN_BLOCKS) k_cast(DevScene s
             float4 r1 = __ldg(rp + 1);
             RayF ray = make_ray(v3(r0.x, r0.y, r0.z), v3(r1.x, r1.y, r1.z), r0.w, r1.w);
             HitF h{ -1, FLT_MAX, 0.0f, 0.0f, -1 };
-            // SL: the reference order of a single-level scene on the threaded tree
+            // SL: the reference order of a single-level scene on the rope records
             bool found = SL ? traverse_stackless<ANY>(sc, ray, h, -1)
                             : traverse_scene<ANY, ORDER, COUNT>(sc, ray, h, cnt, err, -1, -1);
             int4 out;
@@ -154,7 +154,7 @@ __device__ __forceinline__ void shadow_of(const DevScene& sc, const RayF& ray, c
 // instance, for the shadow ray to skip the hit triangle of that instance).
 // FUSED (uncounted frames with a light): each lane whose ray hit traces its
 // shadow ray right after the tile's primary rays, with the shadow kernel's
-// arithmetic (stage 2 below; SL: the threaded walk), and the pixel's record
+// arithmetic (stage 2 below; SL: the stackless walk), and the pixel's record
 // is written once, complete; no queue. The shadow rays of a tile whose
 // pixels all hit (or all miss) keep the warp full (or cost nothing); only
 // tiles on a silhouette leave lanes idle. With the caller's rays in host
@@ -397,18 +397,6 @@ bool whole_frame(uint64_t pixelStart, int64_t count, int64_t width)
     return RC_TRACE_TILES && pixelStart == 0 && width >= 8 && count / width >= 4 && (count / width) * width == count;
 }
 
-// Whether the reference-order queries of uncounted frames (the RAY frame's
-// shadow rays, rc_cast in RC_ORDER_REFERENCE) walk the threaded tree without
-// a stack (RC_STACKLESS=1; read once). The same hits; measured slower on the
-// 1080p heightfield's shadow rays (0.279 vs 0.169 ms), so off by default.
-bool stackless()
-{
-    static const bool on = [] {
-        const char* v = std::getenv("RC_STACKLESS");
-        return v && v[0] == '1';
-    }();
-    return on;
-}
 
 template <int ORDER, bool COUNT, bool PACKET, bool INST, bool SL = false, bool FUSED = false>
 cudaError_t raycast_t(const LaunchInfo& li, const DevScene& sc, const DevCamera& cam, const rc_ray* rays,
@@ -482,12 +470,24 @@ cudaError_t raycast_u(const LaunchInfo& li, const DevScene& sc, const DevCamera&
 
 }  // namespace
 
+// Whether the reference-order queries of uncounted frames (the RAY frame's
+// shadow rays, rc_cast in RC_ORDER_REFERENCE) take the stackless walk over
+// the rope records (RC_STACKLESS=1; read once). The same hits.
+bool stackless_walk()
+{
+    static const bool on = [] {
+        const char* v = std::getenv("RC_STACKLESS");
+        return v && v[0] == '1';
+    }();
+    return on;
+}
+
 cudaError_t launch_cast(const LaunchInfo& li, const DevScene& sc, const rc_ray* rays, int64_t n, int anyHit,
                         int order, rc_hit* hits, DevControl* ctl)
 {
     if (n <= 0)
         return cudaSuccess;
-    const bool sl = !li.counting && sc.numInstances == 0 && stackless();
+    const bool sl = !li.counting && sc.numInstances == 0 && sc.ropes && stackless_walk();
     if (anyHit)
         return li.counting ? cast_t<true, ORDER_REF, true>(li, sc, rays, n, hits, ctl)
                : sl        ? cast_t<true, ORDER_REF, false, true>(li, sc, rays, n, hits, ctl)
@@ -522,7 +522,7 @@ cudaError_t launch_raycast(const LaunchInfo& li, const DevScene& sc, const DevCa
                                       : raycast_t<ORDER_REF, true, false, false>(RC_RAYCAST_ARGS);
     const int packets = trace_packets();
     const bool packet = whole_frame(pixelStart, count, width) && (packets == 2 || (packets == 1 && !rays));
-    if (stackless())
+    if (stackless_walk() && sc.ropes)
     {
         if (packet)
             return order == ORDER_NEAREST ? raycast_u<ORDER_NEAREST, true, false, true>(RC_RAYCAST_ARGS)

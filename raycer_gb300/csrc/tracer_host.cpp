@@ -114,6 +114,9 @@ void release_scene(rc_tracer* h)
     h->wideCount = 0;
     h->wideRoot = 0;
     h->wideTried = false;
+    dev_free(h, &h->dRopes, h->ropeCount);
+    h->ropeCount = 0;
+    h->ropesTried = false;
     h->tlasCount = 0;
     h->nInstances = 0;
     h->tlasRoot = 0;
@@ -266,25 +269,6 @@ void device_nodes(const std::vector<BuildNode>& nodes, std::vector<DevNode>& dn,
     }
     rootLink = nodes[0].rightOffset != 0 ? 0 : link(0);
     inner = uint64_t(count);
-    thread_nodes(dn, rootLink);
-}
-
-void thread_nodes(std::vector<DevNode>& dn, int32_t rootLink)
-{
-    if (rootLink < 0 || dn.empty())
-        return;
-    std::vector<std::pair<int32_t, int32_t>> work{ { rootLink, -1 } };  // (node, its next)
-    while (!work.empty())
-    {
-        const auto [p, next] = work.back();
-        work.pop_back();
-        DevNode& d = dn[size_t(p)];
-        d.link.z = next;
-        if (d.link.y >= 0)
-            work.push_back({ d.link.y, next });  // after the right subtree: p's own next
-        if (d.link.x >= 0)
-            work.push_back({ d.link.x, p });     // after the left subtree: p's right child
-    }
 }
 
 // Triangle, shading and material records of a scene in BVH order.
@@ -458,7 +442,8 @@ DevScene dev_scene(const rc_tracer* h)
     s.numInstances = int(h->nInstances);
     s.wide = h->dWide;
     s.wideRoot = h->wideRoot;
-    s.widePad = 0;
+    s.ropes = h->dRopes;
+    s.ropeCount = int(h->ropeCount);
     return s;
 }
 
@@ -1021,7 +1006,10 @@ rc_status rc_cast_device(rc_tracer* h, const rc_ray* d_rays, int64_t n, int32_t 
     if (order != RC_ORDER_REFERENCE && order != RC_ORDER_NEAREST)
         return fail(h, RC_INVALID_ARG, "cast: invalid traversal order");
     cudaSetDevice(h->device);
-    rc_status s = begin_launch(h);
+    rc_status s = stackless_walk() ? ensure_ropes(h) : RC_OK;
+    if (s != RC_OK)
+        return s;
+    s = begin_launch(h);
     if (s != RC_OK)
         return s;
     RC_CUDA_TRY(h, launch_cast(launch_info(h), dev_scene(h), d_rays, n, any_hit, order, d_hits, h->dCtl),
@@ -1090,7 +1078,9 @@ rc_status rc_cast_with_shadow(rc_tracer* h, const rc_ray* rays, int64_t n, int32
     if (order != RC_ORDER_REFERENCE && order != RC_ORDER_NEAREST)
         return fail(h, RC_INVALID_ARG, "cast_with_shadow: invalid traversal order");
     cudaSetDevice(h->device);
-    rc_status s;
+    rc_status s = stackless_walk() ? ensure_ropes(h) : RC_OK;
+    if (s != RC_OK)
+        return s;
     // In place when the device can reach both host buffers (16-byte aligned):
     // the kernels read the rays and write the results over the host link, so
     // no separate copy has to wait for the persistent kernels.
@@ -1274,7 +1264,10 @@ rc_status raycast_into(rc_tracer* h, const rc_ray* dRays, uint64_t pixelStart, u
     }
     DevCamera cam = dev_camera(h->camera);
     int64_t width = int64_t(h->width ? h->width : 1);
-    rc_status s = begin_launch(h);
+    rc_status s = stackless_walk() ? ensure_ropes(h) : RC_OK;
+    if (s != RC_OK)
+        return s;
+    s = begin_launch(h);
     if (s != RC_OK)
         return s;
     int kernels = 0;

@@ -204,98 +204,80 @@ __device__ __forceinline__ bool traverse(const DevScene& sc, const RayF& ray, Hi
     }
 }
 
-// The reference's order without a stack: the tree is threaded (each inner
-// node's link.z names the node whose right child follows its subtree in the
-// preorder; tracer_host.cpp thread_nodes). At (node p, side s) the walk tests
-// child s's box; a hit inner child is entered at its left side, a hit leaf's
-// triangles are tested in order; then the walk moves to p's right side, or,
-// after the right side, to (next of p, right side). Each ray meets the
-// boxes and triangles of traverse<ANY_HIT, ORDER_REF> in the same order, so
-// it returns the same closest hit (ties to the later triangle) or the same
-// first any-hit; a node is fetched when entered and again when the walk
-// returns to its right side, instead of being pushed and popped.
+// The reference's order without a stack, on the rope records (DevRope,
+// every child box of the binary tree once, in the reference's preorder): a
+// hit inner box continues at the next record (its left child), a hit leaf
+// box's triangles are tested in order, and after a leaf or on a miss the
+// walk jumps to the record after the box's subtree. Each ray meets the boxes
+// and triangles of traverse<ANY_HIT, ORDER_REF> in the same order (the same
+// slab test on the same float boxes), so it returns the same closest hit
+// (ties to the later triangle) or the same first any-hit; one 32-byte record
+// per tested box, no stack, and a descent reads the next record in memory.
+// Needs sc.ropes (callers fall back to traverse() without them).
+template <bool ANY_HIT>
+__device__ __forceinline__ bool test_leaf(const DevScene& sc, const RayF& ray, HitF& hit, int leafCode, int skip,
+                                          bool& found)
+{
+    const int leaf = ~leafCode;
+    const int start = leaf >> kLeafCountBits;
+    const int count = leaf & ((1 << kLeafCountBits) - 1);
+    for (int i = 0; i < count; ++i)
+    {
+        const int slot = start + i;
+        if (slot == skip)
+            continue;
+        const float4* tp = reinterpret_cast<const float4*>(sc.tris + slot);
+        const float4 ta = __ldg(tp + 0);
+        const float4 tb = __ldg(tp + 1);
+        const float4 tc = __ldg(tp + 2);
+        if (ANY_HIT && (__float_as_uint(tc.y) & kMetaNonShadowing))
+            continue;
+        float t, u, v;
+        if (tri_hit(ray, v3(ta.x, ta.y, ta.z), v3(ta.w, tb.x, tb.y), v3(tb.z, tb.w, tc.x), t, u, v) &&
+            (ANY_HIT || !(t > hit.t)))
+        {
+            hit.slot = slot;
+            hit.t = t;
+            hit.u = u;
+            hit.v = v;
+            found = true;
+            if (ANY_HIT)
+                return true;
+        }
+    }
+    return false;
+}
+
 template <bool ANY_HIT>
 __device__ __forceinline__ bool traverse_stackless(const DevScene& sc, const RayF& ray, HitF& hit, int skip)
 {
     bool found = false;
-    int p = sc.rootLink;
-    int side = 0;
-    if (p < 0)
+    if (sc.rootLink < 0)
     {
-        // a leaf root: its triangles only
-        side = 2;
+        test_leaf<ANY_HIT>(sc, ray, hit, sc.rootLink, skip, found);  // a leaf root: its triangles only
+        return found;
     }
-    float4 a, b, c;
-    int4 l;
-    if (p >= 0)
-        load_node(sc.nodes, p, a, b, c, l);
-    while (true)
+    const int end = sc.ropeCount;
+    int r = 0;
+    while (r < end)
     {
-        int child;
-        bool hitBox;
-        if (side == 2)
+        const float4* p = reinterpret_cast<const float4*>(sc.ropes + r);
+        const float4 a = __ldg(p);
+        const float4 b = __ldg(p + 1);  // hi.y, hi.z, link, miss
+        float e;
+        const bool h = ray.finite ? slab_finite(ray, a.x, a.w, a.y, b.x, a.z, b.y, e)
+                                  : slab(ray, a.x, a.w, a.y, b.x, a.z, b.y, e);
+        const int link = __float_as_int(b.z);
+        if (h && link >= 0)
         {
-            child = p;  // the leaf root
-            hitBox = true;
-        }
-        else
-        {
-            float e;
-            const float lox = side ? b.x : a.x, hix = side ? b.y : a.y, loy = side ? b.z : a.z, hiy = side ? b.w : a.w;
-            const float loz = side ? c.z : c.x, hiz = side ? c.w : c.y;
-            hitBox = ray.finite ? slab_finite(ray, lox, hix, loy, hiy, loz, hiz, e) : slab(ray, lox, hix, loy, hiy, loz, hiz, e);
-            child = side ? l.y : l.x;
-        }
-        if (hitBox)
-        {
-            if (child >= 0)
-            {
-                p = child;
-                side = 0;
-                load_node(sc.nodes, p, a, b, c, l);
-                continue;
-            }
-            const int leaf = ~child;
-            const int start = leaf >> kLeafCountBits;
-            const int count = leaf & ((1 << kLeafCountBits) - 1);
-            for (int i = 0; i < count; ++i)
-            {
-                const int slot = start + i;
-                if (slot == skip)
-                    continue;
-                const float4* tp = reinterpret_cast<const float4*>(sc.tris + slot);
-                const float4 ta = __ldg(tp + 0);
-                const float4 tb = __ldg(tp + 1);
-                const float4 tc = __ldg(tp + 2);
-                if (ANY_HIT && (__float_as_uint(tc.y) & kMetaNonShadowing))
-                    continue;
-                float t, u, v;
-                if (tri_hit(ray, v3(ta.x, ta.y, ta.z), v3(ta.w, tb.x, tb.y), v3(tb.z, tb.w, tc.x), t, u, v) &&
-                    (ANY_HIT || !(t > hit.t)))
-                {
-                    hit.slot = slot;
-                    hit.t = t;
-                    hit.u = u;
-                    hit.v = v;
-                    found = true;
-                    if (ANY_HIT)
-                        return true;
-                }
-            }
-        }
-        // advance: the right side of p, or the right side of p's next
-        if (side == 0)
-        {
-            side = 1;
+            ++r;
             continue;
         }
-        if (side == 2)
-            return found;
-        p = l.z;
-        if (p < 0)
-            return found;
-        load_node(sc.nodes, p, a, b, c, l);
+        if (h && test_leaf<ANY_HIT>(sc, ray, hit, link, skip, found))
+            return true;
+        r = __float_as_int(b.w);
     }
+    return found;
 }
 
 // Entry distance of one child box of a wide node, or +inf when the ray misses

@@ -19,6 +19,10 @@
 // The traversal pushes at most (children - 1) entries per node; a tree whose
 // worst root-to-leaf sum exceeds the stack is left binary, and so is every
 // scene when RC_WIDE_BVH=0 is set in the environment (read once).
+//
+// The same file writes the rope records of the stackless walk: every child
+// box of the binary tree once, in the reference's preorder, with the index
+// of the first record after its subtree (DevRope, traverse_stackless).
 
 #include <cuda_runtime.h>
 
@@ -144,6 +148,67 @@ int collapse(const std::vector<DevNode>& nodes, int32_t rootLink, std::vector<De
     return maxNeed;
 }
 
+// Rope records of the binary tree in the reference's preorder (left child
+// first; the root's own box is never tested, so its two children are the
+// first subtrees). Returns false for malformed links.
+bool build_ropes(const std::vector<DevNode>& nodes, int32_t rootLink, std::vector<DevRope>& out)
+{
+    out.clear();
+    if (rootLink < 0)
+        return true;  // a leaf root: the walk tests its triangles only
+    const int32_t count = int32_t(nodes.size());
+    if (rootLink >= count)
+        return false;
+    out.reserve(2 * nodes.size());
+    // Explicit preorder: `work` holds the child boxes still to emit (next on
+    // top). `open` holds the inner records whose subtrees are being emitted
+    // (innermost last) and `pending` how many of their two child subtrees are
+    // not complete yet; a record's miss link is set when its subtree is.
+    std::vector<Child> work;
+    std::vector<int32_t> open;
+    std::vector<int> pending;
+    Child x, y;
+    children_of(nodes[size_t(rootLink)], x, y);
+    work.push_back(y);
+    work.push_back(x);
+    while (!work.empty())
+    {
+        const Child c = work.back();
+        work.pop_back();
+        if (out.size() >= 2 * nodes.size() + 2)
+            return false;  // a cycle in the links
+        const int32_t r = int32_t(out.size());
+        DevRope rec{};
+        rec.a = make_float4(c.lo[0], c.lo[1], c.lo[2], c.hi[0]);
+        rec.hi_y = c.hi[1];
+        rec.hi_z = c.hi[2];
+        rec.link = c.link;
+        rec.miss = 0;
+        out.push_back(rec);
+        if (c.link >= 0)
+        {
+            if (c.link >= count)
+                return false;
+            children_of(nodes[size_t(c.link)], x, y);
+            work.push_back(y);
+            work.push_back(x);
+            open.push_back(r);
+            pending.push_back(2);
+            continue;
+        }
+        out[size_t(r)].miss = r + 1;  // a leaf's subtree is itself
+        // the leaf completes a child subtree of the innermost open record;
+        // each record completed that way completes one of its parent's
+        while (!open.empty() && --pending.back() == 0)
+        {
+            out[size_t(open.back())].miss = int32_t(out.size());
+            open.pop_back();
+            pending.pop_back();
+        }
+    }
+    return open.empty();
+}
+
 }  // namespace
 
 rc_status upload_wide(rc_tracer* h, const std::vector<DevNode>& nodes, int32_t rootLink)
@@ -200,6 +265,43 @@ rc_status ensure_wide(rc_tracer* h)
         }
     }
     return upload_wide(h, nodes, h->rootLink);
+}
+
+rc_status ensure_ropes(rc_tracer* h)
+{
+    if (h->ropesTried || !h->sceneReady || h->nInstances > 0)
+        return RC_OK;
+    h->ropesTried = true;
+    if (h->rootLink < 0)
+        return RC_OK;  // a leaf root: the stack walk tests it directly
+    std::vector<DevNode> nodes(h->innerCount);
+    cudaError_t e = cudaMemcpy(nodes.data(), h->dNodes, nodes.size() * sizeof(DevNode), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess)
+    {
+        cudaGetLastError();
+        h->err = std::string("rope records: download nodes: ") + cudaGetErrorString(e);
+        return RC_CUDA;
+    }
+    std::vector<DevRope> ropes;
+    if (!build_ropes(nodes, h->rootLink, ropes))
+    {
+        h->err = "rope records: malformed binary node links";
+        return RC_DEVICE_ERROR;
+    }
+    e = cudaMalloc(reinterpret_cast<void**>(&h->dRopes), ropes.size() * sizeof(DevRope));
+    if (e == cudaSuccess)
+        e = cudaMemcpy(h->dRopes, ropes.data(), ropes.size() * sizeof(DevRope), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess)
+    {
+        cudaGetLastError();
+        cudaFree(h->dRopes);
+        h->dRopes = nullptr;
+        h->err = std::string("rope records: ") + cudaGetErrorString(e);
+        return e == cudaErrorMemoryAllocation ? RC_OOM : RC_CUDA;
+    }
+    h->ropeCount = ropes.size();
+    h->deviceBytes += ropes.size() * sizeof(DevRope);
+    return RC_OK;
 }
 
 }  // namespace rcx

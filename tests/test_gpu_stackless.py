@@ -1,4 +1,4 @@
-"""The stackless reference-order walk (RC_STACKLESS=1: the threaded tree,
+"""The stackless reference-order walk (RC_STACKLESS=1: the rope records,
 no traversal stack) gives the float32 oracle's results bit for bit: RAY
 frames in both orders (their shadow rays walk it) and reference-order
 rc_cast queries, closest and any hit. The switch is read once per process,
