@@ -26,6 +26,12 @@ constexpr int kBlock = 128;
 #ifndef RC_TRACE_MIN_BLOCKS
 #define RC_TRACE_MIN_BLOCKS 10
 #endif
+// The one-kernel RAY frame (primary + shadow walks) at 9 blocks: 56
+// registers, no spills; 0.405 ms per 1080p heightfield frame against 0.417
+// at 10 blocks (48 registers, spills) and 0.420 at 8.
+#ifndef RC_FUSED_MIN_BLOCKS
+#define RC_FUSED_MIN_BLOCKS 9
+#endif
 #ifndef RC_TRACE_TILES
 #define RC_TRACE_TILES 1
 #endif
@@ -160,7 +166,7 @@ __device__ __forceinline__ void shadow_of(const DevScene& sc, const RayF& ray, c
 // tiles on a silhouette leave lanes idle. With the caller's rays in host
 // memory the shadow work then overlaps the ray reads over the host link.
 template <int ORDER, bool COUNT, bool PACKET, bool INST, bool FUSED = false, bool SL = false>
-__global__ void __launch_bounds__(kBlock, RC_TRACE_MIN_BLOCKS) k_raycast_primary(DevScene sc, DevCamera cam, const rc_ray* __restrict__ rays,
+__global__ void __launch_bounds__(kBlock, FUSED ? RC_FUSED_MIN_BLOCKS : RC_TRACE_MIN_BLOCKS) k_raycast_primary(DevScene sc, DevCamera cam, const rc_ray* __restrict__ rays,
                                                             uint64_t pixelStart, int64_t count, int64_t width,
                                                             int64_t height, int64_t tilesX, int castShadow,
                                                             rc_cast_pixel* __restrict__ out, int* __restrict__ queue,
