@@ -410,7 +410,10 @@ def run_ours(args, rank, local_rank, world):
                          "traffic": traffic,
                          "node_fetches": int(k_nodes), "triangle_tests": int(k_tris),
                          # BVH-node bytes (64 B per inner-node fetch) per second of the kernel
-                         "bvh_node_gbs": round(k_nodes * 64 / prim_avg / 1e9, 1)},
+                         "bvh_node_gbs": round(k_nodes * 64 / prim_avg / 1e9, 1),
+                         # HBM bytes actually moved (ncu DRAM read + write of one launch) per second:
+                         # the nodes and touched triangles are served from L1/L2
+                         "dram_gbs": round(traffic / prim_avg / 1e9, 1) if traffic else None},
             "stages_ms": {"primary": round(statistics.mean(prim_ms), 4), "shadow": round(statistics.mean(shadow_ms), 4)},
             "wall_s": round(t_wall, 3),
             "clocks": clocks.summary(),
