@@ -205,10 +205,14 @@ typedef struct rc_stats
     uint64_t bvh_inner_nodes;  /* inner nodes of the device BVH                */
     uint64_t bvh_depth;        /* depth of the uploaded BVH                    */
     uint64_t device_bytes;     /* device memory held by the handle             */
-    /* Per stage of the last call. RAY render / cast_with_shadow: 0 = primary
-     * closest-hit kernel, 1 = shadow any-hit kernel. PATH render: 0 = the
-     * extend (closest-hit) kernels of all segments, 1 = everything else
-     * (generate, shade, accumulate). cast: 0 = the cast kernel. */
+    /* Per stage of the last call. RAY render / cast_with_shadow: rays, nodes
+     * and triangles 0 = primary closest hit, 1 = shadow any hit; times 0 =
+     * the primary kernel, 1 = the shadow kernel where the frame runs as two
+     * kernels (counted frames, RC_TRACE_FUSED=0), else 0 = the one kernel
+     * that traces both and 1 = 0.0. (The in-place rc_cast_with_shadow
+     * leaves both times 0.0.) PATH render: 0 = the extend (closest-hit)
+     * kernels of all segments, 1 = everything else (generate, shade,
+     * accumulate). cast: 0 = the cast kernel. */
     uint64_t stage_rays[2];
     uint64_t stage_nodes[2];   /* when counting is on */
     uint64_t stage_tris[2];    /* when counting is on */

@@ -2,10 +2,13 @@
 // frame (one primary ray per pixel + one shadow ray per hit).
 //
 // Work distribution: persistent blocks (occupancy x SM count) whose warps
-// take 32 rays at a time from a global atomic work counter; the shadow
-// stage is fed by a queue that the primary stage fills with one atomicAdd
-// per warp after a ballot over the lanes that hit (warp-aggregated
-// compaction), so shadow warps carry no missed pixels.
+// take 32 rays (an 8x4-pixel tile of a whole frame) at a time from a global
+// atomic work counter. An uncounted RAY frame is one kernel: each lane whose
+// primary ray hit traces its shadow ray right after its tile. Counted frames
+// (and RC_TRACE_FUSED=0) keep two stages: the shadow stage is fed by a queue
+// that the primary stage fills with one atomicAdd per warp after a ballot
+// over the lanes that hit (warp-aggregated compaction), so shadow warps
+// carry no missed pixels.
 
 #include <cfloat>
 
