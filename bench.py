@@ -170,6 +170,21 @@ def profiled_traffic(fused=False):
     return float(m.group(1)) if m else None
 
 
+def reduce_replicas(times, counts, world, device):
+    """Whole-job figures of N replicas: each timed region is the maximum over
+    the ranks, each count (rays) the sum. `device` holds the reduction's
+    tensors (the rank's GPU under NCCL, the CPU under gloo). Returns the
+    times then the counts, as floats."""
+    import torch
+
+    t = torch.tensor([float(x) for x in times], dtype=torch.float64, device=device)
+    c = torch.tensor([float(x) for x in counts], dtype=torch.float64, device=device)
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.all_reduce(c, op=torch.distributed.ReduceOp.SUM)
+    return (*t.tolist(), *c.tolist())
+
+
 def cpu_threads():
     try:
         return len(os.sched_getaffinity(0))
@@ -360,15 +375,8 @@ def run_ours(args, rank, local_rank, world):
 
     bvh = tracer.get_bvh() if rank == 0 else None
 
-    # max over ranks of the timed regions
-    times = torch.tensor([dev_sec, e2e_sec, t_wall], dtype=torch.float64, device=torch.device("cuda", local_rank))
-    rays_t = torch.tensor([float(total_rays), float(e2e_rays)], dtype=torch.float64,
-                          device=torch.device("cuda", local_rank))
-    if world > 1:
-        torch.distributed.all_reduce(times, op=torch.distributed.ReduceOp.MAX)
-        torch.distributed.all_reduce(rays_t, op=torch.distributed.ReduceOp.SUM)
-    dev_sec, e2e_sec, t_wall = times.tolist()
-    total_rays, e2e_rays = rays_t.tolist()
+    dev_sec, e2e_sec, t_wall, total_rays, e2e_rays = reduce_replicas(
+        (dev_sec, e2e_sec, t_wall), (total_rays, e2e_rays), world, torch.device("cuda", local_rank))
 
     line = None
     if rank == 0:
