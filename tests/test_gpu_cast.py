@@ -160,3 +160,30 @@ def test_cast_edge_rays_bit_exact(any_hit, order):
     assert same_t.all()
     for g, r in ((hits["u"], u), (hits["v"], v)):
         assert ((g == r) | (np.isnan(g) & np.isnan(r))).all()
+
+
+@pytest.mark.parametrize("order", [N.RC_ORDER_REFERENCE, N.RC_ORDER_NEAREST])
+@pytest.mark.parametrize("shape", [(157, 61, 0, None), (7, 5, 0, None), (300, 3, 0, None), (157, 61, 1000, 3001)])
+def test_raycast_frame_odd_shapes(shape, order):
+    """One-kernel RAY frames at shapes the 8x4 tiling does not divide: partial
+    tiles along both edges (157x61), a frame narrower than a tile (7x5) and
+    one shorter than a tile (300x3; the camera needs two rows at least), both
+    walked pixel by pixel, and a pixel sub-range of a frame (start 1000, 3001
+    pixels), bit-exact against the oracle."""
+    width, height, start, count = shape
+    count = width * height if count is None else count
+    sc = small_heightfield(width=width, height=height)
+    sc.settings["tracer"] = "ray"
+    with CudaTracer(0) as t:
+        t.initializeBuffers(sc)
+        t.set_traversal_order(order)
+        t.initializeImageBuffers(sc.width, sc.height)
+        st = TracerState(scene=sc, filmWidth=sc.width, filmHeight=sc.height, pixelStartOffset=start, pixelCount=count)
+        t.run(st)
+        assert st.pixelsProcessed == count
+        gpu = t.read_cast().view(np.int32).reshape(-1, 4)[:count]
+    L = -np.array(sc.light_direction, np.float32)
+    ref, _ = oracle.Oracle(sc).raycast32(camera_floats(camera_record(sc)), sc.width, count, L, order=order,
+                                         pixel_start=start)
+    assert np.array_equal(gpu, ref), f"{(gpu != ref).any(axis=1).sum()} of {count} pixels differ"
+    assert (ref[:, 0] >= 0).any()
