@@ -187,3 +187,30 @@ def test_raycast_frame_odd_shapes(shape, order):
                                          pixel_start=start)
     assert np.array_equal(gpu, ref), f"{(gpu != ref).any(axis=1).sum()} of {count} pixels differ"
     assert (ref[:, 0] >= 0).any()
+
+
+def test_cast_with_shadow_ray_lists():
+    """Caller ray lists that are not a whole image (a partial frame in pixel
+    order, and the whole frame's rays shuffled) go through the one-kernel
+    frame walked ray by ray; each ray's record equals the camera frame's
+    record of its pixel."""
+    from raycer_gb300.tracer import RAY_DTYPE
+
+    sc = small_heightfield(width=160, height=90)
+    sc.settings["tracer"] = "ray"
+    sc.light_direction = (-1.0, -0.25, -0.2)  # a low light: the hills shadow the valleys
+    n = sc.width * sc.height
+    with CudaTracer(0) as t:
+        t.initializeBuffers(sc)
+        t.initializeImageBuffers(sc.width, sc.height)
+        t.run(TracerState(scene=sc, filmWidth=sc.width, filmHeight=sc.height, pixelCount=n))
+        frame = t.read_cast().copy()
+        rays = np.ascontiguousarray(oracle.camera_rays32(camera_floats(camera_record(sc)), sc.width, n))
+        rays = rays.view(RAY_DTYPE).reshape(-1)
+        part = 5 * sc.width + 17
+        out = t.cast_with_shadow(np.ascontiguousarray(rays[:part]))
+        assert np.array_equal(out, frame[:part])
+        perm = np.random.default_rng(4).permutation(n)
+        out = t.cast_with_shadow(np.ascontiguousarray(rays[perm]))
+        assert np.array_equal(out, frame[perm])
+    assert (frame["prim"] >= 0).any() and (frame["occluder"] >= 0).any()
