@@ -28,17 +28,21 @@ def _frame(sc, order):
 
 
 @pytest.mark.parametrize("order", [N.RC_ORDER_REFERENCE, N.RC_ORDER_NEAREST])
-@pytest.mark.parametrize("which", ["room", "heightfield"])
+@pytest.mark.parametrize("which", ["room", "heightfield", "heightfield_low_light"])
 def test_raycast_frame_bit_exact(which, order):
     sc = small_room() if which == "room" else small_heightfield()
     sc.settings["tracer"] = "ray"
     if which == "room":
         sc.light_direction = (-0.3, -1.0, -0.2)
+    elif which == "heightfield_low_light":
+        sc.light_direction = (-1.0, -0.25, -0.2)  # the hills shadow the valleys
     gpu, cam = _frame(sc, order)
     orc = oracle.Oracle(sc)
     L = -np.array(sc.light_direction, np.float32)
     ref, _ = orc.raycast32(cam, sc.width, sc.width * sc.height, L, order=order)
     assert np.array_equal(gpu, ref), f"{(gpu != ref).any(axis=1).sum()} pixels differ"
+    if which != "heightfield":
+        assert (ref[:, 2] >= 0).any(), "no occluded pixel"
 
 
 @pytest.mark.parametrize("any_hit", [False, True])
@@ -174,6 +178,7 @@ def test_raycast_frame_odd_shapes(shape, order):
     count = width * height if count is None else count
     sc = small_heightfield(width=width, height=height)
     sc.settings["tracer"] = "ray"
+    sc.light_direction = (-1.0, -0.25, -0.2)  # a low light: the hills shadow the valleys
     with CudaTracer(0) as t:
         t.initializeBuffers(sc)
         t.set_traversal_order(order)
@@ -187,6 +192,8 @@ def test_raycast_frame_odd_shapes(shape, order):
                                          pixel_start=start)
     assert np.array_equal(gpu, ref), f"{(gpu != ref).any(axis=1).sum()} of {count} pixels differ"
     assert (ref[:, 0] >= 0).any()
+    if count > 1000:
+        assert (ref[:, 2] >= 0).any()  # occluded pixels
 
 
 def test_cast_with_shadow_ray_lists():

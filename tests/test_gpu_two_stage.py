@@ -31,8 +31,8 @@ for which in ("room", "heightfield"):
     for order in (N.RC_ORDER_REFERENCE, N.RC_ORDER_NEAREST):
         sc = small_room() if which == "room" else small_heightfield()
         sc.settings["tracer"] = "ray"
-        if which == "room":
-            sc.light_direction = (-0.3, -1.0, -0.2)
+        # lights under which both scenes have shadowed pixels
+        sc.light_direction = (-0.3, -1.0, -0.2) if which == "room" else (-1.0, -0.25, -0.2)
         with CudaTracer(0) as t:
             t.initializeBuffers(sc)
             t.set_traversal_order(order)
@@ -45,6 +45,7 @@ for which in ("room", "heightfield"):
         ref, _ = oracle.Oracle(sc).raycast32(camera_floats(camera_record(sc)), sc.width, sc.width * sc.height, L,
                                              order=order)
         assert np.array_equal(gpu, ref), (which, order, int((gpu != ref).any(axis=1).sum()))
+        assert (ref[:, 2] >= 0).any(), "no occluded pixel"
 
 sc = small_heightfield(width=1920, height=1080)
 sc.settings["tracer"] = "ray"
