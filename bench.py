@@ -10,11 +10,14 @@ BVH queries (primary + shadow) per second.
             step, outside the timed events)
   e2e       the same frame through the C ABI with host buffers:
             rc_cast_with_shadow(pinned host rays -> pinned host results), the
-            copies inside the timed region
-  roofline  the primary closest-hit kernel: algorithmic bytes per launch
-            (64 B per inner-node fetch + 48 B per triangle test, counted by a
-            counting render that equals the float32 oracle's count, + 16 B
-            result and 8 B queue entry per pixel) / its average event time
+            host-link traffic inside the timed region (the kernel reads the
+            rays and writes the records in place)
+  roofline  the frame's kernel (primary and shadow rays in one kernel; with
+            RC_TRACE_FUSED=0 the primary kernel of the two): algorithmic
+            bytes per launch (64 B per inner-node fetch + 48 B per triangle
+            test, counted by a counting render that equals the float32
+            oracle's count, + 16 B record per pixel; + 8 B queue entry per
+            hit pixel in the two-kernel form) / its average event time
 
 `--impl reference` times the reference's CPU ray casting on this host's cores
 (the reference's own code where it was compiled, else the float64 port) on
