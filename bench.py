@@ -540,10 +540,10 @@ def run_nrc(args, rank, world):
 
 
 def run_cpu(args, rank, world):
-    """CPU side of the baseline table on this host's cores (the float64 port
-    of the reference's path tracer, all threads): config 0, the room at
-    320x240, 16 spp, depth 4, a full frame (best of 3); config 2, an estimate
-    for the 64-scene batch, each triangle bucket's first scene sampled on
+    """CPU path-tracing throughput on this host's cores (the float64 port of
+    the reference's path tracer, all threads): the room at 320x240, 16 spp,
+    depth 4, a full frame (best of 3); and an estimate for the 64-scene
+    batch, each triangle bucket's first scene sampled on
     16,384 pixels at depth 8 without roulette (the reference has none), its
     Mrays/s and rays per sample applied to every scene of the bucket."""
     if rank != 0:
