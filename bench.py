@@ -13,11 +13,16 @@ BVH queries (primary + shadow) per second.
             host-link traffic inside the timed region (the kernel reads the
             rays and writes the records in place)
   roofline  the frame's kernel (primary and shadow rays in one kernel; with
-            RC_TRACE_FUSED=0 the primary kernel of the two): algorithmic
-            bytes per launch (64 B per inner-node fetch + 48 B per triangle
-            test, counted by a counting render that equals the float32
-            oracle's count, + 16 B record per pixel; + 8 B queue entry per
-            hit pixel in the two-kernel form) / its average event time
+            RC_TRACE_FUSED=0 the primary kernel of the two) against the roof
+            that binds it, instruction issue: warp instructions per launch
+            (ncu) / its average event time, over 4 warp instructions per
+            cycle per SM at the sampled SM clock. Beside it the HBM fraction
+            (ncu DRAM bytes per launch / event time / measured copy
+            bandwidth), ncu's L1 / L2 throughput fractions and the
+            algorithmic bytes per launch (64 B per inner-node fetch + 48 B
+            per triangle test, counted by a counting render that equals the
+            float32 oracle's count, + 16 B record per pixel; + 8 B queue
+            entry per hit pixel in the two-kernel form)
 
 `--impl reference` times the reference's CPU ray casting on this host's cores
 (the reference's own code where it was compiled, else the float64 port) on
@@ -161,16 +166,65 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def profiled_traffic(fused=False):
-    """DRAM bytes per launch of the frame's dominant kernel (the one-kernel
-    frame of primary + shadow rays, or the two-stage frame's primary kernel)
-    from the committed ncu summary, or None."""
+def profiled_metrics(fused=False):
+    """Figures of one launch of the frame's dominant kernel (the one-kernel
+    frame of primary + shadow rays, or the two-kernel frame's primary kernel)
+    from the committed ncu summary: DRAM bytes, warp instructions executed and
+    the issue / L1 / L2 / DRAM throughput fractions ncu reported. Empty when
+    the summary is missing."""
     f = ROOT / "profiles" / ("raycast_frame_fused_heightfield_1080p.md" if fused
                              else "raycast_primary_heightfield_1080p.md")
     if not f.exists():
-        return None
-    m = re.search(r"dram_bytes_per_launch:\s*([0-9.eE+]+)", f.read_text())
-    return float(m.group(1)) if m else None
+        return {}
+    text = f.read_text()
+    out = {}
+    for key in ("dram_bytes_per_launch", "warp_instructions_per_launch", "issue_active_frac", "l1_throughput_frac",
+                "l2_throughput_frac", "dram_throughput_frac"):
+        m = re.search(rf"^{key}:\s*([0-9.eE+]+)", text, re.M)
+        if m:
+            out[key] = float(m.group(1))
+    return out
+
+
+def profiled_traffic(fused=False):
+    """DRAM bytes per launch of the frame's dominant kernel from the committed
+    ncu summary, or None."""
+    return profiled_metrics(fused).get("dram_bytes_per_launch")
+
+
+def issue_roofline(prof, launch_s, sm_mhz, num_sms, alg_bytes, traffic, hbm_peak, peak_kind):
+    """The frame kernel against the roof that binds it: instruction issue.
+
+    The node array (17.6 MB) and the triangles the rays touch stay in L1/L2,
+    so DRAM moves a fraction of a percent of the algorithmic bytes and HBM is
+    not the bound; ncu shows the schedulers issuing in about three cycles of
+    four (ALU pipe: the slab tests' min/max and compares). So:
+      achieved = warp instructions of one launch (ncu; the count is fixed by
+                 the frame's work) / the launch's CUDA-event time
+      peak     = 4 warp instructions per cycle per SM (one per scheduler)
+                 x SMs x the median SM clock sampled in the timed region
+    The HBM fraction (ncu DRAM bytes of one launch / event time / the
+    measured copy bandwidth) and ncu's L1 / L2 throughput fractions are
+    reported beside it, with the algorithmic bytes per second."""
+    out = {"bound": "issue", "unit": "G warp-instructions/s", "achieved": None, "peak": None, "frac": None,
+           "avg_launch_ms": round(launch_s * 1e3, 4), "traffic": traffic,
+           "algorithmic_bytes_per_launch": int(alg_bytes),
+           "algorithmic_gbs": round(alg_bytes / launch_s / 1e9, 1)}
+    inst = prof.get("warp_instructions_per_launch")
+    if inst and sm_mhz:
+        achieved = inst / launch_s / 1e9
+        peak = 4.0 * num_sms * sm_mhz / 1e3
+        out.update(achieved=round(achieved, 1), peak=round(peak, 1), frac=round(achieved / peak, 4),
+                   peak_kind=f"4 warp-instructions/cycle/SM x {num_sms} SMs x {sm_mhz:.0f} MHz (median sampled)",
+                   warp_instructions_per_launch=inst)
+    hbm = {"peak_gbs": hbm_peak, "peak_kind": peak_kind, "achieved_gbs": None, "frac": None}
+    if traffic:
+        hbm["achieved_gbs"] = round(traffic / launch_s / 1e9, 1)
+        hbm["frac"] = round(traffic / launch_s / 1e9 / hbm_peak, 5)
+    out["hbm"] = hbm
+    out["ncu_fracs"] = {k: prof[k] for k in ("issue_active_frac", "l1_throughput_frac", "l2_throughput_frac",
+                                             "dram_throughput_frac") if k in prof}
+    return out
 
 
 def reduce_replicas(times, counts, world, device):
@@ -199,13 +253,19 @@ def cpu_threads():
 # CPU reference / port timing (one full frame per step)
 
 def cpu_raycast(sc, steps, warmup, bvh):
+    """The reference's ray casting of the frame on this host's cores: its own
+    code where oracle/_ref was built, else the float64 port (the oracle's
+    own BVH unless `bvh` is given, its float64 camera). Loads no part of the
+    product library."""
     import oracle
-    from raycer_gb300.tracer import camera_record
 
     threads = cpu_threads()
+    build_s = 0.0
     if oracle.ref_available(fast=True):
         kind = "reference"
+        t_build = time.perf_counter()
         ref = oracle.RefScene(sc, fast=True)
+        build_s = time.perf_counter() - t_build
         ref.set_general(0, 3, 1, 1)
 
         def frame():
@@ -213,10 +273,10 @@ def cpu_raycast(sc, steps, warmup, bvh):
             return rays, sec
     else:
         kind = "port"
+        t_build = time.perf_counter()
         orc = oracle.Oracle(sc, prebuilt=bvh)
-        cam = camera_record(sc)
-        cam64 = np.array(list(cam.position) + list(cam.right) + list(cam.up) + list(cam.image_plane_center) +
-                         [cam.aspect_ratio, cam.image_plane_width, cam.image_plane_height], np.float64)
+        build_s = time.perf_counter() - t_build
+        cam64 = oracle.camera64_of(sc)
         L = -np.array(sc.light_direction, np.float64)
         n = sc.width * sc.height
 
@@ -231,43 +291,44 @@ def cpu_raycast(sc, steps, warmup, bvh):
         tot_rays += rays
         tot_sec += sec
         best = max(best, rays / sec / 1e6)
-    return {"kind": kind, "cores": threads, "value": tot_rays / tot_sec / 1e6, "best": best,
+    return {"kind": kind, "cores": threads, "value": tot_rays / tot_sec / 1e6, "best": best, "bvh_build_s": build_s,
             "rays_per_frame": tot_rays // max(steps, 1), "sec_per_frame": tot_sec / max(steps, 1)}
 
 
 # ---------------------------------------------------------------------------
 
+def bench_config():
+    """The workload both arms time, by the same keys (how each arm runs it
+    goes elsewhere in its line)."""
+    return {"workload": WORKLOAD, "pixels": 1920 * 1080, "triangles": 1_045_506, "spp": 1,
+            "rays": "1 primary closest hit per pixel + 1 directional-light shadow any-hit per primary hit"}
+
+
 def run_reference(args, rank, world):
+    """The reference's CPU ray casting of the same frame on this host's cores:
+    the reference's own code where it was compiled here (oracle/_ref), else
+    the float64 port, which builds its BVH itself with its restatement of
+    FlatBVH::build (FlatBVH.cpp:89-204) outside the timed region. Nothing of
+    the product library is loaded."""
     if rank != 0:
         return 0
     from raycer_gb300 import scenes
     sc = scenes.heightfield_scene()
-    bvh = None
     try:
-        import oracle
-        if not oracle.ref_available(fast=True):
-            import ctypes as C
-            from raycer_gb300 import _native as N
-            v = np.ascontiguousarray(sc.vertices)
-            cnt = C.c_int64(0)
-            N.lib().rc_build_bvh(C.c_void_p(v.ctypes.data), v.shape[0], 4, None, 0, C.byref(cnt), None, None)
-            nodes = np.empty(cnt.value, oracle.NODE_DTYPE)
-            order = np.empty(v.shape[0], np.uint64)
-            N.lib().rc_build_bvh(C.c_void_p(v.ctypes.data), v.shape[0], 4, C.c_void_p(nodes.ctypes.data),
-                                 cnt.value, C.byref(cnt), C.c_void_p(order.ctypes.data), None)
-            bvh = (nodes, order)
+        res = cpu_raycast(sc, args.steps, args.warmup, None)
     except ImportError as e:
         print(json.dumps({"impl": "reference", "unavailable": f"oracle not built: {e}"}))
         return 0
-    res = cpu_raycast(sc, args.steps, args.warmup, bvh)
     line = {
         "impl": "reference", "metric": METRIC, "value": round(res["value"], 3), "unit": METRIC,
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(res["sec_per_frame"] * 1e3, 3), "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded fBm heightfield)",
-        "config": {"workload": WORKLOAD, "rays_per_step": int(res["rays_per_frame"])},
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded fBm heightfield, value noise seed 2)",
+        "config": bench_config(),
+        "rays_per_step": int(res["rays_per_frame"]),
         "cpu_baseline": {"value": round(res["value"], 3), "unit": METRIC, "cores": res["cores"], "kind": res["kind"],
-                         "sample": "full 1920x1080 frame per step (all pixels, primary + shadow rays)"},
+                         "sample": "full 1920x1080 frame per step (all pixels, primary + shadow rays)",
+                         "bvh_build_s": round(res["bvh_build_s"], 2)},
         "e2e": {"value": round(res["value"], 3), "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -296,6 +357,7 @@ def run_ours(args, rank, local_rank, world):
     sc = scenes.heightfield_scene()
     n_pix = sc.width * sc.height
     tracer = CudaTracer(local_rank)
+    num_sms = torch.cuda.get_device_properties(local_rank).multi_processor_count
     tracer.initializeBuffers(sc)
     tracer.initializeImageBuffers(sc.width, sc.height)
     tracer.set_traversal_order(N.RC_ORDER_NEAREST if args.order == "nearest" else N.RC_ORDER_REFERENCE)
@@ -376,7 +438,6 @@ def run_ours(args, rank, local_rank, world):
     e2e_sec = time.perf_counter() - t0
     e2e_rays = rays_per_call * args.steps
 
-    bvh = tracer.get_bvh() if rank == 0 else None
 
     dev_sec, e2e_sec, t_wall, total_rays, e2e_rays = reduce_replicas(
         (dev_sec, e2e_sec, t_wall), (total_rays, e2e_rays), world, torch.device("cuda", local_rank))
@@ -399,35 +460,31 @@ def run_ours(args, rank, local_rank, world):
             prim_bytes = 64 * s0_nodes + 48 * s0_tris + 16 * n_pix + 8 * hits
         prim_avg = statistics.mean(prim_ms) / 1e3
         achieved = prim_bytes / prim_avg / 1e9
-        traffic = profiled_traffic(fused)
+        prof = profiled_metrics(fused)
+        traffic = prof.get("dram_bytes_per_launch")
+        clk = clocks.summary()
+        roofline = issue_roofline(prof, prim_avg, clk.get("sm_mhz"), num_sms, prim_bytes, traffic, peak, peak_kind)
         line = {
             "metric": METRIC, "value": round(total_rays / dev_sec / 1e6, 2), "unit": METRIC,
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(dev_sec / args.steps * 1e3, 4), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded fBm heightfield, value noise seed 2)",
-            "config": {"workload": WORKLOAD, "rays_per_step": int(rays[0]), "pixels": n_pix,
-                       "traversal_order": args.order, "l2": "flushed (512 MB write) before every step",
-                       "parallelism": f"replicas x{world}"},
+            "config": bench_config(),
+            "rays_per_step": int(rays[0]),
+            "setup": {"traversal_order": args.order, "l2": "flushed (512 MB write) before every step",
+                      "parallelism": f"replicas x{world}"},
             "e2e": {"value": round(e2e_rays / e2e_sec / 1e6, 2), "unit": METRIC,
                     "h2d_bytes_per_step": n_pix * 32, "d2h_bytes_per_step": n_pix * 16},
             "gpu_launches": (1 if fused else 2) * args.steps,
-            "roofline": {"bound": "hbm",
-                         "kernel": "k_raycast_primary (closest hit + shadow any-hit, one kernel)" if fused
-                         else "k_raycast_primary (closest hit)",
-                         "achieved": round(achieved, 1),
-                         "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
-                         "algorithmic_bytes_per_launch": int(prim_bytes),
-                         "avg_launch_ms": round(prim_avg * 1e3, 4),
-                         "traffic": traffic,
-                         "node_fetches": int(k_nodes), "triangle_tests": int(k_tris),
-                         # BVH-node bytes (64 B per inner-node fetch) per second of the kernel
-                         "bvh_node_gbs": round(k_nodes * 64 / prim_avg / 1e9, 1),
-                         # HBM bytes actually moved (ncu DRAM read + write of one launch) per second:
-                         # the nodes and touched triangles are served from L1/L2
-                         "dram_gbs": round(traffic / prim_avg / 1e9, 1) if traffic else None},
+            "roofline": dict(roofline,
+                             kernel="k_raycast_primary (closest hit + shadow any-hit, one kernel)" if fused
+                             else "k_raycast_primary (closest hit)",
+                             node_fetches=int(k_nodes), triangle_tests=int(k_tris),
+                             # BVH-node bytes (64 B per inner-node fetch) per second of the kernel
+                             bvh_node_gbs=round(k_nodes * 64 / prim_avg / 1e9, 1)),
             "stages_ms": {"primary": round(statistics.mean(prim_ms), 4), "shadow": round(statistics.mean(shadow_ms), 4)},
             "wall_s": round(t_wall, 3),
-            "clocks": clocks.summary(),
+            "clocks": clk,
         }
     if world > 1:
         torch.distributed.barrier()
@@ -436,7 +493,7 @@ def run_ours(args, rank, local_rank, world):
     if rank == 0:
         if world == 1:
             try:
-                res = cpu_raycast(sc, 2, 1, bvh)
+                res = cpu_raycast(sc, 2, 1, None)
                 line["cpu_baseline"] = {"value": round(res["value"], 3), "unit": METRIC, "cores": res["cores"],
                                         "kind": res["kind"],
                                         "sample": "full 1920x1080 frame (primary + shadow rays), 1 warm-up + 2 "

@@ -42,7 +42,7 @@ typedef enum rc_status
     RC_OOM = 2,          /* device or host allocation refused              */
     RC_CUDA = 3,         /* a CUDA runtime call failed (message has it)    */
     RC_CANCELLED = 4,    /* the caller's cancel flag was raised            */
-    RC_TIMEOUT = 5,      /* a kernel's iteration budget ran out            */
+    RC_TIMEOUT = 5,      /* the render's time budget ran out (rc_set_time_budget) */
     RC_NOT_READY = 6,    /* call order: e.g. render before upload/resize   */
     RC_UNSUPPORTED = 7,  /* valid in the reference, not in this build      */
     RC_DEVICE_ERROR = 8, /* a kernel reported an error status (e.g. stack) */
@@ -308,12 +308,36 @@ rc_status rc_clear(rc_tracer* h);
  * (NetworkRunner.cpp:398-417). PATH: adds filter-weighted samples to the
  * film. RAY: casts the primary ray of every pixel and, for each hit, one
  * shadow ray per directional light, into the cast buffer (rc_read_cast).
- * cancel: optional host flag polled between launches; when it is non-zero
- * the call returns RC_CANCELLED with the film holding whole passes only.
- * pixels_processed: optional; set to pixel_count on success
- * (Tracer.cpp:111-112, CLTracer.cpp:304). Blocks until the device is done. */
+ * Blocks until the device is done.
+ *
+ * Progress and cancellation, as Tracer::run's `interrupted` check and
+ * pixelsProcessed updates (Tracer.cpp:76-112) read by a second thread
+ * (ConsoleRunner.cpp:126-142):
+ *   cancel (optional): a flag another host thread may raise at any time
+ *     during the call. The calling thread forwards it to a word in pinned,
+ *     device-mapped host memory that the kernels check every 64 work items
+ *     (of 32 rays or paths); they then take no more work. The call returns
+ *     RC_CANCELLED. A RAY frame keeps the records of the pixels it traced
+ *     (the others are untouched); a PATH film keeps whole passes only.
+ *   pixels_processed (optional): set to 0 at entry; while the kernels run
+ *     the calling thread stores into it (relaxed atomic stores of a
+ *     uint64_t, so another thread may read it with an atomic load, e.g.
+ *     through a std::atomic<uint64_t> of the same object) the pixels the
+ *     device reports finished: RAY frames per 32-pixel work item, PATH
+ *     renders per pass as each pass's film update lands. At the end it
+ *     holds the pixels finished: pixel_count on success.
+ * A cancel flag or progress counter makes the calling thread wait by
+ * polling (it yields between polls) instead of sleeping in the driver. */
 rc_status rc_render(rc_tracer* h, uint64_t pixel_start, uint64_t pixel_count,
                     const volatile int32_t* cancel, uint64_t* pixels_processed);
+
+/* Time budget of every later rc_render on this handle (GPU-only extension;
+ * the reference has no counterpart): the kernels stop taking work once
+ * `milliseconds` of device time have passed since the render's first work
+ * item (checked every 64 work items), and the call returns RC_TIMEOUT with
+ * the results of rc_render's cancel case. 0 stops at the first check (no
+ * work done); a negative value removes the budget (the default). */
+rc_status rc_set_time_budget(rc_tracer* h, double milliseconds);
 
 /* Film::generateToneMappedImage (Film.cpp:61-69) with the handle's tone
  * mapper (ReinhardToneMapper::apply, ReinhardToneMapper.cpp:18-86), and the
@@ -365,7 +389,12 @@ rc_status rc_cast_with_shadow(rc_tracer* h, const rc_ray* rays, int64_t n, int32
  * returns RC_INVALID_ARG. Every call on every handle shares that array, so
  * calls that overlap on the GPU race. The first call on a device looks up the
  * array's address (once per device); make that first call before any stream
- * capture begins. */
+ * capture begins. The rays are a list, walked one ray per lane: even a whole
+ * camera frame in pixel order does not get the warp-wide tile walk of RAY
+ * renders, so this form is slower than rc_cast_with_shadow on such frames.
+ * With rc_set_counting on it runs the counted two-kernel form (same scratch)
+ * and reports node and triangle counts; rc_get_stats then describes this
+ * call alone, with times of 0. */
 rc_status rc_cast_with_shadow_device_noalloc(rc_tracer* h, const rc_ray* d_rays, int64_t n, int32_t order,
                                              rc_cast_pixel* d_out);
 
@@ -555,7 +584,12 @@ typedef struct rc_nrc_config
     uint64_t seed;              /* weight initialisation and training-slot choice    */
     int32_t lookup_kernel;      /* RC_NRC_TCGEN05 (tcgen05.mma, TMEM accumulators;   */
                                 /* default) or RC_NRC_MMA_SYNC (warp-level mma.sync) */
-    int32_t reserved;           /* 0                                                 */
+    int32_t tc_wait_polls;      /* RC_NRC_TCGEN05: polls of each bounded mbarrier    */
+                                /* wait for an MMA before the kernel gives up and    */
+                                /* the call reports RC_DEVICE_ERROR; 0 = default     */
+                                /* (4,194,304); < 0 = none, so every wait gives up   */
+                                /* at once (exercises that error path; the kernel    */
+                                /* still lets its MMAs finish before it frees TMEM)  */
 } rc_nrc_config;
 
 typedef enum rc_nrc_lookup_kernel { RC_NRC_MMA_SYNC = 0, RC_NRC_TCGEN05 = 1 } rc_nrc_lookup_kernel;

@@ -404,6 +404,60 @@ class RefScene:
         return out
 
 
+def camera_state64(position, pitch: float, yaw: float, roll: float, fov: float, width: int,
+                   height: int) -> np.ndarray:
+    """The perspective camera's float64 state after a non-interactive
+    Camera::update (Camera.cpp:48-284) and Camera::setImagePlaneSize
+    (Camera.cpp:29-34), in the layout of ``RefScene.camera_state``: position,
+    forward, right, up, image-plane centre (3 each), aspect = height / width,
+    width - 1, height - 1, image-plane distance.
+
+    forward = EulerAngle::getDirection (EulerAngle.cpp:77-87) of the pitch
+    clamped to [-89, 89] and both angles wrapped into [-180, 180]
+    (EulerAngle::clampPitch / normalize); right, up = ONB::fromNormal
+    (ONB.cpp:32-39) with Vector3::ALMOST_UP (Vector3.cpp:15); the image-plane
+    centre uses the direction of the angles before clamping, at distance
+    0.5 / tan(fov / 2), fov horizontal in [1, 180] degrees. Roll is unused by
+    the basis, as in the reference."""
+    import math
+
+    d2r = math.pi / 180.0
+
+    def unit(a):
+        n = math.sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2])
+        return (a[0] / n, a[1] / n, a[2] / n)
+
+    def cross(a, b):
+        return (a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0])
+
+    def direction(p, y):
+        return unit((-math.sin(y * d2r) * math.cos(p * d2r), math.sin(p * d2r), -math.cos(y * d2r) * math.cos(p * d2r)))
+
+    def wrap(a):
+        while abs(a) > 180.0:
+            a += -360.0 if a > 0.0 else 360.0
+        return a
+
+    pos = tuple(float(x) for x in position)
+    fwd0 = direction(float(pitch), float(yaw))
+    p = wrap(min(89.0, max(-89.0, float(pitch))))
+    y = wrap(float(yaw))
+    f = max(1.0, min(float(fov), 180.0))
+    ipd = 0.5 / math.tan((f / 2.0) * d2r)
+    w = direction(p, y)
+    u = unit(cross(w, (0.0001, 1.0, 0.0001)))
+    v = unit(cross(u, w))
+    centre = tuple(pos[k] + fwd0[k] * ipd for k in range(3))
+    return np.array([*pos, *w, *u, *v, *centre, float(height) / float(width), float(width - 1), float(height - 1),
+                     ipd], np.float64)
+
+
+def camera64_of(scene) -> np.ndarray:
+    """``raycast64`` camera input of a scene description (float64 throughout)."""
+    c = scene.camera
+    return cam64_from_state(camera_state64(c.position, c.pitch, c.yaw, c.roll, c.fov, scene.width, scene.height))
+
+
 def cam64_from_state(state19: np.ndarray) -> np.ndarray:
     """Camera64 input (pos, right, up, centre, aspect, ipw, iph) from the reference camera state."""
     s = np.asarray(state19, np.float64)

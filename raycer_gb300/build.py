@@ -25,7 +25,11 @@ CSRC = PKG / "csrc"
 BUILD = ROOT / "_build"
 LIB = PKG / "lib" / "libraycer_gb300.so"
 ORACLE_LIB = ROOT / "oracle" / "lib" / "liboracle.so"
-REFERENCE_SRC = Path("/root/reference")
+# The reference checkout whose hot path oracle/_ref is compiled from:
+# $RAYCER_REFERENCE_DIR, else a directory named "reference" beside the
+# repository. Where it is absent (e.g. on a machine with only this
+# repository) the oracle runs on its own restatement.
+REFERENCE_SRC = Path(os.environ.get("RAYCER_REFERENCE_DIR") or (ROOT.parent / "reference"))
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["trace.cu", "pathtrace.cu", "tonemap.cu", "noalloc.cu", "nrc.cu", "nrc_tc.cu", "gpu_build.cu"]

@@ -12,9 +12,11 @@
 #pragma once
 
 #include <atomic>
+#include <chrono>
 #include <cstdint>
 #include <stdexcept>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/raycer_gb300.h"
@@ -107,16 +109,49 @@ public:
         check(rc_release_scene(handle), "Could not release the scene buffers");
     }
 
-    // CLTracer::run (CLTracer.cpp:262-305). `interrupted` is honoured between
-    // device passes (the OpenCL tracer ignores it).
-    void run(TracerStateArrays& state, std::atomic<bool>& interrupted)
+    // CLTracer::run (CLTracer.cpp:262-305) with Tracer::run's progress and
+    // interruption contract (Tracer.cpp:76-112): `progress` (by default the
+    // state's pixelsProcessed) advances while the kernels run, so another
+    // thread can poll it as ConsoleRunner does every 100 ms
+    // (ConsoleRunner.cpp:126-142); setting `interrupted` from another thread
+    // stops the render at its kernels' next work-queue check, and run throws
+    // like any failed call. A watcher thread turns the std::atomic<bool> into
+    // the library's 32-bit cancel word (checked every half millisecond).
+    void run(TracerStateArrays& state, std::atomic<bool>& interrupted, std::atomic<uint64_t>* progress = nullptr)
     {
+        static_assert(sizeof(std::atomic<uint64_t>) == sizeof(uint64_t) && std::atomic<uint64_t>::is_always_lock_free,
+                      "the library stores progress into the atomic's object representation");
+        static_assert(sizeof(std::atomic<int32_t>) == sizeof(int32_t) && std::atomic<int32_t>::is_always_lock_free,
+                      "the library reads the cancel word through the atomic's object representation");
         check(rc_set_camera(handle, &state.camera), "Could not set the camera");
-        volatile int32_t cancel = interrupted.load() ? 1 : 0;
-        uint64_t done = 0;
-        uint64_t count = state.pixelCount ? state.pixelCount : imageWidth * imageHeight;
-        check(rc_render(handle, state.pixelStartOffset, count, &cancel, &done), "Could not run the tracer");
-        state.pixelsProcessed = done;
+        if (!progress)
+            progress = &state.pixelsProcessed;
+        std::atomic<int32_t> cancel{ interrupted.load() ? 1 : 0 };
+        std::atomic<bool> finished{ false };
+        std::thread watcher([&] {
+            while (!finished.load(std::memory_order_acquire))
+            {
+                if (interrupted.load())
+                {
+                    cancel.store(1);
+                    return;
+                }
+                std::this_thread::sleep_for(std::chrono::microseconds(500));
+            }
+        });
+        const uint64_t count = state.pixelCount ? state.pixelCount : imageWidth * imageHeight;
+        const rc_status st = rc_render(handle, state.pixelStartOffset, count,
+                                       reinterpret_cast<const volatile int32_t*>(&cancel),
+                                       reinterpret_cast<uint64_t*>(progress));
+        finished.store(true, std::memory_order_release);
+        watcher.join();
+        check(st, "Could not run the tracer");
+    }
+
+    // Time budget of later renders (rc_set_time_budget; negative: none).
+    void setTimeBudget(double milliseconds)
+    {
+        check(rc_set_time_budget(handle, milliseconds), "Could not set the time budget");
     }
 
     // CLTracer::downloadImage (CLTracer.cpp:307-323): tone-mapped RGBA floats.

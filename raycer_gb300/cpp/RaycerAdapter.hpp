@@ -163,8 +163,8 @@ public:
         s.filmHeight = state.filmHeight;
         s.pixelStartOffset = state.pixelStartOffset;
         s.pixelCount = state.pixelCount;
-        tracer.run(s, interrupted);
-        state.pixelsProcessed = s.pixelsProcessed.load();
+        // the render advances the reference's own counter while it runs
+        tracer.run(s, interrupted, &state.pixelsProcessed);
     }
 
     Raycer::Image downloadImage()

@@ -110,6 +110,20 @@ struct __align__(16) DevInstance
     int identity;  // 1: A = I, b = 0 (no transform needed)
 };
 
+// Progress and stop word of one render (rc_render): pinned host memory mapped
+// into the device's address space, so the persistent kernels read the
+// caller's cancel request and publish their progress while they run. Both
+// fields cross the host link, so the kernels touch them once per 64 work
+// items only.
+struct RenderMonitor
+{
+    volatile int cancel;                 // host -> device: non-zero = stop taking work
+    int pad;
+    volatile unsigned long long pixels;  // device -> host: pixels finished so far
+};
+
+constexpr unsigned long long kNoBudget = ~0ull;
+
 // Device scene handed to every kernel by value. Two-level scenes
 // (numInstances > 0) keep every mesh's BVH in `nodes` / `tris` / `shade`
 // (links already offset into the pools) and a top-level BVH over the
@@ -132,6 +146,8 @@ struct DevScene
     int wideRoot;          // >= 0: DevNode4 0; < 0: the root is a leaf
     int ropeCount;         // records in `ropes`
     const DevRope* ropes;  // the stackless walk's records of a single-level scene, or null
+    RenderMonitor* monitor = nullptr;          // rc_render with a cancel flag or progress counter, else null
+    unsigned long long budgetNs = kNoBudget;   // rc_render's time budget (kNoBudget: none)
 };
 
 // Float32 camera record used by the kernels (same fields as rc_camera).

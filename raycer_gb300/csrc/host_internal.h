@@ -180,17 +180,46 @@ struct rc_tracer
     // FP64 RMSE scratch (rc_film_rmse_f64)
     void* dRmse = nullptr;
     size_t capRmse = 0;
+
+    // rc_render's progress / cancel word: pinned host memory mapped into the
+    // device (monHost, and monDev as the kernels address it), and the time
+    // budget of rc_set_time_budget.
+    rcx::RenderMonitor* monHost = nullptr;
+    rcx::RenderMonitor* monDev = nullptr;
+    unsigned long long budgetNs = rcx::kNoBudget;
 };
 
 namespace rcx
 {
 
+// One rc_render call's monitoring. `dev` (the kernels' monitor pointer) is
+// set when the caller passed a cancel flag or a progress counter; budgetNs
+// when the handle has a time budget. wait_render forwards the caller's flag
+// to the device and the device's progress to the caller while the render's
+// kernels run.
+struct RenderWatch
+{
+    RenderMonitor* dev = nullptr;
+    unsigned long long budgetNs = kNoBudget;
+    const volatile int32_t* cancel = nullptr;
+    uint64_t* pixels = nullptr;
+    uint64_t seen = 0;
+};
+// Blocks until `done` has completed; while it waits, raises the device's
+// cancel word once the caller's flag is set and stores every larger
+// progress value it reads into the caller's counter (relaxed atomic stores).
+rc_status wait_render(rc_tracer* h, RenderWatch* w, cudaEvent_t done);
+// Status of a render whose control block reads `error` (stack overflow,
+// cancel, time budget; RC_OK for none of them). Sets the message.
+rc_status render_outcome(rc_tracer* h, int error, const char* what);
+
 // dOrigins (optional): per shadow-queue entry, the shadow ray's origin
-// (launch_raycast's shadowOrigins).
+// (launch_raycast's shadowOrigins). watch: rc_render's monitoring, or null.
 rc_status raycast_into(rc_tracer* h, const rc_ray* dRays, uint64_t pixelStart, uint64_t count, int order,
-                       rc_cast_pixel* dOut, int* dQueue, float4* dOrigins = nullptr);
-rc_status render_raycast(rc_tracer* h, uint64_t pixelStart, uint64_t count, const rc_ray* dRays);
-rc_status render_path(rc_tracer* h, uint64_t pixelStart, uint64_t count, const volatile int32_t* cancel);
+                       rc_cast_pixel* dOut, int* dQueue, float4* dOrigins = nullptr, RenderWatch* watch = nullptr);
+rc_status render_raycast(rc_tracer* h, uint64_t pixelStart, uint64_t count, const rc_ray* dRays,
+                         RenderWatch* watch = nullptr);
+rc_status render_path(rc_tracer* h, uint64_t pixelStart, uint64_t count, RenderWatch* watch);
 void release_render_buffers(rc_tracer* h);
 // Scene construction (tracer_host.cpp), shared with the scene files (scene_file.cpp).
 void build_host_scene(const double* v, const uint32_t* matIdx, int64_t n, const rc_material* mats, int32_t matCount,

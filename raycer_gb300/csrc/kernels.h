@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
+
 #include "../../include/raycer_gb300.h"
 #include "device_types.h"
 
@@ -16,9 +18,17 @@ struct DevControl
 {
     unsigned int head[8];          // work-queue heads / queue counts
     unsigned long long stats[8];   // per stage s: [3s] rays, [3s+1] node fetches, [3s+2] triangle tests
-    int error;                     // bit0: traversal stack overflow
+    int error;                     // bit0: traversal stack overflow; bit1: radiance-cache wait ran out;
+                                   // bit2: cancelled; bit3: time budget ran out (kErr* below)
     int pad[3];
+    unsigned long long t0;         // %globaltimer at the render's first work-queue check (time budget)
+    unsigned long long progress;   // pixels finished (monitored renders)
 };
+
+constexpr int kErrStack = 1;
+constexpr int kErrCancelled = 4;
+constexpr int kErrBudget = 8;
+constexpr int kErrStop = kErrCancelled | kErrBudget;
 
 struct LaunchInfo
 {
@@ -26,6 +36,60 @@ struct LaunchInfo
     int numSMs;
     int counting;  // count node / triangle tests
 };
+
+// Resident blocks per SM of a persistent kernel, cached per device (the
+// query belongs to the current device's context); launchers multiply it by
+// the launching handle's SM count on every launch. Safe to call from
+// several host threads.
+constexpr int kMaxOccupancyDevices = 64;
+struct OccupancyCache
+{
+    std::atomic<int> perSM[kMaxOccupancyDevices];
+};
+
+// One-time per-device set-up (a kernel's function attributes belong to the
+// current device's context): runs `f` until it succeeds once on each device.
+struct DeviceOnce
+{
+    std::atomic<int> done[kMaxOccupancyDevices];
+};
+
+template <typename F>
+cudaError_t once_per_device(DeviceOnce& once, F&& f)
+{
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxOccupancyDevices)
+        return f();
+    if (once.done[dev].load(std::memory_order_acquire))
+        return cudaSuccess;
+    const cudaError_t e = f();
+    if (e == cudaSuccess)
+        once.done[dev].store(1, std::memory_order_release);
+    return e;
+}
+
+template <typename K>
+int blocks_per_sm(K kernel, int block, size_t smem, OccupancyCache& cache)
+{
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxOccupancyDevices)
+        dev = -1;
+    if (dev >= 0)
+    {
+        const int v = cache.perSM[dev].load(std::memory_order_relaxed);
+        if (v > 0)
+            return v;
+    }
+    int perSM = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kernel, block, smem) != cudaSuccess || perSM < 1)
+    {
+        cudaGetLastError();
+        return 1;
+    }
+    if (dev >= 0)
+        cache.perSM[dev].store(perSM, std::memory_order_relaxed);
+    return perSM;
+}
 
 // Whether uncounted reference-order queries (RAY-frame shadow rays, rc_cast
 // in RC_ORDER_REFERENCE) take the stackless walk (traverse_stackless) where

@@ -1,0 +1,102 @@
+// Cancel, time budget and progress of a render, on the device side.
+//
+// The reference's Tracer::run checks `interrupted` per pixel and advances
+// TracerState::pixelsProcessed every 100 pixels (Tracer.cpp:76-112), while
+// the main thread polls it every 100 ms (ConsoleRunner.cpp:126-142). Here the
+// persistent kernels take their work in items of 32 rays or path slots from
+// an atomic queue head; a monitored render (rc_render with a cancel flag, a
+// progress counter or a time budget) makes lane 0 of the warp that took
+// every 64th item:
+//   * read the host-mapped cancel word and check the time budget (measured
+//     from the render's first check, %globaltimer);
+//   * copy the device progress counter into the host-mapped monitor.
+// A warp that sees a stop records the reason in DevControl::error and pushes
+// the queue head past any item count, so every warp's next fetch ends its
+// loop: the items already taken finish, nothing else starts. Kernels that
+// follow in the same render find the stop bit at their start and return.
+// Nothing waits here, so a stop can never hang a kernel.
+#pragma once
+
+#include "kernels.h"
+
+namespace rcx
+{
+
+constexpr unsigned kPollItemsLog2 = 6;             // check every 64th work item
+constexpr unsigned kHeadPastEnd = 0x7fffffffu;     // above any queue or item count
+
+__device__ __forceinline__ unsigned long long global_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ bool monitored(const RenderMonitor* mon, unsigned long long budgetNs)
+{
+    return mon != nullptr || budgetNs != kNoBudget;
+}
+
+// Stop bit of an earlier kernel (or warp) of the render.
+__device__ __forceinline__ bool render_stopped(const DevControl* ctl)
+{
+    return (*reinterpret_cast<const volatile int*>(&ctl->error) & kErrStop) != 0;
+}
+
+// Lane 0 of the warp that took `item` (counted in 32-wide items) of the
+// queue whose head is `head`. mayStop = false only publishes progress.
+// Returns the stop reason (kErrCancelled / kErrBudget) or 0.
+static __device__ __noinline__ int poll_render(RenderMonitor* mon, unsigned long long budgetNs, DevControl* ctl,
+                                        unsigned* head, bool mayStop)
+{
+    int why = 0;
+    if (mayStop && budgetNs != kNoBudget)
+    {
+        const unsigned long long now = global_ns();
+        unsigned long long t0 = atomicCAS(&ctl->t0, 0ull, now);
+        if (t0 == 0ull)
+            t0 = now;
+        if (now - t0 >= budgetNs)
+            why = kErrBudget;
+    }
+    if (mon)
+    {
+        if (mayStop && mon->cancel)
+            why = kErrCancelled;
+        // a plain store: stores of two warps may land in either order, so the
+        // host keeps the largest value it has read
+        mon->pixels = *reinterpret_cast<const volatile unsigned long long*>(&ctl->progress);
+    }
+    if (why)
+    {
+        atomicOr(&ctl->error, why);
+        atomicMax(head, kHeadPastEnd);
+    }
+    return why;
+}
+
+// Whole warp, after its fetch of `base` (a multiple of 32) from `head`:
+// true when the warp must stop taking work.
+__device__ __forceinline__ bool warp_poll(RenderMonitor* mon, unsigned long long budgetNs, DevControl* ctl,
+                                          unsigned* head, unsigned base, bool mayStop)
+{
+    if (!monitored(mon, budgetNs) || ((base >> 5) & ((1u << kPollItemsLog2) - 1u)) != 0u)
+        return false;
+    int why = 0;
+    if ((threadIdx.x & 31u) == 0u)
+        why = poll_render(mon, budgetNs, ctl, head, mayStop);
+    return __shfl_sync(0xffffffffu, why, 0) != 0;
+}
+
+// Whole warp: adds the pixels the warp finished in this item (lanes with
+// `finished`) to the render's progress counter.
+__device__ __forceinline__ void warp_progress(const RenderMonitor* mon, DevControl* ctl, bool finished)
+{
+    if (!mon)
+        return;
+    const unsigned m = __ballot_sync(0xffffffffu, finished);
+    if ((threadIdx.x & 31u) == 0u && m)
+        atomicAdd(&ctl->progress, static_cast<unsigned long long>(__popc(m)));
+}
+
+}  // namespace rcx

@@ -115,7 +115,7 @@ extern "C" rc_status rc_cast_with_shadow_device_noalloc(rc_tracer* h, const rc_r
     rcx::LaunchInfo li;
     li.stream = h->stream;
     li.numSMs = h->numSMs;
-    li.counting = 0;
+    li.counting = h->counting;  // counted frames: the two-kernel form, same scratch
 
     // The array keeps the previous call's contents: the counters must start at zero.
     e = cudaMemsetAsync(ctl, 0, sizeof(rcx::DevControl), h->stream);
@@ -129,10 +129,21 @@ extern "C" rc_status rc_cast_with_shadow_device_noalloc(rc_tracer* h, const rc_r
         e = cudaStreamSynchronize(h->stream);
     if (e != cudaSuccess)
         return fail(h, RC_CUDA, std::string("cast_with_shadow_device_noalloc: ") + cudaGetErrorString(e));
+    // This call's statistics only, as rc_cast_with_shadow keeps them (the
+    // scene's build time stays); no events are recorded, so the times are 0.
+    const double buildMs = h->stats.build_ms;
+    h->stats = rc_stats{};
+    h->stats.build_ms = buildMs;
+    for (int k = 0; k < 2; ++k)
+    {
+        h->stats.stage_rays[k] = result.stats[3 * k + 0];
+        h->stats.stage_nodes[k] = result.stats[3 * k + 1];
+        h->stats.stage_tris[k] = result.stats[3 * k + 2];
+    }
     h->stats.rays_traced = result.stats[0] + result.stats[3];
-    h->stats.stage_rays[0] = result.stats[0];
-    h->stats.stage_rays[1] = result.stats[3];
-    if (result.error & 1)
+    h->stats.node_visits = result.stats[1] + result.stats[4];
+    h->stats.tri_tests = result.stats[2] + result.stats[5];
+    if (result.error & rcx::kErrStack)
         return fail(h, RC_DEVICE_ERROR, "cast_with_shadow_device_noalloc: traversal stack overflow");
     return RC_OK;
 }

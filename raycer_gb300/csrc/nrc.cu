@@ -23,6 +23,7 @@
 
 #include "nrc.cuh"
 #include "sampling.cuh"
+#include "kernels.h"
 #include "nrc_kernels.h"
 
 namespace rcx
@@ -649,18 +650,14 @@ int nrc_train_blocks(int numSMs) { return numSMs; }
 
 cudaError_t launch_nrc_infer(const NrcInferParams& p, int maxRecords, cudaStream_t stream, int numSMs)
 {
-    static int perSM = 0;
-    if (perSM == 0)
-    {
-        cudaError_t e =
-            cudaFuncSetAttribute(k_nrc_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, int(nrc_infer_smem()));
-        if (e != cudaSuccess)
-            return e;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_nrc_infer, kThreads, nrc_infer_smem()) !=
-                cudaSuccess ||
-            perSM < 1)
-            perSM = 1;
-    }
+    static DeviceOnce once;
+    static OccupancyCache occ;
+    cudaError_t e = once_per_device(once, [] {
+        return cudaFuncSetAttribute(k_nrc_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, int(nrc_infer_smem()));
+    });
+    if (e != cudaSuccess)
+        return e;
+    const int perSM = blocks_per_sm(k_nrc_infer, kThreads, nrc_infer_smem(), occ);
     int tiles = (maxRecords + 15) / 16;
     int grid = std::max(1, std::min((tiles + kWarps - 1) / kWarps, numSMs * perSM));
     k_nrc_infer<<<grid, kThreads, nrc_infer_smem(), stream>>>(p);
@@ -669,15 +666,12 @@ cudaError_t launch_nrc_infer(const NrcInferParams& p, int maxRecords, cudaStream
 
 cudaError_t launch_nrc_train(const NrcTrainParams& p, int blocks, cudaStream_t stream)
 {
-    static bool configured = false;
-    if (!configured)
-    {
-        cudaError_t e =
-            cudaFuncSetAttribute(k_nrc_train, cudaFuncAttributeMaxDynamicSharedMemorySize, int(nrc_train_smem()));
-        if (e != cudaSuccess)
-            return e;
-        configured = true;
-    }
+    static DeviceOnce once;
+    cudaError_t e = once_per_device(once, [] {
+        return cudaFuncSetAttribute(k_nrc_train, cudaFuncAttributeMaxDynamicSharedMemorySize, int(nrc_train_smem()));
+    });
+    if (e != cudaSuccess)
+        return e;
     k_nrc_train<<<blocks, kTThreads, nrc_train_smem(), stream>>>(p);
     return cudaGetLastError();
 }

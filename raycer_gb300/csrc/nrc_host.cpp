@@ -291,6 +291,7 @@ rc_status nrc_lookups(rc_tracer* h, const PassParams& pp)
     ip.weights = n.dW;
     ip.rec = pp.nrc.query;
     ip.count = n.dCounters;
+    ip.waitPolls = nrc_wait_polls(n.cfg.tc_wait_polls);
     ip.out = nullptr;
     ip.thr = pp.thr;
     ip.res = pp.res;
@@ -379,8 +380,8 @@ rc_status rc_nrc_configure(rc_tracer* h, const rc_nrc_config* c)
     if (!(c->learning_rate > 0.0f) || !(c->beta1 >= 0.0f && c->beta1 < 1.0f) || !(c->beta2 >= 0.0f && c->beta2 < 1.0f) ||
         !(c->epsilon > 0.0f))
         return fail(h, RC_INVALID_ARG, "nrc_configure: invalid optimizer settings");
-    if ((c->lookup_kernel != RC_NRC_MMA_SYNC && c->lookup_kernel != RC_NRC_TCGEN05) || c->reserved != 0)
-        return fail(h, RC_INVALID_ARG, "nrc_configure: unknown lookup kernel / reserved not 0");
+    if (c->lookup_kernel != RC_NRC_MMA_SYNC && c->lookup_kernel != RC_NRC_TCGEN05)
+        return fail(h, RC_INVALID_ARG, "nrc_configure: unknown lookup kernel");
     cudaSetDevice(h->device);
     h->nrc.cfg = *c;
     NRC_STATUS(alloc_state(h));
@@ -445,6 +446,7 @@ rc_status rc_nrc_infer(rc_tracer* h, const float* queries, int64_t n, float* rgb
     ip.weights = st.dW;
     ip.rec = static_cast<const NrcRecord*>(st.dApi);
     ip.count = st.dCounters + 2;
+    ip.waitPolls = nrc_wait_polls(st.cfg.tc_wait_polls);
     ip.out = static_cast<float*>(st.dApiOut);
     NRC_STATUS(encoding_box(h, ip.box));
     int errWord = 0;

@@ -42,7 +42,14 @@ struct NrcInferParams
     const float4* thr;       // res[tag] += thr[tag] * cache (out == nullptr)
     float4* res;
     NrcBox box;
+    unsigned waitPolls;      // tcgen05 kernel: polls per bounded MMA wait (0: give up at once)
 };
+
+// Polls per bounded mbarrier wait of a configuration's tc_wait_polls.
+inline unsigned nrc_wait_polls(int32_t configured)
+{
+    return configured == 0 ? (1u << 22) : configured < 0 ? 0u : unsigned(configured);
+}
 
 struct NrcTrainParams
 {

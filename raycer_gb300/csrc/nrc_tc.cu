@@ -34,6 +34,7 @@
 #include <algorithm>
 
 #include "nrc.cuh"
+#include "kernels.h"
 #include "nrc_kernels.h"
 
 namespace rcx
@@ -104,10 +105,12 @@ __device__ __forceinline__ void mma_commit(uint32_t bar)
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(bar));
 }
 
-// Bounded wait for the mbarrier phase `parity` to complete.
-__device__ __forceinline__ bool bar_wait(uint32_t bar, uint32_t parity)
+// Bounded wait for the mbarrier phase `parity` to complete: at most `polls`
+// polls (the MMA waits take NrcInferParams::waitPolls; the drain after a wait
+// ran out always takes kWaitLimit).
+__device__ __forceinline__ bool bar_wait(uint32_t bar, uint32_t parity, unsigned polls)
 {
-    for (unsigned i = 0; i < kWaitLimit; ++i)
+    for (unsigned i = 0; i < polls; ++i)
     {
         uint32_t done;
         asm volatile(
@@ -262,6 +265,7 @@ struct Group
     uint32_t bar;     // the group's mbarrier
     uint32_t aaddr;   // the group's operand buffer (shared address)
     uint32_t phase;   // parity of the mbarrier phase the next wait is for
+    unsigned polls;   // polls per MMA wait
 };
 
 // Operands written -> visible to the tensor core, then the group's first
@@ -282,7 +286,7 @@ __device__ __forceinline__ bool run_mma(Group& G, uint32_t bbase, int K, int bK,
                       idesc, (acc || ks > 0) ? 1 : 0);
         mma_commit(G.bar);
     }
-    const bool ok = group_all(bar_wait(G.bar, G.phase), G.g);
+    const bool ok = group_all(bar_wait(G.bar, G.phase, G.polls), G.g);
     G.phase ^= 1u;
     tc_after_sync();
     return ok;
@@ -314,6 +318,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_nrc_infer_tc(NrcInferParams p
     G.gt = tid % kGroupThreads;
     G.bar = sm_addr(smem + kOffBar + 8 * G.g);
     G.phase = 0;
+    G.polls = p.waitPolls;
     uint32_t* tmemSlot = reinterpret_cast<uint32_t*>(smem + kOffBar + 8 * kGroups);
     stage_weights(smem, p.weights);
     const int n = int(*p.count);
@@ -410,7 +415,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_nrc_infer_tc(NrcInferParams p
             atomicOr(errorFlag, kNrcTcTimeout);
         // let this group's MMAs still in flight finish before the TMEM is
         // released (run_mma flipped the parity past the phase that ran out)
-        bar_wait(G.bar, G.phase ^ 1u);
+        bar_wait(G.bar, G.phase ^ 1u, kWaitLimit);
     }
     tc_before_sync();
     __syncthreads();
@@ -426,14 +431,11 @@ size_t nrc_infer_tc_smem() { return size_t(kTcSmem); }
 cudaError_t launch_nrc_infer_tc(const NrcInferParams& p, int maxRecords, int* errorFlag, cudaStream_t stream,
                                 int numSMs)
 {
-    static bool configured = false;
-    if (!configured)
-    {
-        cudaError_t e = cudaFuncSetAttribute(k_nrc_infer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
-        if (e != cudaSuccess)
-            return e;
-        configured = true;
-    }
+    static DeviceOnce once;
+    cudaError_t e = once_per_device(
+        once, [] { return cudaFuncSetAttribute(k_nrc_infer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem); });
+    if (e != cudaSuccess)
+        return e;
     // one CTA per SM: it allocates all of the SM's TMEM columns
     const int tiles = (maxRecords + kRows - 1) / kRows;
     const int grid = std::max(1, std::min((tiles + kGroups - 1) / kGroups, numSMs));

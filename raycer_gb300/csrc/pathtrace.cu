@@ -28,6 +28,7 @@
 #include <cfloat>
 
 #include "filters.cuh"
+#include "monitor.cuh"
 #include "pathtrace.h"
 #include "sampling.cuh"
 #include "traverse.cuh"
@@ -62,6 +63,14 @@ __device__ __forceinline__ unsigned warp_fetch(unsigned* head, unsigned amount)
     if (lane_id() == 0)
         base = atomicAdd(head, amount);
     return __shfl_sync(0xffffffffu, base, 0);
+}
+
+// A monitored render whose earlier kernel stopped it (cancel or time
+// budget): the pass's remaining kernels do nothing, so the film keeps whole
+// passes only.
+__device__ __forceinline__ bool pass_stopped(const PassParams& p)
+{
+    return monitored(p.monitor, p.budgetNs) && render_stopped(p.ctl);
 }
 
 // Largest chunk whose first slot (pixel) is <= s.
@@ -114,16 +123,18 @@ __device__ __forceinline__ SlotInfo slot_info(const PathChunk& ch, const PathSce
 __global__ void __launch_bounds__(256) k_generate(PassParams p)
 {
     uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool stopped = pass_stopped(p);
     if (s == 0)
     {
-        p.counts[0] = uint32_t(p.nslots);
+        // a stopped render's pass: an empty queue, no lookups or samples
+        p.counts[0] = stopped ? 0u : uint32_t(p.nslots);
         if (p.nrc.counters)
         {
             p.nrc.counters[0] = 0;
             p.nrc.counters[1] = 0;
         }
     }
-    if (s >= uint32_t(p.nslots))
+    if (stopped || s >= uint32_t(p.nslots))
         return;
     // Training-path records start inactive; the path's end marks them.
     if (p.nrc.term && s % uint32_t(p.nrc.trainStride) == 0)
@@ -215,10 +226,14 @@ __global__ void __launch_bounds__(BLOCK, ((ORDER == ORDER_WIDE ? RC_EXTEND_WIDE_
     TravCount cnt{ 0, 0 };
     int err = 0;
     unsigned long long done = 0;
+    if (pass_stopped(p))
+        return;
     while (true)
     {
         unsigned base = warp_fetch(&p.counts[segment * 4 + 1], 32u);
         if (base >= total)
+            break;
+        if (warp_poll(p.monitor, p.budgetNs, p.ctl, &p.counts[segment * 4 + 1], base, true))
             break;
         unsigned q = base + lane_id();
         if (q < total)
@@ -248,10 +263,14 @@ __global__ void __launch_bounds__(128, RC_EXTEND_INST_MIN_BLOCKS) k_extend_insta
     TravCount cnt{ 0, 0 };
     int err = 0;
     unsigned long long done = 0;
+    if (pass_stopped(p))
+        return;
     while (true)
     {
         unsigned base = warp_fetch(&p.counts[segment * 4 + 1], 32u);
         if (base >= total)
+            break;
+        if (warp_poll(p.monitor, p.budgetNs, p.ctl, &p.counts[segment * 4 + 1], base, true))
             break;
         unsigned q = base + lane_id();
         if (q < total)
@@ -377,6 +396,8 @@ __global__ void __launch_bounds__(BLOCK) k_shade(PassParams p, int segment)
     const int* __restrict__ qin = (segment & 1) ? p.qb : p.qa;
     int* __restrict__ qout = (segment & 1) ? p.qa : p.qb;
     unsigned* outCount = &p.counts[(segment + 1) * 4 + 0];
+    if (pass_stopped(p))
+        return;
     while (true)
     {
         unsigned base = warp_fetch(&p.counts[segment * 4 + 2], 32u);
@@ -568,8 +589,10 @@ __global__ void __launch_bounds__(BLOCK) k_shade(PassParams p, int segment)
 __global__ void __launch_bounds__(256) k_accumulate(PassParams p)
 {
     int pix = blockIdx.x * blockDim.x + threadIdx.x;
-    if (pix >= p.npixels)
+    if (pix >= p.npixels || pass_stopped(p))
         return;
+    if (p.monitor && threadIdx.x == 0)
+        atomicAdd(&p.ctl->progress, static_cast<unsigned long long>(min(256, p.npixels - pix)));
     const PathChunk ch = p.chunks[chunk_of_pixel(p, uint32_t(pix))];
     const PathScene& sc = p.scenes[ch.scene];
     const uint32_t inChunk = uint32_t(pix) - ch.pixelPassBegin;
@@ -599,23 +622,20 @@ __global__ void __launch_bounds__(256) k_accumulate(PassParams p)
     *fp = f;
 }
 
+// Persistent grid: resident blocks per SM (cached per device) x the
+// launching handle's SMs.
 template <typename K>
-int persistent_blocks(K kernel, int block, int numSMs)
+int persistent_blocks(K kernel, int block, int numSMs, OccupancyCache& cache)
 {
-    int perSM = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kernel, block, 0) != cudaSuccess || perSM < 1)
-        perSM = 1;
-    return perSM * numSMs;
+    return blocks_per_sm(kernel, block, 0, cache) * numSMs;
 }
 
 template <int ORDER, bool COUNT, int BLOCK>
 cudaError_t extend_b(const PassParams& p, int segment, cudaStream_t stream, int numSMs)
 {
     auto k = k_extend<ORDER, COUNT, BLOCK>;
-    static int grid = 0;
-    if (grid == 0)
-        grid = persistent_blocks(k, BLOCK, numSMs);
-    k<<<grid, BLOCK, 0, stream>>>(p, segment);
+    static OccupancyCache occ;
+    k<<<persistent_blocks(k, BLOCK, numSMs, occ), BLOCK, 0, stream>>>(p, segment);
     return cudaGetLastError();
 }
 
@@ -633,10 +653,8 @@ template <bool COUNT>
 cudaError_t extend_inst(const PassParams& p, int segment, cudaStream_t stream, int numSMs)
 {
     auto k = k_extend_instanced<COUNT>;
-    static int grid = 0;
-    if (grid == 0)
-        grid = persistent_blocks(k, 128, numSMs);
-    k<<<grid, 128, 0, stream>>>(p, segment);
+    static OccupancyCache occ;
+    k<<<persistent_blocks(k, 128, numSMs, occ), 128, 0, stream>>>(p, segment);
     return cudaGetLastError();
 }
 
@@ -644,10 +662,8 @@ template <int BLOCK, bool NRC>
 cudaError_t shade_b(const PassParams& p, int segment, cudaStream_t stream, int numSMs)
 {
     auto k = k_shade<BLOCK, NRC>;
-    static int grid = 0;
-    if (grid == 0)
-        grid = persistent_blocks(k, BLOCK, numSMs);
-    k<<<grid, BLOCK, 0, stream>>>(p, segment);
+    static OccupancyCache occ;
+    k<<<persistent_blocks(k, BLOCK, numSMs, occ), BLOCK, 0, stream>>>(p, segment);
     return cudaGetLastError();
 }
 
@@ -671,7 +687,7 @@ cudaError_t shade_t(const PassParams& p, int segment, int block, cudaStream_t st
 __global__ void __launch_bounds__(256) k_nrc_targets(PassParams p)
 {
     const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= uint32_t(p.nrc.groups))
+    if (g >= uint32_t(p.nrc.groups) || pass_stopped(p))
         return;
     const float4 t = p.nrc.term[g];
     const uint32_t flags = __float_as_uint(t.w);

@@ -101,6 +101,8 @@ struct PassParams
     NrcPass nrc;
     int instanced;   // 1: the pass has two-level scenes (k_extend_instanced)
     int wide;        // 1: every scene of the pass has its 4-wide BVH (uncounted nearest-first extend uses it)
+    RenderMonitor* monitor = nullptr;         // monitored render (rc_render): cancel word and progress, else null
+    unsigned long long budgetNs = kNoBudget;  // the render's time budget (kNoBudget: none)
 };
 
 // Bytes of path state per slot (o, d, thr, res, hit, two queue entries, chunk id).

@@ -207,8 +207,9 @@ PassParams pass_params(void* state, uint64_t slots, unsigned* counts, DevControl
     return p;
 }
 
-rc_status render_path(rc_tracer* h, uint64_t pixelStart, uint64_t count, const volatile int32_t* cancel)
+rc_status render_path(rc_tracer* h, uint64_t pixelStart, uint64_t count, RenderWatch* watch)
 {
+    const volatile int32_t* cancel = watch ? watch->cancel : nullptr;
     const rc_general& g = h->general;
     {
         rc_status ws = ensure_wide(h);
@@ -277,6 +278,11 @@ rc_status render_path(rc_tracer* h, uint64_t pixelStart, uint64_t count, const v
     pp.segments = g.max_path_length;
     pp.instanced = h->nInstances > 0 ? 1 : 0;
     pp.wide = h->dWide != nullptr && h->nInstances == 0 ? 1 : 0;
+    if (watch)
+    {
+        pp.monitor = watch->dev;
+        pp.budgetNs = watch->budgetNs;
+    }
     PassShape shape;
     const bool nrc = nrc_active(h);
     if (nrc)
@@ -292,8 +298,16 @@ rc_status render_path(rc_tracer* h, uint64_t pixelStart, uint64_t count, const v
     {
         if (pass > 0 && cancel && *cancel)
         {
+            // raised while the passes were being queued: the device stops the
+            // passes already queued at their next work-queue check
+            if (watch && watch->dev)
+                h->monHost->cancel = 1;
             cudaStreamSynchronize(h->stream);
             h->frameIndex++;
+            DevControl ctl;
+            if (cudaMemcpy(&ctl, h->dCtl, sizeof(ctl), cudaMemcpyDeviceToHost) == cudaSuccess && watch &&
+                watch->pixels)
+                __atomic_store_n(watch->pixels, uint64_t(ctl.progress), __ATOMIC_RELAXED);
             return fail(h, RC_CANCELLED, "render: cancelled");
         }
         pp.chunks = dChunks + pass;
@@ -323,6 +337,11 @@ rc_status render_path(rc_tracer* h, uint64_t pixelStart, uint64_t count, const v
     DevControl ctl;
     RC_CUDA_TRY(h, cudaMemcpyAsync(&ctl, h->dCtl, sizeof(ctl), cudaMemcpyDeviceToHost, h->stream),
                 "read control block");
+    {
+        rc_status ws = wait_render(h, watch, h->ev1);
+        if (ws != RC_OK)
+            return ws;
+    }
     RC_CUDA_TRY(h, cudaStreamSynchronize(h->stream), "path tracing");
     float ms = 0.0f;
     cudaEventElapsedTime(&ms, h->ev0, h->ev1);
@@ -353,11 +372,11 @@ rc_status render_path(rc_tracer* h, uint64_t pixelStart, uint64_t count, const v
     h->stats.stage_tris[0] = ctl.stats[2];
     h->stats.stage_rays[1] = h->stats.stage_nodes[1] = h->stats.stage_tris[1] = 0;
     h->frameIndex++;
-    if (ctl.error & 1)
-        return fail(h, RC_DEVICE_ERROR, "path tracing: traversal stack overflow");
-    if (ctl.error & kNrcTcTimeout)
+    if (watch && watch->pixels)
+        __atomic_store_n(watch->pixels, uint64_t(ctl.progress), __ATOMIC_RELAXED);
+    if ((ctl.error & kNrcTcTimeout) && !(ctl.error & kErrStack))
         return fail(h, RC_DEVICE_ERROR, "path tracing: a radiance-cache tensor-core wait timed out");
-    return RC_OK;
+    return render_outcome(h, ctl.error, "path tracing");
 }
 
 }  // namespace rcx

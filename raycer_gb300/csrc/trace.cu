@@ -15,6 +15,8 @@
 #include "kernels.h"
 #include <cstdlib>
 
+#include "monitor.cuh"
+
 #include "traverse.cuh"
 
 namespace rcx
@@ -189,6 +191,8 @@ __global__ void __launch_bounds__(kBlock, FUSED ? RC_FUSED_MIN_BLOCKS : RC_TRACE
         unsigned base = warp_fetch(&ctl->head[0], 32u);
         if (int64_t(base) >= items)
             break;
+        if (warp_poll(sc.monitor, sc.budgetNs, ctl, &ctl->head[0], base, true))
+            break;
         int64_t i = int64_t(base) + lane_id();
         bool valid = i < items;
         if (tilesX > 0 && valid)
@@ -279,6 +283,8 @@ __global__ void __launch_bounds__(kBlock, FUSED ? RC_FUSED_MIN_BLOCKS : RC_TRACE
             hitSlot = h.slot;
             done++;
         }
+        // a pixel is finished here unless its shadow ray is queued
+        warp_progress(sc.monitor, ctl, valid && !hitAny);
         // Warp-aggregated compaction of the hit pixels into the shadow queue.
         unsigned mask = FUSED ? 0u : __ballot_sync(0xffffffffu, hitAny);
         if (mask)
@@ -321,7 +327,10 @@ __global__ void __launch_bounds__(kBlock, RC_TRACE_MIN_BLOCKS) k_raycast_shadow(
         unsigned base = warp_fetch(&ctl->head[2], 32u);
         if (base >= total)
             break;
+        // the queued pixels of a stopped frame are still finished: progress only
+        warp_poll(sc.monitor, sc.budgetNs, ctl, &ctl->head[2], base, false);
         unsigned q = base + lane_id();
+        warp_progress(sc.monitor, ctl, q < total);
         if (q < total)
         {
             int2 e = reinterpret_cast<const int2*>(queue)[q];
@@ -362,13 +371,12 @@ __global__ void __launch_bounds__(kBlock, RC_TRACE_MIN_BLOCKS) k_raycast_shadow(
     flush_counts(ctl, 1, done, cnt, err);
 }
 
+// Persistent grid of a ray kernel: resident blocks per SM (cached per
+// device) x the launching handle's SMs.
 template <typename K>
-int persistent_blocks(K kernel, int numSMs)
+int persistent_blocks(K kernel, int numSMs, OccupancyCache& cache)
 {
-    int perSM = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kernel, kBlock, 0) != cudaSuccess || perSM < 1)
-        perSM = 1;
-    return perSM * numSMs;
+    return blocks_per_sm(kernel, kBlock, 0, cache) * numSMs;
 }
 
 template <bool ANY, int ORDER, bool COUNT, bool SL = false>
@@ -376,10 +384,8 @@ cudaError_t cast_t(const LaunchInfo& li, const DevScene& sc, const rc_ray* rays,
                    DevControl* ctl)
 {
     auto k = k_cast<ANY, ORDER, COUNT, SL>;
-    static int grid = 0;
-    if (grid == 0)
-        grid = persistent_blocks(k, li.numSMs);
-    k<<<grid, kBlock, 0, li.stream>>>(sc, rays, int(n), hits, ctl);
+    static OccupancyCache occ;
+    k<<<persistent_blocks(k, li.numSMs, occ), kBlock, 0, li.stream>>>(sc, rays, int(n), hits, ctl);
     return cudaGetLastError();
 }
 
@@ -422,22 +428,16 @@ cudaError_t raycast_t(const LaunchInfo& li, const DevScene& sc, const DevCamera&
     if (FUSED && castShadow)
     {
         auto kf = k_raycast_primary<ORDER, false, PACKET, INST, true, SL>;
-        static int gf = 0;
-        if (gf == 0)
-            gf = persistent_blocks(kf, li.numSMs);
-        kf<<<gf, kBlock, 0, li.stream>>>(sc, cam, rays, pixelStart, count, width, height, tilesX, castShadow, out,
+        static OccupancyCache occF;
+        kf<<<persistent_blocks(kf, li.numSMs, occF), kBlock, 0, li.stream>>>(sc, cam, rays, pixelStart, count, width, height, tilesX, castShadow, out,
                                          queue, ctl, L, off, nullptr);
         kernels = 1;
         return cudaGetLastError();
     }
     auto kp = k_raycast_primary<ORDER, COUNT, PACKET, INST>;
     auto ks = k_raycast_shadow<COUNT, INST, SL>;
-    static int gp = 0, gs = 0;
-    if (gp == 0)
-        gp = persistent_blocks(kp, li.numSMs);
-    if (gs == 0)
-        gs = persistent_blocks(ks, li.numSMs);
-    kp<<<gp, kBlock, 0, li.stream>>>(sc, cam, rays, pixelStart, count, width, height, tilesX, castShadow, out, queue,
+    static OccupancyCache occP, occS;
+    kp<<<persistent_blocks(kp, li.numSMs, occP), kBlock, 0, li.stream>>>(sc, cam, rays, pixelStart, count, width, height, tilesX, castShadow, out, queue,
                                      ctl, L, off, castShadow ? origins : nullptr);
     kernels = 1;
     cudaError_t e = cudaGetLastError();
@@ -447,7 +447,7 @@ cudaError_t raycast_t(const LaunchInfo& li, const DevScene& sc, const DevCamera&
         e = cudaEventRecord(between, li.stream);
     if (e != cudaSuccess)
         return e;
-    ks<<<gs, kBlock, 0, li.stream>>>(sc, cam, rays, pixelStart, width, L, off, out, queue, ctl, origins);
+    ks<<<persistent_blocks(ks, li.numSMs, occS), kBlock, 0, li.stream>>>(sc, cam, rays, pixelStart, width, L, off, out, queue, ctl, origins);
     kernels = 2;
     return cudaGetLastError();
 }

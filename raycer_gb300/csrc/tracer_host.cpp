@@ -14,6 +14,7 @@
 #include <limits>
 #include <new>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/raycer_gb300.h"
@@ -480,12 +481,17 @@ rc_status begin_launch(rc_tracer* h)
     return RC_OK;
 }
 
-rc_status end_launch(rc_tracer* h, const char* what, bool twoStage)
+rc_status end_launch(rc_tracer* h, const char* what, bool twoStage, RenderWatch* watch = nullptr)
 {
     RC_CUDA_TRY(h, cudaEventRecord(h->ev1, h->stream), "record end event");
     DevControl ctl;
     RC_CUDA_TRY(h, cudaMemcpyAsync(&ctl, h->dCtl, sizeof(ctl), cudaMemcpyDeviceToHost, h->stream),
                 "read control block");
+    {
+        rc_status ws = wait_render(h, watch, h->ev1);
+        if (ws != RC_OK)
+            return ws;
+    }
     RC_CUDA_TRY(h, cudaStreamSynchronize(h->stream), what);
     float ms = 0.0f, ms0 = 0.0f;
     cudaEventElapsedTime(&ms, h->ev0, h->ev1);
@@ -510,9 +516,9 @@ rc_status end_launch(rc_tracer* h, const char* what, bool twoStage)
     h->stats.rays_traced = ctl.stats[0] + ctl.stats[3];
     h->stats.node_visits = ctl.stats[1] + ctl.stats[4];
     h->stats.tri_tests = ctl.stats[2] + ctl.stats[5];
-    if (ctl.error & 1)
-        return fail(h, RC_DEVICE_ERROR, std::string(what) + ": traversal stack overflow");
-    return RC_OK;
+    if (watch && watch->pixels)
+        __atomic_store_n(watch->pixels, uint64_t(ctl.progress), __ATOMIC_RELAXED);
+    return render_outcome(h, ctl.error, what);
 }
 
 }  // namespace
@@ -545,6 +551,14 @@ rc_status rc_create(rc_tracer** out, int device)
         e = cudaEventCreate(&h->evMid);
     if (e == cudaSuccess)
         e = cudaMalloc(reinterpret_cast<void**>(&h->dCtl), sizeof(DevControl));
+    if (e == cudaSuccess)
+        e = cudaHostAlloc(reinterpret_cast<void**>(&h->monHost), sizeof(RenderMonitor), cudaHostAllocMapped);
+    if (e == cudaSuccess)
+    {
+        h->monHost->cancel = 0;
+        h->monHost->pixels = 0;
+        e = cudaHostGetDevicePointer(reinterpret_cast<void**>(&h->monDev), h->monHost, 0);
+    }
     if (e != cudaSuccess)
     {
         cudaGetLastError();
@@ -578,6 +592,8 @@ void rc_destroy(rc_tracer* h)
         cudaFree(h->dTmpB);
     if (h->dCtl)
         cudaFree(h->dCtl);
+    if (h->monHost)
+        cudaFreeHost(h->monHost);
     if (h->ev0)
         cudaEventDestroy(h->ev0);
     if (h->ev1)
@@ -964,17 +980,46 @@ rc_status rc_render(rc_tracer* h, uint64_t pixel_start, uint64_t pixel_count, co
     if (pixel_start + pixel_count < pixel_start)
         return fail(h, RC_INVALID_ARG, "render: pixel range overflows");
     cudaSetDevice(h->device);
+    if (pixels_processed)
+        __atomic_store_n(pixels_processed, uint64_t(0), __ATOMIC_RELAXED);
     if (cancel && *cancel)
         return fail(h, RC_CANCELLED, "render: cancelled");
 
+    // The previous render on this handle has finished (every call blocks
+    // until its kernels are done), so nothing reads the monitor now.
+    RenderWatch watch;
+    watch.cancel = cancel;
+    watch.pixels = pixels_processed;
+    watch.budgetNs = h->budgetNs;
+    if (cancel || pixels_processed)
+    {
+        h->monHost->cancel = 0;
+        h->monHost->pixels = 0;
+        watch.dev = h->monDev;
+    }
     rc_status s;
     if (h->general.tracer_type == RC_TRACER_RAY)
-        s = render_raycast(h, pixel_start, pixel_count, nullptr);
+        s = render_raycast(h, pixel_start, pixel_count, nullptr, &watch);
     else
-        s = render_path(h, pixel_start, pixel_count, cancel);
+        s = render_path(h, pixel_start, pixel_count, &watch);
     if (s == RC_OK && pixels_processed)
-        *pixels_processed = pixel_count;
+        __atomic_store_n(pixels_processed, pixel_count, __ATOMIC_RELAXED);
     return s;
+}
+
+rc_status rc_set_time_budget(rc_tracer* h, double milliseconds)
+{
+    if (!h)
+        return RC_INVALID_ARG;
+    if (std::isnan(milliseconds))
+        return fail(h, RC_INVALID_ARG, "set_time_budget: NaN");
+    if (milliseconds < 0.0)
+        h->budgetNs = kNoBudget;
+    else if (milliseconds >= 1.0e12)
+        return fail(h, RC_INVALID_ARG, "set_time_budget: budget above 1e12 ms");
+    else
+        h->budgetNs = static_cast<unsigned long long>(milliseconds * 1.0e6);
+    return RC_OK;
 }
 
 rc_status rc_read_cast(rc_tracer* h, rc_cast_pixel* out)
@@ -1252,8 +1297,50 @@ rc_status rc_sync(rc_tracer* h)
 namespace rcx
 {
 
+rc_status wait_render(rc_tracer* h, RenderWatch* w, cudaEvent_t done)
+{
+    if (!w || (!w->cancel && !w->pixels))
+        return RC_OK;
+    bool raised = false;
+    while (true)
+    {
+        const cudaError_t q = cudaEventQuery(done);
+        if (!raised && w->cancel && *w->cancel)
+        {
+            h->monHost->cancel = 1;
+            raised = true;
+        }
+        if (w->pixels)
+        {
+            const uint64_t p = h->monHost->pixels;
+            if (p > w->seen)
+            {
+                w->seen = p;
+                __atomic_store_n(w->pixels, p, __ATOMIC_RELAXED);
+            }
+        }
+        if (q == cudaSuccess)
+            return RC_OK;
+        if (q != cudaErrorNotReady)
+            return cuda_fail(h, q, "render");
+        std::this_thread::yield();
+    }
+}
+
+rc_status render_outcome(rc_tracer* h, int error, const char* what)
+{
+    if (error & kErrStack)
+        return fail(h, RC_DEVICE_ERROR, std::string(what) + ": traversal stack overflow");
+    if (error & kErrCancelled)
+        return fail(h, RC_CANCELLED, std::string(what) + ": cancelled");
+    if (error & kErrBudget)
+        return fail(h, RC_TIMEOUT, std::string(what) + ": the time budget of " +
+                                       std::to_string(double(h->budgetNs) / 1.0e6) + " ms ran out");
+    return RC_OK;
+}
+
 rc_status raycast_into(rc_tracer* h, const rc_ray* dRays, uint64_t pixelStart, uint64_t count, int order,
-                       rc_cast_pixel* dOut, int* dQueue, float4* dOrigins)
+                       rc_cast_pixel* dOut, int* dQueue, float4* dOrigins, RenderWatch* watch)
 {
     float3 L = make_float3(0.0f, 0.0f, 0.0f);
     int castShadow = h->lights.empty() ? 0 : 1;
@@ -1271,17 +1358,22 @@ rc_status raycast_into(rc_tracer* h, const rc_ray* dRays, uint64_t pixelStart, u
     if (s != RC_OK)
         return s;
     int kernels = 0;
+    DevScene sc = dev_scene(h);
+    if (watch)
+    {
+        sc.monitor = watch->dev;
+        sc.budgetNs = watch->budgetNs;
+    }
     RC_CUDA_TRY(h,
-                launch_raycast(launch_info(h), dev_scene(h), cam, dRays, pixelStart, int64_t(count), width, order,
-                               castShadow, L, h->general.ray_start_offset, dOut, dQueue, h->dCtl, h->evMid,
-                               dOrigins, &kernels),
+                launch_raycast(launch_info(h), sc, cam, dRays, pixelStart, int64_t(count), width, order, castShadow,
+                               L, h->general.ray_start_offset, dOut, dQueue, h->dCtl, h->evMid, dOrigins, &kernels),
                 "launch ray-cast kernels");
-    return end_launch(h, "ray cast", kernels == 2);
+    return end_launch(h, "ray cast", kernels == 2, watch);
 }
 
-rc_status render_raycast(rc_tracer* h, uint64_t pixelStart, uint64_t count, const rc_ray* dRays)
+rc_status render_raycast(rc_tracer* h, uint64_t pixelStart, uint64_t count, const rc_ray* dRays, RenderWatch* watch)
 {
-    return raycast_into(h, dRays, pixelStart, count, h->order, h->dCast, h->dQueue);
+    return raycast_into(h, dRays, pixelStart, count, h->order, h->dCast, h->dQueue, nullptr, watch);
 }
 
 }  // namespace rcx

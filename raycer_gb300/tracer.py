@@ -20,7 +20,6 @@ from __future__ import annotations
 
 import ctypes as C
 import threading
-from dataclasses import dataclass, field
 from enum import IntEnum
 
 import numpy as np
@@ -115,16 +114,48 @@ def tonemapper_record(desc: SceneDesc) -> N.rc_tonemapper:
     return t
 
 
-@dataclass
 class TracerState:
-    """TracerState (TracerState.h:13-26)."""
-    scene: SceneDesc | None = None
-    film: "Film | None" = None
-    filmWidth: int = 0
-    filmHeight: int = 0
-    pixelStartOffset: int = 0
-    pixelCount: int = 0
-    pixelsProcessed: int = 0
+    """TracerState (TracerState.h:13-26). ``pixelsProcessed`` is a 64-bit
+    word that a running render advances, so another thread can watch it as
+    ConsoleRunner's main thread does (ConsoleRunner.cpp:126-142)."""
+
+    def __init__(self, scene: SceneDesc | None = None, film: "Film | None" = None, filmWidth: int = 0,
+                 filmHeight: int = 0, pixelStartOffset: int = 0, pixelCount: int = 0, pixelsProcessed: int = 0):
+        self.scene = scene
+        self.film = film
+        self.filmWidth = filmWidth
+        self.filmHeight = filmHeight
+        self.pixelStartOffset = pixelStartOffset
+        self.pixelCount = pixelCount
+        self._processed = C.c_uint64(int(pixelsProcessed))
+
+    @property
+    def pixelsProcessed(self) -> int:
+        return int(self._processed.value)
+
+    @pixelsProcessed.setter
+    def pixelsProcessed(self, value: int) -> None:
+        self._processed.value = int(value)
+
+
+class Interrupted:
+    """The ``interrupted`` flag of Tracer::run (std::atomic<bool>&,
+    Tracer.h:28): ``set()`` from any thread stops a running render at its
+    kernels' next work-queue check (the render then raises RaycerError with
+    status RC_CANCELLED). A ``threading.Event`` works too, through a watcher
+    thread that polls it every millisecond."""
+
+    def __init__(self) -> None:
+        self._word = C.c_int32(0)
+
+    def set(self) -> None:
+        self._word.value = 1
+
+    def clear(self) -> None:
+        self._word.value = 0
+
+    def is_set(self) -> bool:
+        return bool(self._word.value)
 
 
 class Film:
@@ -338,17 +369,45 @@ class CudaTracer:
         self._check(self._lib.rc_release_scene(self._h), "releaseBuffers")
         self._scene = None
 
-    def run(self, state: TracerState, interrupted: "threading.Event | None" = None) -> None:
-        """CLTracer::run (CLTracer.cpp:262-305): camera upload, then the render."""
+    def run(self, state: TracerState, interrupted: "Interrupted | threading.Event | None" = None) -> None:
+        """CLTracer::run (CLTracer.cpp:262-305): camera upload, then the
+        render. ``state.pixelsProcessed`` advances while it runs; setting
+        ``interrupted`` from another thread stops it (RC_CANCELLED)."""
         scene = state.scene or self._scene
         self.set_camera(camera_record(scene, state.filmWidth or self.imageWidth,
                                       state.filmHeight or self.imageHeight))
-        flag = C.c_int32(1 if (interrupted is not None and interrupted.is_set()) else 0)
-        done = C.c_uint64(0)
         count = state.pixelCount or self.imageWidth * self.imageHeight
-        self._check(self._lib.rc_render(self._h, int(state.pixelStartOffset), int(count), C.byref(flag),
-                                        C.byref(done)), "run")
-        state.pixelsProcessed = int(done.value)
+        watcher = None
+        if interrupted is None:
+            flag = None
+        elif isinstance(interrupted, Interrupted):
+            flag = C.byref(interrupted._word)
+        else:
+            word = C.c_int32(1 if interrupted.is_set() else 0)
+            flag = C.byref(word)
+            finished = threading.Event()
+
+            def watch():
+                while not finished.is_set():
+                    if interrupted.wait(0.001):
+                        word.value = 1
+                        return
+
+            watcher = threading.Thread(target=watch, daemon=True)
+            watcher.start()
+        try:
+            st = self._lib.rc_render(self._h, int(state.pixelStartOffset), int(count), flag,
+                                     C.byref(state._processed))
+        finally:
+            if watcher is not None:
+                finished.set()
+                watcher.join()
+        self._check(st, "run")
+
+    def set_time_budget(self, milliseconds: float | None) -> None:
+        """Time budget of later renders (rc_set_time_budget); None removes it."""
+        self._check(self._lib.rc_set_time_budget(self._h, -1.0 if milliseconds is None else float(milliseconds)),
+                    "set_time_budget")
 
     def downloadImage(self) -> np.ndarray:
         """Tone-mapped image (CLTracer::downloadImage, CLTracer.cpp:307): (height, width, 4) float32."""

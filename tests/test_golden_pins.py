@@ -91,6 +91,17 @@ def test_camera_from_euler_matches_reference():
         assert np.array_equal(mine, state[:18].astype(np.float32))
 
 
+def test_oracle_camera_state64_matches_reference():
+    """The oracle's float64 camera (what the CPU baseline renders through,
+    without the product library) agrees with the reference's Camera state to
+    a few units in the last place (libm and operation order)."""
+    g = _load("camera_poses.npz")
+    for pose, state in zip(g["poses"], g["states"]):
+        mine = oracle.camera_state64(pose[0:3], pose[3], pose[4], pose[5], pose[6], int(pose[7]), int(pose[8]))
+        assert mine.shape == state.shape
+        assert np.all(np.abs(mine - state) <= 4 * np.spacing(np.maximum(np.abs(state), 1.0))), pose
+
+
 def test_value_noise_matches_reference():
     g = _load("math.npz")
     p = g["noise_points"]

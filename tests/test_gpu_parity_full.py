@@ -59,6 +59,43 @@ def test_heightfield_frame_bit_exact_and_counters(heightfield, order):
     assert stats["tri_tests"] == cnt[2]
 
 
+@pytest.mark.parametrize("light", ["config", "low"])
+@pytest.mark.parametrize("order", [N.RC_ORDER_NEAREST, N.RC_ORDER_REFERENCE])
+def test_heightfield_timed_frame_bit_exact(heightfield, order, light):
+    """The frame the benchmark times: uncounted, so one kernel traces each
+    8x4 tile's primary rays warp-wide and then every hit pixel's shadow ray
+    (k_raycast_primary, packet + fused form). Every pixel's 16-byte record of
+    the 1920x1080 frame equals the float32 oracle's, in both traversal
+    orders, under the scene's light and under a low light whose shadow rays
+    meet the hills (reference: intersectBVH intersections.cl:98-148,
+    FlatBVH::intersect FlatBVH.cpp:22-75)."""
+    import dataclasses
+
+    sc, t, orc = heightfield
+    lit = sc if light == "config" else dataclasses.replace(sc, light_direction=(-1.0, -0.25, -0.2))
+    t._set_lights(lit)
+    try:
+        t.set_traversal_order(order)
+        t.set_counting(False)
+        st = TracerState(scene=sc, filmWidth=sc.width, filmHeight=sc.height, pixelCount=sc.width * sc.height)
+        t.run(st)
+        stats = t.stats()
+        gpu = t.read_cast().view(np.int32).reshape(-1, 4)
+    finally:
+        t._set_lights(sc)
+    # one kernel: the shadow stage has no launch of its own
+    assert stats["stage_ms"][1] == 0.0 and stats["stage_ms"][0] > 0.0
+    cam = camera_floats(camera_record(sc))
+    L = -np.array(lit.light_direction, np.float32)
+    ref, cnt = orc.raycast32(cam, sc.width, sc.width * sc.height, L, order=order)
+    diff = (gpu != ref).any(axis=1)
+    assert not diff.any(), f"{diff.sum()} pixels differ"
+    assert stats["rays_traced"] == cnt[0]
+    occluded = int((ref[:, 2] >= 0).sum())
+    if light == "low":
+        assert occluded > 100_000, occluded
+
+
 def test_heightfield_vs_reference_fp64(heightfield):
     sc, t, orc = heightfield
     g = _load("heightfield.npz")
