@@ -24,6 +24,16 @@ BVH queries (primary + shadow) per second.
             float32 oracle's count, + 16 B record per pixel; + 8 B queue
             entry per hit pixel in the two-kernel form)
 
+At N = 1 the line also carries the rest of the headline (unless
+--headline-only):
+  path_1m   plain path tracing of the same heightfield (+ an emissive panel
+            overhead) at 1080p, 1 path per pixel, depth 4: device and e2e
+            Mrays/s and the float64 port of the reference's path tracer on
+            this host's cores (Tracer.cpp:58, PathTracer.cpp:25)
+  nrc       time to display RMSE 0.01 of the radiance-cache tracer and of
+            the plain tracer against a float64 4096-spp ground truth on the
+            heightfield + 200 blobs scene at 1080p
+
 `--impl reference` times the reference's CPU ray casting on this host's cores
 (the reference's own code where it was compiled, else the float64 port) on
 the same workload, one full frame per step.
@@ -70,6 +80,8 @@ def parse_args():
     ap.add_argument("--scale", type=float, default=1.0, help="nrc: film scale (1 = 1920x1080)")
     ap.add_argument("--terminate-segment", type=int, default=2,
                     help="nrc: paths end into the cache at the hit of this segment")
+    ap.add_argument("--headline-only", action="store_true",
+                    help="raycast: the RAY frame only, without the path-tracing and radiance-cache records")
     args = ap.parse_args()
     if args.steps is None:
         args.steps = 5 if args.workload == "batch" else 200
@@ -491,6 +503,11 @@ def run_ours(args, rank, local_rank, world):
         torch.distributed.destroy_process_group()
     tracer.close()
     if rank == 0:
+        if world == 1 and not args.headline_only:
+            # the rest of the headline: plain path tracing on the 1M-triangle
+            # scene, and the radiance cache's time to RMSE 0.01
+            line["path_1m"] = path_1m_record(max(3, min(args.steps, 20)), max(3, min(args.warmup, 5)), local_rank)
+            line["nrc"] = nrc_record(args.gt_spp, local_rank)
         if world == 1:
             try:
                 res = cpu_raycast(sc, 2, 1, None)
@@ -503,6 +520,114 @@ def run_ours(args, rank, local_rank, world):
                                         "sample": f"unavailable: {e}"}
         print(json.dumps(line))
     return 0
+
+
+def path_1m_record(steps, warmup, device):
+    """Plain path tracing of the 1,045,506-triangle heightfield at 1920x1080
+    (Tracer::run Tracer.cpp:58 -> PathTracer::traceRecursive PathTracer.cpp:25:
+    one camera ray per pixel, 4 segments, the 2 rho |cos| estimator; an
+    emissive panel overhead is the light, see scenes.heightfield_path_scene).
+    One step = one frame (rc_render of every pixel). Device Mrays/s from the
+    renders' CUDA events with the L2 flushed before every frame; e2e through
+    the public API: the render and the tone-mapped image read back to the
+    host (rc_render + rc_resolve), wall clock. CPU: the float64 port of the
+    reference's path tracer (its own BVH build, outside the timing) on all
+    host cores, full frames."""
+    import torch
+
+    import oracle
+    from raycer_gb300 import _native as N
+    from raycer_gb300 import scenes
+    from raycer_gb300.tracer import CudaTracer, TracerState
+
+    sc = scenes.heightfield_path_scene()
+    n = sc.width * sc.height
+    dev = torch.device("cuda", device)
+    out = {"workload": "path tracing 1920x1080, 1 camera ray per pixel, depth 4, heightfield 1,045,506 tris "
+                       "+ 2-triangle emissive panel", "triangles": sc.triangle_count}
+    with CudaTracer(device) as t:
+        t.initializeBuffers(sc, seed=1)
+        t.initializeImageBuffers(sc.width, sc.height)
+        st = TracerState(scene=sc, filmWidth=sc.width, filmHeight=sc.height, pixelCount=n)
+        stream = torch.cuda.ExternalStream(N.lib().rc_stream(t.handle), device=dev)
+        flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device=dev)
+        for _ in range(warmup):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            t.run(st)
+        ms, rays, ext = [], [], []
+        for _ in range(steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            t.run(st)
+            s = t.stats()
+            ms.append(s["last_ms"])
+            rays.append(s["rays_traced"])
+            ext.append(s["stage_ms"][0])
+        img = t.downloadImage()
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            t.run(st)
+            img = t.downloadImage()
+        e2e_s = time.perf_counter() - t0
+        e2e_rays = t.stats()["rays_traced"] * steps
+    dev_mrays = sum(rays) / (sum(ms) / 1e3) / 1e6
+    out.update({"steps": steps, "warmup": warmup, "mrays_per_s": round(dev_mrays, 1),
+                "ms_per_frame": round(statistics.mean(ms), 4), "rays_per_frame": int(statistics.mean(rays)),
+                "extend_share": round(sum(ext) / sum(ms), 3),
+                "e2e": {"value": round(e2e_rays / e2e_s / 1e6, 1), "unit": METRIC, "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": n * 16,
+                        "note": "rc_render + rc_resolve (tone-mapped RGBA float image to the host) per frame"},
+                "image_mean": round(float(img[..., :3].mean()), 4)})
+    try:
+        threads = cpu_threads()
+        t0 = time.perf_counter()
+        orc = oracle.Oracle(sc)
+        build_s = time.perf_counter() - t0
+        cam64 = oracle.camera64_of(sc)
+        orc.render_path64(cam64, sc.width, n, 4, 1, 1, seed=1, threads=threads)   # warm-up
+        c_rays = c_sec = 0
+        for k in range(2):
+            _, r, sec = orc.render_path64(cam64, sc.width, n, 4, 1, 1, seed=2 + k, threads=threads)
+            c_rays += r
+            c_sec += sec
+        cpu = c_rays / c_sec / 1e6
+        out["cpu_baseline"] = {"value": round(cpu, 3), "unit": METRIC, "cores": threads, "kind": "port",
+                               "sample": "full 1920x1080 frame, 1 warm-up + 2 timed frames",
+                               "bvh_build_s": round(build_s, 2)}
+        out["device_over_cpu"] = round(dev_mrays / cpu, 1)
+        out["e2e_over_cpu"] = round(out["e2e"]["value"] / cpu, 1)
+    except ImportError as e:
+        out["cpu_baseline"] = {"value": None, "sample": f"unavailable: {e}"}
+    return out
+
+
+def nrc_record(gt_spp, device, enclosed=False, max_seconds=60.0):
+    """Time to display RMSE 0.01 at 1080p: the radiance-cache tracer against
+    the plain path tracer, both against a float64 ground truth of `gt_spp`
+    plain frames (raycer_gb300.nrc_eval.time_to_rmse)."""
+    from raycer_gb300 import scenes
+    from raycer_gb300.nrc_eval import time_to_rmse
+
+    t0 = time.perf_counter()
+    sc = scenes.heightfield_blobs_scene(enclosed=enclosed)
+    build_s = time.perf_counter() - t0
+    res = time_to_rmse(sc, target=0.01, gt_spp=gt_spp, max_frames=4096, max_seconds=max_seconds, device=device)
+
+    def run_dict(r):
+        return {"frames": r.frames, "seconds": round(r.seconds, 3), "gpu_ms": round(r.gpu_ms, 1),
+                "rmse": round(r.rmse, 5), "reached": r.reached,
+                "mrays_per_s": round(r.rays / max(r.seconds, 1e-9) / 1e6, 1)}
+
+    return {"workload": f"radiance cache vs plain path tracing: heightfield + 200 blobs, {sc.triangle_count} tris, "
+                        f"{sc.width}x{sc.height}, 1 spp/frame, depth 12, "
+                        + ("closed box lit by an emissive panel" if enclosed else "sky-lit"),
+            "target_rmse": 0.01, "gt_spp": res.gt_spp, "gt_seconds": round(res.gt_seconds, 1),
+            "scene_build_s": round(build_s, 1), "plain": run_dict(res.plain), "cache": run_dict(res.cache),
+            "time_ratio_cache_over_plain": (round(res.cache.seconds / res.plain.seconds, 3)
+                                            if res.plain.reached and res.cache.reached else None),
+            "cache_stats": {k: (round(v, 4) if isinstance(v, float) else v) for k, v in res.cache_stats.items()}}
 
 
 def run_batch(args, rank, world):

@@ -323,9 +323,11 @@ rc_status rc_clear(rc_tracer* h);
  *     the calling thread stores into it (relaxed atomic stores of a
  *     uint64_t, so another thread may read it with an atomic load, e.g.
  *     through a std::atomic<uint64_t> of the same object) the pixels the
- *     device reports finished: RAY frames per 32-pixel work item, PATH
- *     renders per pass as each pass's film update lands. At the end it
- *     holds the pixels finished: pixel_count on success.
+ *     device reports finished, never decreasing: PATH renders per pass as
+ *     each pass's film update lands; RAY frames a lower bound (the pixels
+ *     of the 32-pixel work items taken before those still in flight). At
+ *     the end it holds the exact number of pixels finished: pixel_count on
+ *     success.
  * A cancel flag or progress counter makes the calling thread wait by
  * polling (it yields between polls) instead of sleeping in the driver. */
 rc_status rc_render(rc_tracer* h, uint64_t pixel_start, uint64_t pixel_count,

@@ -22,7 +22,7 @@ struct DevControl
                                    // bit2: cancelled; bit3: time budget ran out (kErr* below)
     int pad[3];
     unsigned long long t0;         // %globaltimer at the render's first work-queue check (time budget)
-    unsigned long long progress;   // pixels finished (monitored renders)
+    unsigned long long progress;   // PATH renders: pixels whose samples the film has taken (monitored renders)
 };
 
 constexpr int kErrStack = 1;

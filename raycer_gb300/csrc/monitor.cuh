@@ -9,7 +9,10 @@
 // every 64th item:
 //   * read the host-mapped cancel word and check the time budget (measured
 //     from the render's first check, %globaltimer);
-//   * copy the device progress counter into the host-mapped monitor.
+//   * publish the pixels finished so far in the host-mapped monitor (PATH
+//     renders: the pixels whose samples the film has taken; one-kernel RAY
+//     frames: a lower bound from the queue head; the call's exact count is
+//     read from the kernels' statistics at the end).
 // A warp that sees a stop records the reason in DevControl::error and pushes
 // the queue head past any item count, so every warp's next fetch ends its
 // loop: the items already taken finish, nothing else starts. Kernels that
@@ -43,11 +46,15 @@ __device__ __forceinline__ bool render_stopped(const DevControl* ctl)
     return (*reinterpret_cast<const volatile int*>(&ctl->error) & kErrStop) != 0;
 }
 
-// Lane 0 of the warp that took `item` (counted in 32-wide items) of the
-// queue whose head is `head`. mayStop = false only publishes progress.
-// Returns the stop reason (kErrCancelled / kErrBudget) or 0.
+// What a poll writes into the monitor's pixel count.
+constexpr unsigned long long kPublishNone = ~0ull;            // nothing (two-kernel RAY frames)
+constexpr unsigned long long kPublishProgress = ~0ull - 1ull;  // DevControl::progress (PATH renders)
+
+// Lane 0 of the warp that took a work item of the queue whose head is
+// `head`. mayStop = false only publishes. Returns the stop reason
+// (kErrCancelled / kErrBudget) or 0.
 static __device__ __noinline__ int poll_render(RenderMonitor* mon, unsigned long long budgetNs, DevControl* ctl,
-                                        unsigned* head, bool mayStop)
+                                               unsigned* head, bool mayStop, unsigned long long publish)
 {
     int why = 0;
     if (mayStop && budgetNs != kNoBudget)
@@ -63,9 +70,15 @@ static __device__ __noinline__ int poll_render(RenderMonitor* mon, unsigned long
     {
         if (mayStop && mon->cancel)
             why = kErrCancelled;
-        // a plain store: stores of two warps may land in either order, so the
-        // host keeps the largest value it has read
-        mon->pixels = *reinterpret_cast<const volatile unsigned long long*>(&ctl->progress);
+        if (publish != kPublishNone)
+        {
+            // a plain store: stores of two warps may land in either order, so
+            // the host keeps the largest value it has read
+            mon->pixels = publish == kPublishProgress
+                              ? *reinterpret_cast<const volatile unsigned long long*>(&ctl->progress)
+                              : publish;
+            __threadfence_system();
+        }
     }
     if (why)
     {
@@ -76,27 +89,32 @@ static __device__ __noinline__ int poll_render(RenderMonitor* mon, unsigned long
 }
 
 // Whole warp, after its fetch of `base` (a multiple of 32) from `head`:
-// true when the warp must stop taking work.
+// true when the warp must stop taking work. `publish` as poll_render's, or
+// for a one-kernel RAY frame kPublishEstimate: the pixels of the items
+// before the ones in flight (every warp of the grid holds at most one item,
+// so when item k is taken at least k - warps items are finished), at most
+// `pixels`.
+constexpr unsigned long long kPublishEstimate = ~0ull - 2ull;
+
 __device__ __forceinline__ bool warp_poll(RenderMonitor* mon, unsigned long long budgetNs, DevControl* ctl,
-                                          unsigned* head, unsigned base, bool mayStop)
+                                          unsigned* head, unsigned base, bool mayStop, unsigned long long publish,
+                                          unsigned long long pixels = 0)
 {
     if (!monitored(mon, budgetNs) || ((base >> 5) & ((1u << kPollItemsLog2) - 1u)) != 0u)
         return false;
     int why = 0;
     if ((threadIdx.x & 31u) == 0u)
-        why = poll_render(mon, budgetNs, ctl, head, mayStop);
+    {
+        if (publish == kPublishEstimate)
+        {
+            const unsigned long long warps = static_cast<unsigned long long>(gridDim.x) * (blockDim.x >> 5);
+            const unsigned long long item = base >> 5;
+            publish = item > warps ? (item - warps) * 32ull : 0ull;
+            publish = publish < pixels ? publish : pixels;
+        }
+        why = poll_render(mon, budgetNs, ctl, head, mayStop, publish);
+    }
     return __shfl_sync(0xffffffffu, why, 0) != 0;
-}
-
-// Whole warp: adds the pixels the warp finished in this item (lanes with
-// `finished`) to the render's progress counter.
-__device__ __forceinline__ void warp_progress(const RenderMonitor* mon, DevControl* ctl, bool finished)
-{
-    if (!mon)
-        return;
-    const unsigned m = __ballot_sync(0xffffffffu, finished);
-    if ((threadIdx.x & 31u) == 0u && m)
-        atomicAdd(&ctl->progress, static_cast<unsigned long long>(__popc(m)));
 }
 
 }  // namespace rcx

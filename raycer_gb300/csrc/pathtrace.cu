@@ -233,7 +233,7 @@ __global__ void __launch_bounds__(BLOCK, ((ORDER == ORDER_WIDE ? RC_EXTEND_WIDE_
         unsigned base = warp_fetch(&p.counts[segment * 4 + 1], 32u);
         if (base >= total)
             break;
-        if (warp_poll(p.monitor, p.budgetNs, p.ctl, &p.counts[segment * 4 + 1], base, true))
+        if (warp_poll(p.monitor, p.budgetNs, p.ctl, &p.counts[segment * 4 + 1], base, true, kPublishProgress))
             break;
         unsigned q = base + lane_id();
         if (q < total)
@@ -270,7 +270,7 @@ __global__ void __launch_bounds__(128, RC_EXTEND_INST_MIN_BLOCKS) k_extend_insta
         unsigned base = warp_fetch(&p.counts[segment * 4 + 1], 32u);
         if (base >= total)
             break;
-        if (warp_poll(p.monitor, p.budgetNs, p.ctl, &p.counts[segment * 4 + 1], base, true))
+        if (warp_poll(p.monitor, p.budgetNs, p.ctl, &p.counts[segment * 4 + 1], base, true, kPublishProgress))
             break;
         unsigned q = base + lane_id();
         if (q < total)

@@ -334,14 +334,16 @@ rc_status render_path(rc_tracer* h, uint64_t pixelStart, uint64_t count, RenderW
             return s;
     }
     RC_CUDA_TRY(h, cudaEventRecord(h->ev1, h->stream), "record end event");
-    DevControl ctl;
-    RC_CUDA_TRY(h, cudaMemcpyAsync(&ctl, h->dCtl, sizeof(ctl), cudaMemcpyDeviceToHost, h->stream),
-                "read control block");
     {
+        // before the read-back below: a copy into pageable memory returns
+        // only once the kernels are done
         rc_status ws = wait_render(h, watch, h->ev1);
         if (ws != RC_OK)
             return ws;
     }
+    DevControl ctl;
+    RC_CUDA_TRY(h, cudaMemcpyAsync(&ctl, h->dCtl, sizeof(ctl), cudaMemcpyDeviceToHost, h->stream),
+                "read control block");
     RC_CUDA_TRY(h, cudaStreamSynchronize(h->stream), "path tracing");
     float ms = 0.0f;
     cudaEventElapsedTime(&ms, h->ev0, h->ev1);

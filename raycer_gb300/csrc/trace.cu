@@ -191,7 +191,8 @@ __global__ void __launch_bounds__(kBlock, FUSED ? RC_FUSED_MIN_BLOCKS : RC_TRACE
         unsigned base = warp_fetch(&ctl->head[0], 32u);
         if (int64_t(base) >= items)
             break;
-        if (warp_poll(sc.monitor, sc.budgetNs, ctl, &ctl->head[0], base, true))
+        if (warp_poll(sc.monitor, sc.budgetNs, ctl, &ctl->head[0], base, true,
+                      FUSED ? kPublishEstimate : kPublishNone, static_cast<unsigned long long>(count)))
             break;
         int64_t i = int64_t(base) + lane_id();
         bool valid = i < items;
@@ -283,8 +284,6 @@ __global__ void __launch_bounds__(kBlock, FUSED ? RC_FUSED_MIN_BLOCKS : RC_TRACE
             hitSlot = h.slot;
             done++;
         }
-        // a pixel is finished here unless its shadow ray is queued
-        warp_progress(sc.monitor, ctl, valid && !hitAny);
         // Warp-aggregated compaction of the hit pixels into the shadow queue.
         unsigned mask = FUSED ? 0u : __ballot_sync(0xffffffffu, hitAny);
         if (mask)
@@ -327,10 +326,7 @@ __global__ void __launch_bounds__(kBlock, RC_TRACE_MIN_BLOCKS) k_raycast_shadow(
         unsigned base = warp_fetch(&ctl->head[2], 32u);
         if (base >= total)
             break;
-        // the queued pixels of a stopped frame are still finished: progress only
-        warp_poll(sc.monitor, sc.budgetNs, ctl, &ctl->head[2], base, false);
         unsigned q = base + lane_id();
-        warp_progress(sc.monitor, ctl, q < total);
         if (q < total)
         {
             int2 e = reinterpret_cast<const int2*>(queue)[q];

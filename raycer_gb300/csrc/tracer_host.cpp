@@ -484,14 +484,16 @@ rc_status begin_launch(rc_tracer* h)
 rc_status end_launch(rc_tracer* h, const char* what, bool twoStage, RenderWatch* watch = nullptr)
 {
     RC_CUDA_TRY(h, cudaEventRecord(h->ev1, h->stream), "record end event");
-    DevControl ctl;
-    RC_CUDA_TRY(h, cudaMemcpyAsync(&ctl, h->dCtl, sizeof(ctl), cudaMemcpyDeviceToHost, h->stream),
-                "read control block");
     {
+        // before the read-back below: a copy into pageable memory returns
+        // only once the kernels are done
         rc_status ws = wait_render(h, watch, h->ev1);
         if (ws != RC_OK)
             return ws;
     }
+    DevControl ctl;
+    RC_CUDA_TRY(h, cudaMemcpyAsync(&ctl, h->dCtl, sizeof(ctl), cudaMemcpyDeviceToHost, h->stream),
+                "read control block");
     RC_CUDA_TRY(h, cudaStreamSynchronize(h->stream), what);
     float ms = 0.0f, ms0 = 0.0f;
     cudaEventElapsedTime(&ms, h->ev0, h->ev1);
@@ -516,8 +518,10 @@ rc_status end_launch(rc_tracer* h, const char* what, bool twoStage, RenderWatch*
     h->stats.rays_traced = ctl.stats[0] + ctl.stats[3];
     h->stats.node_visits = ctl.stats[1] + ctl.stats[4];
     h->stats.tri_tests = ctl.stats[2] + ctl.stats[5];
+    // pixels finished: those whose primary ray was traced (a queued shadow
+    // ray is always traced by the end of the call)
     if (watch && watch->pixels)
-        __atomic_store_n(watch->pixels, uint64_t(ctl.progress), __ATOMIC_RELAXED);
+        __atomic_store_n(watch->pixels, uint64_t(ctl.stats[0]), __ATOMIC_RELAXED);
     return render_outcome(h, ctl.error, what);
 }
 

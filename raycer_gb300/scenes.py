@@ -284,6 +284,31 @@ def heightfield_scene(seed: int = 2, nx: int = 1024, nz: int = 512, width: int =
     )
 
 
+def heightfield_path_scene(width: int = 1920, height: int = 1080, max_path_length: int = 4,
+                           panel_height: float = 30.0, panel_half: float = 400.0, radiance: float = 1.0,
+                           **kw) -> SceneDesc:
+    """The 1,045,506-triangle heightfield path traced with the reference's
+    estimator. The heightfield has no emitter and PathTracer::traceRecursive
+    collects emission only (PathTracer.cpp:25-75; its directional light does
+    nothing there), so a large emissive quad of `radiance` faces down from
+    `panel_height` over the terrain (2 triangles): paths that leave the
+    terrain upwards end on it, as under an overcast sky. One camera ray per
+    pixel (multiSampleCountSqrt 1: the pixel centre, Tracer.cpp:119-123),
+    `max_path_length` segments, box filter."""
+    sc = heightfield_scene(width=width, height=height, **kw)
+    y, r = float(panel_height), float(panel_half)
+    # winding (v1 - v0) x (v2 - v0) = -y: the panel faces the terrain
+    panel = np.array([[-r, y, -r, r, y, -r, r, y, r],
+                      [-r, y, -r, r, y, r, -r, y, r]], np.float64)
+    sc.vertices = np.concatenate([sc.vertices, _f32(panel)])
+    sc.materials = list(sc.materials) + [Material(emittance=(radiance, radiance, radiance), is_emissive=True)]
+    sc.material_index = np.concatenate([sc.material_index, np.full(2, len(sc.materials) - 1, np.uint32)])
+    sc.name = sc.name + " + emissive sky panel"
+    sc.settings = dict(tracer="path", max_path_length=int(max_path_length), multi_sample_count_sqrt=1,
+                       path_sample_count=1, filter="box")
+    return sc
+
+
 # ---------------------------------------------------------------------------
 # Batch of rooms (batched path tracing).
 
