@@ -113,7 +113,7 @@ struct __align__(16) DevInstance
 // Progress and stop word of one render (rc_render): pinned host memory mapped
 // into the device's address space, so the persistent kernels read the
 // caller's cancel request and publish their progress while they run. Both
-// fields cross the host link, so the kernels touch them once per 64 work
+// fields cross the host link, so the kernels touch them once per 256 work
 // items only.
 struct RenderMonitor
 {

@@ -6,7 +6,7 @@
 // persistent kernels take their work in items of 32 rays or path slots from
 // an atomic queue head; a monitored render (rc_render with a cancel flag, a
 // progress counter or a time budget) makes lane 0 of the warp that took
-// every 64th item:
+// every 256th item:
 //   * read the host-mapped cancel word and check the time budget (measured
 //     from the render's first check, %globaltimer);
 //   * publish the pixels finished so far in the host-mapped monitor (PATH
@@ -25,7 +25,7 @@
 namespace rcx
 {
 
-constexpr unsigned kPollItemsLog2 = 6;             // check every 64th work item
+constexpr unsigned kPollItemsLog2 = 8;             // check every 256th work item
 constexpr unsigned kHeadPastEnd = 0x7fffffffu;     // above any queue or item count
 
 __device__ __forceinline__ unsigned long long global_ns()
