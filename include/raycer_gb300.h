@@ -592,7 +592,15 @@ typedef struct rc_nrc_config
                                 /* (4,194,304); < 0 = none, so every wait gives up   */
                                 /* at once (exercises that error path; the kernel    */
                                 /* still lets its MMAs finish before it frees TMEM)  */
+    int32_t sample_vertices;    /* training samples of a training path: RC_NRC_ALL_ */
+                                /* VERTICES (each diffuse vertex with a long enough */
+                                /* suffix; default) or RC_NRC_LOOKUP_VERTEX (only   */
+                                /* the vertex at terminate_segment: its suffix has  */
+                                /* exactly the depth budget a lookup stands for)    */
+    int32_t reserved;           /* 0                                                 */
 } rc_nrc_config;
+
+typedef enum rc_nrc_sample_vertices { RC_NRC_ALL_VERTICES = 0, RC_NRC_LOOKUP_VERTEX = 1 } rc_nrc_sample_vertices;
 
 typedef enum rc_nrc_lookup_kernel { RC_NRC_MMA_SYNC = 0, RC_NRC_TCGEN05 = 1 } rc_nrc_lookup_kernel;
 

@@ -116,7 +116,8 @@ class rc_nrc_config(C.Structure):
                 ("train_steps", C.c_int32), ("train_batch", C.c_int32), ("min_suffix", C.c_int32),
                 ("learning_rate", C.c_float), ("beta1", C.c_float), ("beta2", C.c_float), ("epsilon", C.c_float),
                 ("box_min", C.c_float * 3), ("box_max", C.c_float * 3), ("seed", C.c_uint64),
-                ("lookup_kernel", C.c_int32), ("tc_wait_polls", C.c_int32)]
+                ("lookup_kernel", C.c_int32), ("tc_wait_polls", C.c_int32), ("sample_vertices", C.c_int32),
+                ("reserved", C.c_int32)]
 
 
 class rc_nrc_stats(C.Structure):

@@ -280,6 +280,7 @@ void nrc_pass_state(rc_tracer* h, PassParams& pp, uint32_t passIndex)
     q.trainStride = std::max(n.cfg.train_stride, 1);
     q.groups = int((uint64_t(pp.nslots) + uint64_t(q.trainStride) - 1) / uint64_t(q.trainStride));
     q.minSuffix = n.cfg.min_suffix;
+    q.lookupVertexOnly = n.cfg.sample_vertices == RC_NRC_LOOKUP_VERTEX ? 1 : 0;
     q.trainKey = mix32(mix32(mix32(uint32_t(n.cfg.seed) ^ 0x4e524331u) ^ uint32_t(n.cfg.seed >> 32) ^ h->frameIndex) ^
                        passIndex);
 }
@@ -382,6 +383,8 @@ rc_status rc_nrc_configure(rc_tracer* h, const rc_nrc_config* c)
         return fail(h, RC_INVALID_ARG, "nrc_configure: invalid optimizer settings");
     if (c->lookup_kernel != RC_NRC_MMA_SYNC && c->lookup_kernel != RC_NRC_TCGEN05)
         return fail(h, RC_INVALID_ARG, "nrc_configure: unknown lookup kernel");
+    if ((c->sample_vertices != RC_NRC_ALL_VERTICES && c->sample_vertices != RC_NRC_LOOKUP_VERTEX) || c->reserved != 0)
+        return fail(h, RC_INVALID_ARG, "nrc_configure: unknown sample_vertices / reserved not 0");
     cudaSetDevice(h->device);
     h->nrc.cfg = *c;
     NRC_STATUS(alloc_state(h));

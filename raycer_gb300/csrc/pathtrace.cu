@@ -709,7 +709,7 @@ __global__ void __launch_bounds__(256) k_nrc_targets(PassParams p)
         // tag: vertex index << 24 | training path (group) index
         p.nrc.vtx[idx].d = make_float4(r, gg, b, __uint_as_float((uint32_t(i) << 24) | g));
         // specular (dielectric) vertices carry albedo -1: not samples
-        if (i <= last && !(p.nrc.vtx[idx].c.y < 0.0f))
+        if (i <= last && !(p.nrc.vtx[idx].c.y < 0.0f) && (!p.nrc.lookupVertexOnly || i == p.nrc.termSegment))
             count++;
     }
     if (count == 0)
@@ -718,7 +718,7 @@ __global__ void __launch_bounds__(256) k_nrc_targets(PassParams p)
     for (int i = last; i >= 0; --i)
     {
         const size_t idx = size_t(i) * size_t(p.nrc.groups) + g;
-        if (!(p.nrc.vtx[idx].c.y < 0.0f))
+        if (!(p.nrc.vtx[idx].c.y < 0.0f) && (!p.nrc.lookupVertexOnly || i == p.nrc.termSegment))
             p.nrc.index[k++] = int(idx);
     }
 }

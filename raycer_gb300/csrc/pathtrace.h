@@ -75,6 +75,7 @@ struct NrcPass
     int groups;           // ceil(nslots / trainStride)
     int minSuffix;        // vertices a suffix cut by the depth limit needs to be a sample
     uint32_t trainKey;    // per-pass key of the training-slot choice
+    int lookupVertexOnly; // 1: the vertex at termSegment is a path's only sample
 };
 // NrcPass::term flags: vertex count | truncated << 8 | active << 9.
 constexpr uint32_t kNrcTermTruncated = 1u << 8;

@@ -420,7 +420,8 @@ def _random_rotations(rng, count):
 
 def heightfield_blobs_scene(instances: int = 200, blob_level: int = 5, seed: int = 4, hf_nx: int = 1024,
                             hf_nz: int = 512, width: int = 1920, height: int = 1080,
-                            sky=(1.0, 1.0, 1.0), enclosed: bool = False) -> SceneDesc:
+                            sky=(1.0, 1.0, 1.0), enclosed: bool = False, panel=(10.0, 5.0),
+                            panel_radiance: float = 12.0) -> SceneDesc:
     """The radiance-cache workload: the 1,045,506-triangle heightfield (value
     noise seed 2) plus `instances` copies of one 20,480-triangle random blob at
     uniform random positions over the terrain, uniform random rotations,
@@ -429,8 +430,9 @@ def heightfield_blobs_scene(instances: int = 200, blob_level: int = 5, seed: int
 
     enclosed=True: the same geometry inside a closed box (x -14..14, y -1..8,
     z -8..14, inward-facing walls of albedo 0.75, the camera inside) lit by an
-    emissive 10 x 5 panel of radiance 12 just under the ceiling, and no sky:
-    every path runs to the depth limit unless it reaches the panel."""
+    emissive `panel` (width x depth, centred; 10 x 5 by default) of radiance
+    `panel_radiance` just under the ceiling, and no sky: every path runs to
+    the depth limit unless it reaches the panel."""
     hf = heightfield_scene(seed=2, nx=hf_nx, nz=hf_nz, width=width, height=height)
     blob = blob_mesh(seed=seed, level=blob_level).reshape(-1, 3, 3)
     rng = np.random.Generator(np.random.PCG64(seed))
@@ -464,9 +466,11 @@ def heightfield_blobs_scene(instances: int = 200, blob_level: int = 5, seed: int
             _quad((x0, y0, z0), (0, dy, 0), (0, 0, dz)),   # left, +x
             _quad((x1, y0, z0), (0, 0, dz), (0, dy, 0)),   # right, -x
         ])
-        panel = np.array(_quad((-5.0, y1 - 0.01, -2.5), (10.0, 0, 0), (0, 0, 5.0)))  # facing down, -y
+        pw, pd = float(panel[0]), float(panel[1])
+        panel = np.array(_quad((-0.5 * pw, y1 - 0.01, -0.5 * pd), (pw, 0, 0), (0, 0, pd)))  # facing down, -y
+        le = float(panel_radiance)
         mats = mats + [Material(diffuse=(0.75, 0.75, 0.75)),
-                       Material(diffuse=(0.0, 0.0, 0.0), emittance=(12.0, 12.0, 12.0), is_emissive=True)]
+                       Material(diffuse=(0.0, 0.0, 0.0), emittance=(le, le, le), is_emissive=True)]
         wall_id, light_id = len(mats) - 2, len(mats) - 1
         verts = np.concatenate([verts, _f32(walls), _f32(panel)])
         midx = np.concatenate([midx, np.full(walls.shape[0], wall_id, np.uint32),
