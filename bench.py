@@ -32,7 +32,9 @@ At N = 1 the line also carries the rest of the headline (unless
             this host's cores (Tracer.cpp:58, PathTracer.cpp:25)
   nrc       time to display RMSE 0.01 of the radiance-cache tracer and of
             the plain tracer against a float64 4096-spp ground truth on the
-            heightfield + 200 blobs scene at 1080p
+            heightfield + 200 blobs scene at 1080p, closed in a box lit by an
+            emissive ceiling panel (the scene has no emitter of its own)
+  nrc_sky   the same under a uniform sky instead of the box
 
 `--impl reference` times the reference's CPU ray casting on this host's cores
 (the reference's own code where it was compiled, else the float64 port) on
@@ -507,7 +509,8 @@ def run_ours(args, rank, local_rank, world):
             # the rest of the headline: plain path tracing on the 1M-triangle
             # scene, and the radiance cache's time to RMSE 0.01
             line["path_1m"] = path_1m_record(max(3, min(args.steps, 20)), max(3, min(args.warmup, 5)), local_rank)
-            line["nrc"] = nrc_record(args.gt_spp, local_rank)
+            line["nrc"] = nrc_record(args.gt_spp, local_rank, enclosed=True)
+            line["nrc_sky"] = nrc_record(args.gt_spp, local_rank, enclosed=False)
         if world == 1:
             try:
                 res = cpu_raycast(sc, 2, 1, None)
@@ -622,7 +625,8 @@ def nrc_record(gt_spp, device, enclosed=False, max_seconds=60.0):
 
     return {"workload": f"radiance cache vs plain path tracing: heightfield + 200 blobs, {sc.triangle_count} tris, "
                         f"{sc.width}x{sc.height}, 1 spp/frame, depth 12, "
-                        + ("closed box lit by an emissive panel" if enclosed else "sky-lit"),
+                        + ("closed box lit by a 20 x 11 emissive ceiling panel of radiance 3" if enclosed
+                           else "sky-lit"),
             "target_rmse": 0.01, "gt_spp": res.gt_spp, "gt_seconds": round(res.gt_seconds, 1),
             "scene_build_s": round(build_s, 1), "plain": run_dict(res.plain), "cache": run_dict(res.cache),
             "time_ratio_cache_over_plain": (round(res.cache.seconds / res.plain.seconds, 3)

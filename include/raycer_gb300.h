@@ -592,11 +592,15 @@ typedef struct rc_nrc_config
                                 /* (4,194,304); < 0 = none, so every wait gives up   */
                                 /* at once (exercises that error path; the kernel    */
                                 /* still lets its MMAs finish before it frees TMEM)  */
-    int32_t sample_vertices;    /* training samples of a training path: RC_NRC_ALL_ */
-                                /* VERTICES (each diffuse vertex with a long enough */
-                                /* suffix; default) or RC_NRC_LOOKUP_VERTEX (only   */
-                                /* the vertex at terminate_segment: its suffix has  */
-                                /* exactly the depth budget a lookup stands for)    */
+    int32_t sample_vertices;    /* training samples of a training path:             */
+                                /* RC_NRC_LOOKUP_VERTEX (default): only the vertex  */
+                                /* at terminate_segment, whose suffix has exactly   */
+                                /* the depth budget (max_path_length minus the      */
+                                /* segments before it) that a lookup stands for;    */
+                                /* RC_NRC_ALL_VERTICES: every diffuse vertex with a */
+                                /* long enough suffix (deeper vertices have smaller */
+                                /* budgets, so a depth-limited render is biased low */
+                                /* where paths reach the limit)                     */
     int32_t reserved;           /* 0                                                 */
 } rc_nrc_config;
 

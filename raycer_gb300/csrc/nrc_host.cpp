@@ -366,6 +366,7 @@ rc_status rc_nrc_defaults(rc_nrc_config* c)
     c->epsilon = 1e-8f;
     c->seed = 1;
     c->lookup_kernel = RC_NRC_TCGEN05;
+    c->sample_vertices = RC_NRC_LOOKUP_VERTEX;
     return RC_OK;
 }
 

@@ -420,8 +420,8 @@ def _random_rotations(rng, count):
 
 def heightfield_blobs_scene(instances: int = 200, blob_level: int = 5, seed: int = 4, hf_nx: int = 1024,
                             hf_nz: int = 512, width: int = 1920, height: int = 1080,
-                            sky=(1.0, 1.0, 1.0), enclosed: bool = False, panel=(10.0, 5.0),
-                            panel_radiance: float = 12.0) -> SceneDesc:
+                            sky=(1.0, 1.0, 1.0), enclosed: bool = False, panel=(20.0, 11.0),
+                            panel_radiance: float = 3.0) -> SceneDesc:
     """The radiance-cache workload: the 1,045,506-triangle heightfield (value
     noise seed 2) plus `instances` copies of one 20,480-triangle random blob at
     uniform random positions over the terrain, uniform random rotations,
@@ -430,9 +430,9 @@ def heightfield_blobs_scene(instances: int = 200, blob_level: int = 5, seed: int
 
     enclosed=True: the same geometry inside a closed box (x -14..14, y -1..8,
     z -8..14, inward-facing walls of albedo 0.75, the camera inside) lit by an
-    emissive `panel` (width x depth, centred; 10 x 5 by default) of radiance
-    `panel_radiance` just under the ceiling, and no sky: every path runs to
-    the depth limit unless it reaches the panel."""
+    emissive `panel` (width x depth, centred; 20 x 11 by default, a third of
+    the ceiling) of radiance `panel_radiance` (3) just under the ceiling, and
+    no sky: every path runs to the depth limit unless it reaches the panel."""
     hf = heightfield_scene(seed=2, nx=hf_nx, nz=hf_nz, width=width, height=height)
     blob = blob_mesh(seed=seed, level=blob_level).reshape(-1, 3, 3)
     rng = np.random.Generator(np.random.PCG64(seed))
