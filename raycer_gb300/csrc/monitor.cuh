@@ -117,4 +117,21 @@ __device__ __forceinline__ bool warp_poll(RenderMonitor* mon, unsigned long long
     return __shfl_sync(0xffffffffu, why, 0) != 0;
 }
 
+// warp_poll for a fetch of `n` entries (1..32) at `base` that need not be a
+// multiple of 32: polls where the range starts a 256-item block or crosses
+// into one.
+__device__ __forceinline__ bool warp_poll_range(RenderMonitor* mon, unsigned long long budgetNs, DevControl* ctl,
+                                                unsigned* head, unsigned base, unsigned n, bool mayStop,
+                                                unsigned long long publish)
+{
+    constexpr unsigned kShift = kPollItemsLog2 + 5;
+    if (!monitored(mon, budgetNs) ||
+        ((base & ((1u << kShift) - 1u)) != 0u && (base >> kShift) == ((base + n - 1u) >> kShift)))
+        return false;
+    int why = 0;
+    if ((threadIdx.x & 31u) == 0u)
+        why = poll_render(mon, budgetNs, ctl, head, mayStop, publish);
+    return __shfl_sync(0xffffffffu, why, 0) != 0;
+}
+
 }  // namespace rcx

@@ -26,6 +26,7 @@
 // host never waits on (and can be captured in a CUDA graph).
 
 #include <cfloat>
+#include <cstdlib>
 
 #include "filters.cuh"
 #include "monitor.cuh"
@@ -251,6 +252,91 @@ __global__ void __launch_bounds__(BLOCK, ((ORDER == ORDER_WIDE ? RC_EXTEND_WIDE_
         }
     }
     flush_extend_counts(p, done, cnt, err);
+}
+
+// Extend through the 4-wide BVH with lane refill (Aila & Laine 2009's
+// dynamic fetch): bounce rays are incoherent and their walks differ in
+// length, so a warp that takes 32 rays and walks them to the end spends most
+// of its issue slots on a few long walks (about 7.6 of 32 lanes active per
+// instruction). Here a lane whose ray is done takes a new one: whenever at
+// least kRefillLanes lanes are idle the warp takes that many queue entries
+// with one atomic and hands them to its idle lanes, which start their walks
+// while the others continue theirs (wide_step keeps each walk's position
+// between steps). Each ray's walk, hence its hit, is traverse_wide's.
+#ifndef RC_EXTEND_REFILL_LANES
+#define RC_EXTEND_REFILL_LANES 8
+#endif
+#ifndef RC_EXTEND_REFILL_MIN_BLOCKS
+#define RC_EXTEND_REFILL_MIN_BLOCKS 8
+#endif
+
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK, (RC_EXTEND_REFILL_MIN_BLOCKS * 128) / BLOCK)
+    k_extend_refill(PassParams p, int segment)
+{
+    const unsigned total = *reinterpret_cast<volatile unsigned*>(&p.counts[segment * 4 + 0]);
+    const int* __restrict__ queue = (segment & 1) ? p.qb : p.qa;
+    unsigned* head = &p.counts[segment * 4 + 1];
+    if (pass_stopped(p))
+        return;
+    int err = 0;
+    unsigned long long done = 0;
+    int stack[kMaxStack];
+    float sdist[kMaxStack];
+    int s = -1;  // this lane's path slot, -1 = idle
+    RayF ray;
+    HitF h{ -1, FLT_MAX, 0.0f, 0.0f, -1 };
+    WideWalk w{ 0, 0, false };
+    int skip = -1;
+    const DevNode4* wide = nullptr;
+    const DevTri* tris = nullptr;
+    bool drained = false;  // warp-uniform
+    const unsigned below = (1u << lane_id()) - 1u;
+    while (true)
+    {
+        const unsigned idle = __ballot_sync(0xffffffffu, s < 0);
+        if (!drained && __popc(idle) >= RC_EXTEND_REFILL_LANES)
+        {
+            const unsigned n = unsigned(__popc(idle));
+            unsigned base = 0;
+            if (lane_id() == 0)
+                base = atomicAdd(head, n);
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (base >= total ||
+                warp_poll_range(p.monitor, p.budgetNs, p.ctl, head, base, n, true, kPublishProgress))
+                drained = true;
+            else if (s < 0)
+            {
+                const unsigned q = base + unsigned(__popc(idle & below));
+                if (q < total)
+                {
+                    s = queue[q];
+                    const DevScene sc = scene_of_slot(p, s);
+                    const float4 o = p.o[s];
+                    const float4 d = p.d[s];
+                    ray = make_ray(v3(o.x, o.y, o.z), v3(d.x, d.y, d.z), 0.0f, FLT_MAX);
+                    h = HitF{ -1, FLT_MAX, 0.0f, 0.0f, -1 };
+                    w = WideWalk{ sc.wideRoot, 0, false };
+                    skip = __float_as_int(o.w);
+                    wide = sc.wide;
+                    tris = sc.tris;
+                }
+            }
+        }
+        if (__ballot_sync(0xffffffffu, s >= 0) == 0u)
+        {
+            if (drained)
+                break;
+            continue;
+        }
+        if (s >= 0 && wide_step(wide, tris, ray, h, w, stack, sdist, skip, err))
+        {
+            p.hit[s] = make_int4(w.found ? h.slot : -1, __float_as_int(h.t), __float_as_int(h.u), __float_as_int(h.v));
+            done++;
+            s = -1;
+        }
+    }
+    flush_extend_counts(p, done, TravCount{ 0, 0 }, err);
 }
 
 // Extend for passes with two-level scenes: 32 queue entries per warp fetch,
@@ -639,9 +725,37 @@ cudaError_t extend_b(const PassParams& p, int segment, cudaStream_t stream, int 
     return cudaGetLastError();
 }
 
+template <int BLOCK>
+cudaError_t extend_refill_b(const PassParams& p, int segment, cudaStream_t stream, int numSMs)
+{
+    auto k = k_extend_refill<BLOCK>;
+    static OccupancyCache occ;
+    k<<<persistent_blocks(k, BLOCK, numSMs, occ), BLOCK, 0, stream>>>(p, segment);
+    return cudaGetLastError();
+}
+
+// Whether the uncounted 4-wide extend refills idle lanes (k_extend_refill;
+// RC_EXTEND_REFILL=0 keeps one batch of 32 rays per warp; read once).
+bool extend_refill()
+{
+    static const bool on = [] {
+        const char* v = std::getenv("RC_EXTEND_REFILL");
+        return !(v && v[0] == '0');
+    }();
+    return on;
+}
+
 template <int ORDER, bool COUNT>
 cudaError_t extend_t(const PassParams& p, int segment, int block, cudaStream_t stream, int numSMs)
 {
+    if (ORDER == ORDER_WIDE && !COUNT && extend_refill())
+    {
+        if (block == 64)
+            return extend_refill_b<64>(p, segment, stream, numSMs);
+        if (block == 256)
+            return extend_refill_b<256>(p, segment, stream, numSMs);
+        return extend_refill_b<128>(p, segment, stream, numSMs);
+    }
     if (block == 64)
         return extend_b<ORDER, COUNT, 64>(p, segment, stream, numSMs);
     if (block == 256)

@@ -312,106 +312,125 @@ __device__ __forceinline__ void wide_cswap(float& da, int& la, float& db, int& l
 // hit (minimum t, ties to the larger slot) does not depend on the order, so
 // it is traverse<false, ORDER_NEAREST>'s. No node or triangle counts: counted
 // frames use the binary traversal.
-__device__ __forceinline__ bool traverse_wide(const DevScene& sc, const RayF& ray, HitF& hit, int& err, int skip)
+// Where a 4-wide walk stands between steps: the node or leaf link to visit
+// next and the stack depth (the stack arrays are the caller's).
+struct WideWalk
+{
+    int cur;
+    int sp;
+    bool found;
+};
+
+// One step of the 4-wide walk: a node fetch (entering its nearest child hit
+// within the current closest distance, the others pushed) or a leaf's
+// triangle tests; where no child is entered, the pop of the next stack entry
+// still in range. Returns true when the walk is over (stack empty, or
+// overflow: err = 1).
+__device__ __forceinline__ bool wide_step(const DevNode4* __restrict__ wide, const DevTri* __restrict__ tris,
+                                          const RayF& ray, HitF& hit, WideWalk& w, int* stack, float* sdist,
+                                          int skip, int& err)
 {
     const float kInf = __int_as_float(0x7f800000);
-    int stack[kMaxStack];
-    float sdist[kMaxStack];
-    int sp = 0;
-    int cur = sc.wideRoot;
-    bool found = false;
-    while (true)
+    if (w.cur >= 0)
     {
-        if (cur >= 0)
+        const float4* p = reinterpret_cast<const float4*>(wide + w.cur);
+        const float4 lox = __ldg(p + 0), hix = __ldg(p + 1), loy = __ldg(p + 2), hiy = __ldg(p + 3);
+        const float4 loz = __ldg(p + 4), hiz = __ldg(p + 5);
+        const int4 l = __ldg(reinterpret_cast<const int4*>(p + 6));
+        const int nc = __ldg(reinterpret_cast<const int*>(p + 7));
+        float d0 = wide_entry(ray, lox.x, hix.x, loy.x, hiy.x, loz.x, hiz.x, hit.t);
+        float d1 = wide_entry(ray, lox.y, hix.y, loy.y, hiy.y, loz.y, hiz.y, hit.t);
+        float d2 = nc > 2 ? wide_entry(ray, lox.z, hix.z, loy.z, hiy.z, loz.z, hiz.z, hit.t) : kInf;
+        float d3 = nc > 3 ? wide_entry(ray, lox.w, hix.w, loy.w, hiy.w, loz.w, hiz.w, hit.t) : kInf;
+        int l0 = l.x, l1 = l.y, l2 = l.z, l3 = l.w;
+        const int hits = (d0 < kInf ? 1 : 0) + (d1 < kInf ? 1 : 0) + (d2 < kInf ? 1 : 0) + (d3 < kInf ? 1 : 0);
+        if (hits == 1)
         {
-            const float4* p = reinterpret_cast<const float4*>(sc.wide + cur);
-            const float4 lox = __ldg(p + 0), hix = __ldg(p + 1), loy = __ldg(p + 2), hiy = __ldg(p + 3);
-            const float4 loz = __ldg(p + 4), hiz = __ldg(p + 5);
-            const int4 l = __ldg(reinterpret_cast<const int4*>(p + 6));
-            const int nc = __ldg(reinterpret_cast<const int*>(p + 7));
-            float d0 = wide_entry(ray, lox.x, hix.x, loy.x, hiy.x, loz.x, hiz.x, hit.t);
-            float d1 = wide_entry(ray, lox.y, hix.y, loy.y, hiy.y, loz.y, hiz.y, hit.t);
-            float d2 = nc > 2 ? wide_entry(ray, lox.z, hix.z, loy.z, hiy.z, loz.z, hiz.z, hit.t) : kInf;
-            float d3 = nc > 3 ? wide_entry(ray, lox.w, hix.w, loy.w, hiy.w, loz.w, hiz.w, hit.t) : kInf;
-            int l0 = l.x, l1 = l.y, l2 = l.z, l3 = l.w;
-            const int hits = (d0 < kInf ? 1 : 0) + (d1 < kInf ? 1 : 0) + (d2 < kInf ? 1 : 0) + (d3 < kInf ? 1 : 0);
-            if (hits == 1)
-            {
-                cur = d0 < kInf ? l0 : (d1 < kInf ? l1 : (d2 < kInf ? l2 : l3));
-                continue;
-            }
-            if (hits > 1)
-            {
-                wide_cswap(d0, l0, d1, l1);
-                wide_cswap(d2, l2, d3, l3);
-                wide_cswap(d0, l0, d2, l2);
-                wide_cswap(d1, l1, d3, l3);
-                wide_cswap(d1, l1, d2, l2);
-                if (sp + hits - 1 > kMaxStack)
-                {
-                    err = 1;
-                    return found;
-                }
-                if (d3 < kInf)
-                {
-                    stack[sp] = l3;
-                    sdist[sp] = d3;
-                    sp++;
-                }
-                if (d2 < kInf)
-                {
-                    stack[sp] = l2;
-                    sdist[sp] = d2;
-                    sp++;
-                }
-                if (d1 < kInf)
-                {
-                    stack[sp] = l1;
-                    sdist[sp] = d1;
-                    sp++;
-                }
-                cur = l0;
-                continue;
-            }
+            w.cur = d0 < kInf ? l0 : (d1 < kInf ? l1 : (d2 < kInf ? l2 : l3));
+            return false;
         }
-        else
+        if (hits > 1)
         {
-            const int leaf = ~cur;
-            const int start = leaf >> kLeafCountBits;
-            const int count = leaf & ((1 << kLeafCountBits) - 1);
-            for (int i = 0; i < count; ++i)
+            wide_cswap(d0, l0, d1, l1);
+            wide_cswap(d2, l2, d3, l3);
+            wide_cswap(d0, l0, d2, l2);
+            wide_cswap(d1, l1, d3, l3);
+            wide_cswap(d1, l1, d2, l2);
+            if (w.sp + hits - 1 > kMaxStack)
             {
-                const int slot = start + i;
-                if (slot == skip)
-                    continue;
-                const float4* tp = reinterpret_cast<const float4*>(sc.tris + slot);
-                const float4 ta = __ldg(tp + 0);
-                const float4 tb = __ldg(tp + 1);
-                const float4 tc = __ldg(tp + 2);
-                float t, u, v;
-                if (tri_hit(ray, v3(ta.x, ta.y, ta.z), v3(ta.w, tb.x, tb.y), v3(tb.z, tb.w, tc.x), t, u, v) &&
-                    (t < hit.t || (t == hit.t && slot > hit.slot)))
-                {
-                    hit.slot = slot;
-                    hit.t = t;
-                    hit.u = u;
-                    hit.v = v;
-                    found = true;
-                }
+                err = 1;
+                return true;
             }
-        }
-        // pop
-        while (true)
-        {
-            if (sp == 0)
-                return found;
-            sp--;
-            cur = stack[sp];
-            if (sdist[sp] > hit.t)
-                continue;
-            break;
+            if (d3 < kInf)
+            {
+                stack[w.sp] = l3;
+                sdist[w.sp] = d3;
+                w.sp++;
+            }
+            if (d2 < kInf)
+            {
+                stack[w.sp] = l2;
+                sdist[w.sp] = d2;
+                w.sp++;
+            }
+            if (d1 < kInf)
+            {
+                stack[w.sp] = l1;
+                sdist[w.sp] = d1;
+                w.sp++;
+            }
+            w.cur = l0;
+            return false;
         }
     }
+    else
+    {
+        const int leaf = ~w.cur;
+        const int start = leaf >> kLeafCountBits;
+        const int count = leaf & ((1 << kLeafCountBits) - 1);
+        for (int i = 0; i < count; ++i)
+        {
+            const int slot = start + i;
+            if (slot == skip)
+                continue;
+            const float4* tp = reinterpret_cast<const float4*>(tris + slot);
+            const float4 ta = __ldg(tp + 0);
+            const float4 tb = __ldg(tp + 1);
+            const float4 tc = __ldg(tp + 2);
+            float t, u, v;
+            if (tri_hit(ray, v3(ta.x, ta.y, ta.z), v3(ta.w, tb.x, tb.y), v3(tb.z, tb.w, tc.x), t, u, v) &&
+                (t < hit.t || (t == hit.t && slot > hit.slot)))
+            {
+                hit.slot = slot;
+                hit.t = t;
+                hit.u = u;
+                hit.v = v;
+                w.found = true;
+            }
+        }
+    }
+    // pop
+    while (true)
+    {
+        if (w.sp == 0)
+            return true;
+        w.sp--;
+        w.cur = stack[w.sp];
+        if (sdist[w.sp] > hit.t)
+            continue;
+        return false;
+    }
+}
+
+__device__ __forceinline__ bool traverse_wide(const DevScene& sc, const RayF& ray, HitF& hit, int& err, int skip)
+{
+    int stack[kMaxStack];
+    float sdist[kMaxStack];
+    WideWalk w{ sc.wideRoot, 0, false };
+    while (!wide_step(sc.wide, sc.tris, ray, hit, w, stack, sdist, skip, err))
+    {
+    }
+    return w.found;
 }
 
 // One stack entry of the warp-wide traversal: a node link and the lanes

@@ -7,6 +7,7 @@ import numpy as np
 import pytest
 
 import oracle
+from raycer_gb300 import _native as N
 from raycer_gb300 import scenes
 from raycer_gb300.nrc import GroundTruth, RadianceCache, unpack_layers
 from raycer_gb300.tracer import CudaTracer, TracerState, general_record
@@ -153,7 +154,8 @@ def test_training_targets_are_path_radiance():
     """With every slot a training path, vertex 0's target is that pixel's plain
     path value (the film at 1 sample per pixel)."""
     sc = nrc_scene()
-    film, samples = render_film(sc, seed=4, cache_cfg=dict(train_stride=1, train_steps=0),
+    film, samples = render_film(sc, seed=4, cache_cfg=dict(train_stride=1, train_steps=0,
+                                                            sample_vertices=N.RC_NRC_ALL_VERTICES),
                                 read_cache=lambda c: c.samples())
     vi, gi = RadianceCache.sample_tags(samples)
     assert samples.shape[0] > film.shape[0] // 2
@@ -168,6 +170,26 @@ def test_training_targets_are_path_radiance():
     # at most max_path_length vertices per path, each counted once
     assert vi.max() < sc.settings["max_path_length"]
     assert len(set(zip(vi.tolist(), gi.tolist()))) == samples.shape[0]
+
+
+def test_lookup_vertex_samples_are_the_lookup_vertex_targets():
+    """RC_NRC_LOOKUP_VERTEX (the default): a training path's only sample is
+    its vertex at terminate_segment, whose suffix has the depth budget of a
+    lookup there; on the same paths it equals the every-vertex run's sample
+    of that vertex, record for record."""
+    sc = nrc_scene()
+    runs = {}
+    for mode in (N.RC_NRC_ALL_VERTICES, N.RC_NRC_LOOKUP_VERTEX):
+        _, samples = render_film(sc, seed=4, cache_cfg=dict(train_stride=1, train_steps=0, sample_vertices=mode),
+                                 read_cache=lambda c: c.samples())
+        runs[mode] = samples
+    vi, gi = RadianceCache.sample_tags(runs[N.RC_NRC_LOOKUP_VERTEX])
+    assert vi.size > 100 and np.all(vi == 2)
+    va, ga = RadianceCache.sample_tags(runs[N.RC_NRC_ALL_VERTICES])
+    at2 = runs[N.RC_NRC_ALL_VERTICES][va == 2]
+    key = lambda a: np.lexsort((RadianceCache.sample_tags(a)[1],))
+    lv = runs[N.RC_NRC_LOOKUP_VERTEX]
+    assert np.array_equal(lv[key(lv)], at2[key(at2)])
 
 
 def zero_cache_params() -> np.ndarray:
