@@ -145,6 +145,8 @@ RC_BUILDER_REFERENCE_SAH = 0
 RC_BUILDER_GPU_LBVH = 1
 RC_NRC_MMA_SYNC = 0
 RC_NRC_TCGEN05 = 1
+RC_NRC_ALL_VERTICES = 0
+RC_NRC_LOOKUP_VERTEX = 1
 RC_NRC_PARAMS = 20992
 RC_NRC_QUERY_FLOATS = 12
 RC_NRC_INPUTS = 128

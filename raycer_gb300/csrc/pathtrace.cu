@@ -734,13 +734,15 @@ cudaError_t extend_refill_b(const PassParams& p, int segment, cudaStream_t strea
     return cudaGetLastError();
 }
 
-// Whether the uncounted 4-wide extend refills idle lanes (k_extend_refill;
-// RC_EXTEND_REFILL=0 keeps one batch of 32 rays per warp; read once).
+// Whether the uncounted 4-wide extend refills idle lanes (k_extend_refill,
+// RC_EXTEND_REFILL=1; read once). Off by default: on the 1080p workloads it
+// measured 3-6 % slower than one batch of 32 rays per warp at every refill
+// threshold (4-24 idle lanes) and register budget (6-9 blocks per SM) tried.
 bool extend_refill()
 {
     static const bool on = [] {
         const char* v = std::getenv("RC_EXTEND_REFILL");
-        return !(v && v[0] == '0');
+        return v && v[0] == '1';
     }();
     return on;
 }
