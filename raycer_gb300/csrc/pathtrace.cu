@@ -195,7 +195,8 @@ __global__ void __launch_bounds__(256) k_generate(PassParams p)
 
 __device__ __forceinline__ DevScene scene_of_slot(const PassParams& p, int s)
 {
-    return p.scenes[p.chunks[p.chunkOf[s]].scene].sc;
+    // one-scene renders: no dependent loads through the slot's chunk
+    return p.singleScene ? p.scene0 : p.scenes[p.chunks[p.chunkOf[s]].scene].sc;
 }
 
 __device__ __forceinline__ void flush_extend_counts(const PassParams& p, unsigned long long done, const TravCount& cnt,

@@ -102,6 +102,9 @@ struct PassParams
     NrcPass nrc;
     int instanced;   // 1: the pass has two-level scenes (k_extend_instanced)
     int wide;        // 1: every scene of the pass has its 4-wide BVH (uncounted nearest-first extend uses it)
+    int singleScene = 0;  // 1: every slot of the pass is scene0's (a one-scene render), so the
+                          // extend kernels read the scene record from the parameters, not the table
+    DevScene scene0;
     RenderMonitor* monitor = nullptr;         // monitored render (rc_render): cancel word and progress, else null
     unsigned long long budgetNs = kNoBudget;  // the render's time budget (kNoBudget: none)
 };

@@ -278,6 +278,8 @@ rc_status render_path(rc_tracer* h, uint64_t pixelStart, uint64_t count, RenderW
     pp.segments = g.max_path_length;
     pp.instanced = h->nInstances > 0 ? 1 : 0;
     pp.wide = h->dWide != nullptr && h->nInstances == 0 ? 1 : 0;
+    pp.singleScene = 1;
+    pp.scene0 = ps.sc;
     if (watch)
     {
         pp.monitor = watch->dev;
