@@ -315,8 +315,9 @@ rc_status rc_clear(rc_tracer* h);
  * (ConsoleRunner.cpp:126-142):
  *   cancel (optional): a flag another host thread may raise at any time
  *     during the call. The calling thread forwards it to a word in pinned,
- *     device-mapped host memory that the kernels check every 256 work items
- *     (of 32 rays or paths); they then take no more work. The call returns
+ *     device-mapped host memory that one watching warp of the kernels checks
+ *     about every 2 microseconds; the working warps then take no more work
+ *     (items of 32 rays or paths already taken finish). The call returns
  *     RC_CANCELLED. A RAY frame keeps the records of the pixels it traced
  *     (the others are untouched); a PATH film keeps whole passes only.
  *   pixels_processed (optional): set to 0 at entry; while the kernels run
@@ -336,9 +337,10 @@ rc_status rc_render(rc_tracer* h, uint64_t pixel_start, uint64_t pixel_count,
 /* Time budget of every later rc_render on this handle (GPU-only extension;
  * the reference has no counterpart): the kernels stop taking work once
  * `milliseconds` of device time have passed since the render's first work
- * item (checked every 256 work items), and the call returns RC_TIMEOUT with
- * the results of rc_render's cancel case. 0 stops at the first check (no
- * work done); a negative value removes the budget (the default). */
+ * (checked about every 2 microseconds), and the call returns RC_TIMEOUT with
+ * the results of rc_render's cancel case. 0 stops at the first check (the
+ * items taken by then still finish); a negative value removes the budget
+ * (the default). */
 rc_status rc_set_time_budget(rc_tracer* h, double milliseconds);
 
 /* Film::generateToneMappedImage (Film.cpp:61-69) with the handle's tone

@@ -113,8 +113,8 @@ struct __align__(16) DevInstance
 // Progress and stop word of one render (rc_render): pinned host memory mapped
 // into the device's address space, so the persistent kernels read the
 // caller's cancel request and publish their progress while they run. Both
-// fields cross the host link, so the kernels touch them once per 256 work
-// items only.
+// fields cross the host link, so only one watching warp of each kernel
+// touches them, about every 2 microseconds.
 struct RenderMonitor
 {
     volatile int cancel;                 // host -> device: non-zero = stop taking work

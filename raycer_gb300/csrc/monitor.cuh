@@ -4,20 +4,22 @@
 // TracerState::pixelsProcessed every 100 pixels (Tracer.cpp:76-112), while
 // the main thread polls it every 100 ms (ConsoleRunner.cpp:126-142). Here the
 // persistent kernels take their work in items of 32 rays or path slots from
-// an atomic queue head; a monitored render (rc_render with a cancel flag, a
-// progress counter or a time budget) makes lane 0 of the warp that took
-// every 256th item:
-//   * read the host-mapped cancel word and check the time budget (measured
+// an atomic queue head. In a monitored render (rc_render with a cancel flag,
+// a progress counter or a time budget) one warp of each such kernel, the
+// last of block 0, takes no work and watches instead (watch_queue): every
+// ~2 us its lane 0
+//   * reads the host-mapped cancel word and checks the time budget (measured
 //     from the render's first check, %globaltimer);
-//   * publish the pixels finished so far in the host-mapped monitor (PATH
+//   * publishes the pixels finished so far in the host-mapped monitor (PATH
 //     renders: the pixels whose samples the film has taken; one-kernel RAY
 //     frames: a lower bound from the queue head; the call's exact count is
 //     read from the kernels' statistics at the end).
-// A warp that sees a stop records the reason in DevControl::error and pushes
-// the queue head past any item count, so every warp's next fetch ends its
-// loop: the items already taken finish, nothing else starts. Kernels that
-// follow in the same render find the stop bit at their start and return.
-// Nothing waits here, so a stop can never hang a kernel.
+// On a stop it records the reason in DevControl::error and pushes the queue
+// head past any item count, so every warp's next fetch ends its loop: the
+// items already taken finish, nothing else starts. Kernels that follow in
+// the same render find the stop bit at their start and return. The working
+// warps' loops carry no poll, and nothing waits on the host, so a stop can
+// never hang a kernel.
 #pragma once
 
 #include "kernels.h"
@@ -25,7 +27,6 @@
 namespace rcx
 {
 
-constexpr unsigned kPollItemsLog2 = 8;             // check every 256th work item
 constexpr unsigned kHeadPastEnd = 0x7fffffffu;     // above any queue or item count
 
 __device__ __forceinline__ unsigned long long global_ns()
@@ -49,10 +50,11 @@ __device__ __forceinline__ bool render_stopped(const DevControl* ctl)
 // What a poll writes into the monitor's pixel count.
 constexpr unsigned long long kPublishNone = ~0ull;            // nothing (two-kernel RAY frames)
 constexpr unsigned long long kPublishProgress = ~0ull - 1ull;  // DevControl::progress (PATH renders)
+constexpr unsigned long long kPublishEstimate = ~0ull - 2ull;  // a lower bound from the queue head (RAY frames)
 
-// Lane 0 of the warp that took a work item of the queue whose head is
-// `head`. mayStop = false only publishes. Returns the stop reason
-// (kErrCancelled / kErrBudget) or 0.
+// One poll by the watch warp's lane 0, for the queue whose head is `head`.
+// mayStop = false only publishes. Returns the stop reason (kErrCancelled /
+// kErrBudget) or 0.
 static __device__ __noinline__ int poll_render(RenderMonitor* mon, unsigned long long budgetNs, DevControl* ctl,
                                                unsigned* head, bool mayStop, unsigned long long publish)
 {
@@ -88,50 +90,44 @@ static __device__ __noinline__ int poll_render(RenderMonitor* mon, unsigned long
     return why;
 }
 
-// Whole warp, after its fetch of `base` (a multiple of 32) from `head`:
-// true when the warp must stop taking work. `publish` as poll_render's, or
-// for a one-kernel RAY frame kPublishEstimate: the pixels of the items
-// before the ones in flight (every warp of the grid holds at most one item,
-// so when item k is taken at least k - warps items are finished), at most
-// `pixels`.
-constexpr unsigned long long kPublishEstimate = ~0ull - 2ull;
+// The watch warp of a monitored persistent kernel (the last warp of block
+// 0): it takes no work; its lane 0 polls the cancel word and the time budget
+// and publishes progress, sleeping ~2 us between polls, until the queue head
+// reaches `items` (every item taken), a stop, or kWatchPolls polls (then it
+// just stops watching). The other warps' work loop carries no poll at all.
+// publish: kPublishNone, kPublishProgress, or kPublishEstimate (the pixels of
+// the items taken before those the other warps may hold, at most `pixels`).
+constexpr unsigned kWatchPolls = 1u << 24;
 
-__device__ __forceinline__ bool warp_poll(RenderMonitor* mon, unsigned long long budgetNs, DevControl* ctl,
-                                          unsigned* head, unsigned base, bool mayStop, unsigned long long publish,
-                                          unsigned long long pixels = 0)
+static __device__ __forceinline__ void watch_queue(RenderMonitor* mon, unsigned long long budgetNs, DevControl* ctl,
+                                         unsigned* head, unsigned long long items, unsigned long long publish,
+                                         unsigned long long pixels)
 {
-    if (!monitored(mon, budgetNs) || ((base >> 5) & ((1u << kPollItemsLog2) - 1u)) != 0u)
-        return false;
-    int why = 0;
-    if ((threadIdx.x & 31u) == 0u)
+    if ((threadIdx.x & 31u) != 0u)
+        return;
+    const unsigned long long workers = static_cast<unsigned long long>(gridDim.x) * (blockDim.x >> 5) - 1ull;
+    for (unsigned i = 0; i < kWatchPolls; ++i)
     {
+        const unsigned long long h = *reinterpret_cast<const volatile unsigned*>(head);
+        if (h >= items)
+            return;
+        unsigned long long pub = publish;
         if (publish == kPublishEstimate)
         {
-            const unsigned long long warps = static_cast<unsigned long long>(gridDim.x) * (blockDim.x >> 5);
-            const unsigned long long item = base >> 5;
-            publish = item > warps ? (item - warps) * 32ull : 0ull;
-            publish = publish < pixels ? publish : pixels;
+            const unsigned long long item = h >> 5;
+            pub = item > workers ? (item - workers) * 32ull : 0ull;
+            pub = pub < pixels ? pub : pixels;
         }
-        why = poll_render(mon, budgetNs, ctl, head, mayStop, publish);
+        if (poll_render(mon, budgetNs, ctl, head, true, pub))
+            return;
+        __nanosleep(2000);
     }
-    return __shfl_sync(0xffffffffu, why, 0) != 0;
 }
 
-// warp_poll for a fetch of `n` entries (1..32) at `base` that need not be a
-// multiple of 32: polls where the range starts a 256-item block or crosses
-// into one.
-__device__ __forceinline__ bool warp_poll_range(RenderMonitor* mon, unsigned long long budgetNs, DevControl* ctl,
-                                                unsigned* head, unsigned base, unsigned n, bool mayStop,
-                                                unsigned long long publish)
+// Whether this warp is the watch warp of a monitored kernel.
+__device__ __forceinline__ bool is_watch_warp(const RenderMonitor* mon, unsigned long long budgetNs)
 {
-    constexpr unsigned kShift = kPollItemsLog2 + 5;
-    if (!monitored(mon, budgetNs) ||
-        ((base & ((1u << kShift) - 1u)) != 0u && (base >> kShift) == ((base + n - 1u) >> kShift)))
-        return false;
-    int why = 0;
-    if ((threadIdx.x & 31u) == 0u)
-        why = poll_render(mon, budgetNs, ctl, head, mayStop, publish);
-    return __shfl_sync(0xffffffffu, why, 0) != 0;
+    return monitored(mon, budgetNs) && blockIdx.x == 0 && (threadIdx.x >> 5) == (blockDim.x >> 5) - 1u;
 }
 
 }  // namespace rcx

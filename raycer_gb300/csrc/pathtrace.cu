@@ -230,12 +230,15 @@ __global__ void __launch_bounds__(BLOCK, ((ORDER == ORDER_WIDE ? RC_EXTEND_WIDE_
     unsigned long long done = 0;
     if (pass_stopped(p))
         return;
+    if (is_watch_warp(p.monitor, p.budgetNs))
+    {
+        watch_queue(p.monitor, p.budgetNs, p.ctl, &p.counts[segment * 4 + 1], total, kPublishProgress, 0);
+        return;
+    }
     while (true)
     {
         unsigned base = warp_fetch(&p.counts[segment * 4 + 1], 32u);
         if (base >= total)
-            break;
-        if (warp_poll(p.monitor, p.budgetNs, p.ctl, &p.counts[segment * 4 + 1], base, true, kPublishProgress))
             break;
         unsigned q = base + lane_id();
         if (q < total)
@@ -293,6 +296,11 @@ __global__ void __launch_bounds__(BLOCK, (RC_EXTEND_REFILL_MIN_BLOCKS * 128) / B
     const DevTri* tris = nullptr;
     bool drained = false;  // warp-uniform
     const unsigned below = (1u << lane_id()) - 1u;
+    if (is_watch_warp(p.monitor, p.budgetNs))
+    {
+        watch_queue(p.monitor, p.budgetNs, p.ctl, head, total, kPublishProgress, 0);
+        return;
+    }
     while (true)
     {
         const unsigned idle = __ballot_sync(0xffffffffu, s < 0);
@@ -303,8 +311,7 @@ __global__ void __launch_bounds__(BLOCK, (RC_EXTEND_REFILL_MIN_BLOCKS * 128) / B
             if (lane_id() == 0)
                 base = atomicAdd(head, n);
             base = __shfl_sync(0xffffffffu, base, 0);
-            if (base >= total ||
-                warp_poll_range(p.monitor, p.budgetNs, p.ctl, head, base, n, true, kPublishProgress))
+            if (base >= total)
                 drained = true;
             else if (s < 0)
             {
@@ -352,12 +359,15 @@ __global__ void __launch_bounds__(128, RC_EXTEND_INST_MIN_BLOCKS) k_extend_insta
     unsigned long long done = 0;
     if (pass_stopped(p))
         return;
+    if (is_watch_warp(p.monitor, p.budgetNs))
+    {
+        watch_queue(p.monitor, p.budgetNs, p.ctl, &p.counts[segment * 4 + 1], total, kPublishProgress, 0);
+        return;
+    }
     while (true)
     {
         unsigned base = warp_fetch(&p.counts[segment * 4 + 1], 32u);
         if (base >= total)
-            break;
-        if (warp_poll(p.monitor, p.budgetNs, p.ctl, &p.counts[segment * 4 + 1], base, true, kPublishProgress))
             break;
         unsigned q = base + lane_id();
         if (q < total)

@@ -186,13 +186,16 @@ __global__ void __launch_bounds__(kBlock, FUSED ? RC_FUSED_MIN_BLOCKS : RC_TRACE
     int err = 0;
     unsigned long long done = 0;
     const int64_t items = tilesX > 0 ? tilesX * ((height + 3) / 4) * 32 : count;
+    if (is_watch_warp(sc.monitor, sc.budgetNs))
+    {
+        watch_queue(sc.monitor, sc.budgetNs, ctl, &ctl->head[0], static_cast<unsigned long long>(items),
+                    FUSED ? kPublishEstimate : kPublishNone, static_cast<unsigned long long>(count));
+        return;
+    }
     while (true)
     {
         unsigned base = warp_fetch(&ctl->head[0], 32u);
         if (int64_t(base) >= items)
-            break;
-        if (warp_poll(sc.monitor, sc.budgetNs, ctl, &ctl->head[0], base, true,
-                      FUSED ? kPublishEstimate : kPublishNone, static_cast<unsigned long long>(count)))
             break;
         int64_t i = int64_t(base) + lane_id();
         bool valid = i < items;
