@@ -30,6 +30,8 @@ At N = 1 the line also carries the rest of the headline (unless
             overhead) at 1080p, 1 path per pixel, depth 4: device and e2e
             Mrays/s and the float64 port of the reference's path tracer on
             this host's cores (Tracer.cpp:58, PathTracer.cpp:25)
+  path_room the same measures on the room (2,012 triangles, 320x240, 16 spp
+            CMJ, depth 4)
   nrc       time to display RMSE 0.01 of the radiance-cache tracer and of
             the plain tracer against a float64 4096-spp ground truth on the
             heightfield + 200 blobs scene at 1080p, closed in a box lit by an
@@ -509,6 +511,7 @@ def run_ours(args, rank, local_rank, world):
             # the rest of the headline: plain path tracing on the 1M-triangle
             # scene, and the radiance cache's time to RMSE 0.01
             line["path_1m"] = path_1m_record(max(3, min(args.steps, 20)), max(3, min(args.warmup, 5)), local_rank)
+            line["path_room"] = path_room_record(max(3, min(args.steps, 20)), max(3, min(args.warmup, 5)), local_rank)
             line["nrc"] = nrc_record(args.gt_spp, local_rank, enclosed=True)
             line["nrc_sky"] = nrc_record(args.gt_spp, local_rank, enclosed=False)
         if world == 1:
@@ -529,25 +532,40 @@ def path_1m_record(steps, warmup, device):
     """Plain path tracing of the 1,045,506-triangle heightfield at 1920x1080
     (Tracer::run Tracer.cpp:58 -> PathTracer::traceRecursive PathTracer.cpp:25:
     one camera ray per pixel, 4 segments, the 2 rho |cos| estimator; an
-    emissive panel overhead is the light, see scenes.heightfield_path_scene).
-    One step = one frame (rc_render of every pixel). Device Mrays/s from the
+    emissive panel overhead is the light, see scenes.heightfield_path_scene)."""
+    from raycer_gb300 import scenes
+
+    return path_record(scenes.heightfield_path_scene(), "path tracing 1920x1080, 1 camera ray per pixel, depth 4, "
+                       "heightfield 1,045,506 tris + 2-triangle emissive panel", steps, warmup, device)
+
+
+def path_room_record(steps, warmup, device):
+    """Plain path tracing of the room (2,012 triangles, emissive ceiling quad)
+    at 320x240, 4x4 CMJ samples per pixel, 4 segments, box filter."""
+    from raycer_gb300 import scenes
+
+    return path_record(scenes.room_scene(), "path tracing 320x240, 16 spp (4x4 CMJ), depth 4, room 2,012 tris",
+                       steps, warmup, device)
+
+
+def path_record(sc, workload, steps, warmup, device):
+    """One step = one frame (rc_render of every pixel). Device Mrays/s from the
     renders' CUDA events with the L2 flushed before every frame; e2e through
     the public API: the render and the tone-mapped image read back to the
     host (rc_render + rc_resolve), wall clock. CPU: the float64 port of the
     reference's path tracer (its own BVH build, outside the timing) on all
-    host cores, full frames."""
+    host cores, full frames, the same samples per pixel and depth."""
     import torch
 
     import oracle
     from raycer_gb300 import _native as N
-    from raycer_gb300 import scenes
     from raycer_gb300.tracer import CudaTracer, TracerState
 
-    sc = scenes.heightfield_path_scene()
     n = sc.width * sc.height
+    depth = int(sc.settings.get("max_path_length", 4))
+    ms_sqrt = int(sc.settings.get("multi_sample_count_sqrt", 1))
     dev = torch.device("cuda", device)
-    out = {"workload": "path tracing 1920x1080, 1 camera ray per pixel, depth 4, heightfield 1,045,506 tris "
-                       "+ 2-triangle emissive panel", "triangles": sc.triangle_count}
+    out = {"workload": workload, "triangles": sc.triangle_count}
     with CudaTracer(device) as t:
         t.initializeBuffers(sc, seed=1)
         t.initializeImageBuffers(sc.width, sc.height)
@@ -589,10 +607,10 @@ def path_1m_record(steps, warmup, device):
         orc = oracle.Oracle(sc)
         build_s = time.perf_counter() - t0
         cam64 = oracle.camera64_of(sc)
-        orc.render_path64(cam64, sc.width, n, 4, 1, 1, seed=1, threads=threads)   # warm-up
+        orc.render_path64(cam64, sc.width, n, depth, 1, ms_sqrt, seed=1, threads=threads)   # warm-up
         c_rays = c_sec = 0
         for k in range(2):
-            _, r, sec = orc.render_path64(cam64, sc.width, n, 4, 1, 1, seed=2 + k, threads=threads)
+            _, r, sec = orc.render_path64(cam64, sc.width, n, depth, 1, ms_sqrt, seed=2 + k, threads=threads)
             c_rays += r
             c_sec += sec
         cpu = c_rays / c_sec / 1e6
