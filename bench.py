@@ -37,6 +37,9 @@ At N = 1 the line also carries the rest of the headline (unless
             heightfield + 200 blobs scene at 1080p, closed in a box lit by an
             emissive ceiling panel (the scene has no emitter of its own)
   nrc_sky   the same under a uniform sky instead of the box
+  batch     64 rooms of uneven size in one CUDA-graph launch per frame
+            (1 warm-up + 2 timed frames): aggregate Mrays/s, per-scene
+            latency p50 / p99
 
 `--impl reference` times the reference's CPU ray casting on this host's cores
 (the reference's own code where it was compiled, else the float64 port) on
@@ -514,6 +517,7 @@ def run_ours(args, rank, local_rank, world):
             line["path_room"] = path_room_record(max(3, min(args.steps, 20)), max(3, min(args.warmup, 5)), local_rank)
             line["nrc"] = nrc_record(args.gt_spp, local_rank, enclosed=True)
             line["nrc_sky"] = nrc_record(args.gt_spp, local_rank, enclosed=False)
+            line["batch"] = batch_record(2, 1, local_rank)
         if world == 1:
             try:
                 res = cpu_raycast(sc, 2, 1, None)
@@ -652,47 +656,58 @@ def nrc_record(gt_spp, device, enclosed=False, max_seconds=60.0):
             "cache_stats": {k: (round(v, 4) if isinstance(v, float) else v) for k, v in res.cache_stats.items()}}
 
 
-def run_batch(args, rank, world):
+def batch_record(steps, warmup, device=0):
     """64 independent rooms (extra triangles log-uniform in [1e3, 2e6], film
     256..1024 square, 1..64 spp, depth 8 with Russian roulette from segment 3)
-    rendered as one CUDA-graph launch per frame after autotuning."""
-    if rank != 0:
-        return 0
+    rendered as one CUDA-graph launch per frame after autotuning; device time
+    of the graph launch (CUDA events)."""
     from raycer_gb300 import scenes
     from raycer_gb300.batch import Batch
 
     scs = scenes.batch_scenes(seed=3)
     t0 = time.perf_counter()
-    b = Batch(0)
+    b = Batch(device)
     for i, sc in enumerate(scs):
         b.add_scene(sc, seed=3000 + i)
     setup_s = time.perf_counter() - t0
     tuning = b.autotune(budget_ms=4000.0)
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         b.render()
     ms, rays, done = [], [], []
-    for _ in range(args.steps):
+    for _ in range(steps):
         d = b.render()
         s = b.stats()
         ms.append(s["last_ms"])
         rays.append(s["rays_traced"])
         done.append(d)
     done = np.concatenate(done)
-    line = {
-        "metric": METRIC, "value": round(sum(rays) / (sum(ms) / 1e3) / 1e6, 2), "unit": METRIC,
-        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(statistics.mean(ms), 3),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (64 seeded rooms)",
-        "config": {"workload": "batched path tracing: 64 rooms + log-uniform[1e3, 2e6] extra tris, 256^2..1024^2, "
-                               "1..64 spp, depth 8, Russian roulette from segment 3, one CUDA-graph launch",
-                   "triangles": int(sum(sc.triangle_count for sc in scs)), "paths_per_step": int(s["paths"]),
-                   "rays_per_step": int(statistics.mean(rays)), "passes": s["passes"],
-                   "graph_nodes": s["graph_nodes"], "setup_s": round(setup_s, 1)},
+    out = {
+        "workload": "batched path tracing: 64 rooms + log-uniform[1e3, 2e6] extra tris, 256^2..1024^2, "
+                    "1..64 spp, depth 8, Russian roulette from segment 3, one CUDA-graph launch per frame",
+        "steps": steps, "warmup": warmup, "mrays_per_s": round(sum(rays) / (sum(ms) / 1e3) / 1e6, 2),
+        "ms_per_frame": round(statistics.mean(ms), 3),
+        "triangles": int(sum(sc.triangle_count for sc in scs)), "paths_per_frame": int(s["paths"]),
+        "rays_per_frame": int(statistics.mean(rays)), "passes": s["passes"], "graph_nodes": s["graph_nodes"],
+        "setup_s": round(setup_s, 1),
         "per_scene_latency_ms": {"p50": round(float(np.percentile(done, 50)), 3),
                                  "p99": round(float(np.percentile(done, 99)), 3)},
         "tuning": {k: tuning[k] for k in ("slots", "extend_block", "measured_paths_per_ms")},
     }
     b.close()
+    return out
+
+
+def run_batch(args, rank, world):
+    """The batch workload on its own (batch_record), one JSON line."""
+    if rank != 0:
+        return 0
+    r = batch_record(args.steps, args.warmup)
+    line = {"metric": METRIC, "value": r["mrays_per_s"], "unit": METRIC, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": r["ms_per_frame"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (64 seeded rooms)",
+            "config": {k: r[k] for k in ("workload", "triangles", "paths_per_frame", "rays_per_frame", "passes",
+                                         "graph_nodes", "setup_s")},
+            "per_scene_latency_ms": r["per_scene_latency_ms"], "tuning": r["tuning"]}
     print(json.dumps(line))
     return 0
 
