@@ -82,7 +82,7 @@ def parse_args():
                     help="raycast: the 1080p heightfield frame (default); batch: 64 rooms in one graph launch; "
                          "nrc: time to display RMSE 0.01, radiance cache vs plain path tracing")
     ap.add_argument("--enclosed", action="store_true",
-                    help="nrc workload: the same geometry inside a closed box lit by an emissive panel, no sky")
+                    help="nrc / large workloads: the geometry inside a closed box lit by an emissive panel, no sky")
     ap.add_argument("--gt-spp", type=int, default=4096, help="nrc / large: ground-truth samples per pixel")
     ap.add_argument("--scale", type=float, default=1.0, help="nrc: film scale (1 = 1920x1080)")
     ap.add_argument("--terminate-segment", type=int, default=2,
@@ -875,12 +875,25 @@ def run_build(args, rank, world):
 def run_large(args, rank, world):
     """The combined run: 3840x2160, depth 16, a 4,188,162-triangle fBm
     heightfield (seed 5) + 800 instances of a 20,480-triangle blob (30 %
-    dielectric, IOR U(1.3, 1.7)), sky-lit. Plain path tracing for 256 frames
-    of 1 spp, then the radiance-cache tracer until its display RMSE against a
-    float64 ground truth (1,024 spp: 64 frames of 16 paths per pixel) reaches
-    the plain run's; times are the renders' wall clock."""
+    dielectric, IOR U(1.3, 1.7)), lit by a uniform sky or (--enclosed) by the
+    radiance-cache workload's closed box and ceiling panel. Plain path tracing
+    for 256 frames of 1 spp, then the radiance-cache tracer until its display
+    RMSE against a float64 ground truth of --gt-spp samples per pixel
+    (rendered 16 per frame) reaches the plain run's; times are the renders'
+    wall clock.
+
+    CPU arm: the reference's path tracer has no dielectrics, so the float64
+    port traces the same geometry with every material Lambertian (the
+    dielectric blobs take their albedo), flattened, from its own BVH, at a
+    reduced 480x270 sample of the frame on all host cores; its Mrays/s times
+    the rays the plain GPU tracer traced to reach its RMSE estimate the CPU's
+    time to the same error (linear in pixels x samples, as the Mrays/s of the
+    sample)."""
     if rank != 0:
         return 0
+    import dataclasses
+
+    import oracle
     from raycer_gb300 import scenes
     from raycer_gb300.nrc import GroundTruth, RadianceCache
     from raycer_gb300.nrc_eval import _run
@@ -889,7 +902,7 @@ def run_large(args, rank, world):
     w, h = int(round(3840 * args.scale)), int(round(2160 * args.scale))
     t0 = time.perf_counter()
     sc = scenes.heightfield_blobs_instanced(instances=800, blob_level=5, seed=5, hf_nx=2048, hf_nz=1024, width=w,
-                                            height=h, dielectric_fraction=0.3, hf_seed=5)
+                                            height=h, dielectric_fraction=0.3, hf_seed=5, enclosed=args.enclosed)
     sc.settings.update(max_path_length=16)
     gen_s = time.perf_counter() - t0
     log = lambda m: print(m, file=sys.stderr, flush=True)
@@ -915,6 +928,7 @@ def run_large(args, rank, world):
         cached = _run(t, st, gt, plain.rmse, 1024, 180.0, 4)
         log(f"cache: {cached.frames} frames, {cached.seconds:.2f} s, rmse {cached.rmse:.4f}")
         stats = cache.stats()
+    lighting = "closed box, 20 x 11 ceiling panel of radiance 3" if args.enclosed else "sky-lit"
     line = {
         "metric": "Mrays/s", "value": round(plain.rays / plain.seconds / 1e6, 1), "unit": "Mrays/s",
         "n_gpus": 1, "steps": plain.frames, "warmup": 0,
@@ -922,20 +936,40 @@ def run_large(args, rank, world):
         "vs_baseline": None, "dtype": "f32 (paths) / bf16 (cache MLP)",
         "data": "synthetic (seeded heightfield + blob instances)",
         "config": {"workload": f"combined run: {w}x{h}, depth 16, heightfield 4,188,162 tris + 800 x 20,480-tri "
-                               f"blob instances ({sc.triangle_count} flattened), 30 % dielectric, sky-lit",
+                               f"blob instances ({sc.triangle_count} flattened), 30 % dielectric, {lighting}",
                    "scene_generation_s": round(gen_s, 1), "upload_and_build_ms": round(upload_ms, 1),
                    "gt_spp": args.gt_spp, "gt_seconds": round(gt_s, 1)},
         "plain_256spp": {"seconds": round(plain.seconds, 3), "rmse": round(plain.rmse, 5),
-                         "mrays_per_s": round(plain.rays / plain.seconds / 1e6, 1)},
+                         "mrays_per_s": round(plain.rays / plain.seconds / 1e6, 1), "rays": int(plain.rays)},
         "cache_equal_rmse": {"frames": cached.frames, "seconds": round(cached.seconds, 3),
                              "rmse": round(cached.rmse, 5), "reached": cached.reached,
                              "mrays_per_s": round(cached.rays / max(cached.seconds, 1e-9) / 1e6, 1)},
         "time_ratio_cache_over_plain": round(cached.seconds / plain.seconds, 3) if cached.reached else None,
         "cache_stats": {k: (round(v, 4) if isinstance(v, float) else v) for k, v in stats.items()},
-        "cpu_baseline": None,
-        "cpu_baseline_note": "the reference's CPU path tracer has no dielectrics and its instancing is host-only; "
-                             "the CPU comparison is the RAY-frame workload's",
     }
+    # CPU arm (see the docstring): the Lambertian version, flattened, 480x270 sample
+    try:
+        flat = sc.flatten()
+        flat.materials = [dataclasses.replace(m, dielectric=False, ior=0.0) for m in flat.materials]
+        cw, ch = 480, 270
+        flat.width, flat.height = cw, ch
+        threads = cpu_threads()
+        tb = time.perf_counter()
+        orc = oracle.Oracle(flat)
+        build_s = time.perf_counter() - tb
+        _, rays, sec = orc.render_path64(oracle.camera64_of(flat), cw, cw * ch, 16, 1, 1, seed=1, threads=threads)
+        cpu = rays / sec / 1e6
+        line["cpu_baseline"] = {
+            "value": round(cpu, 3), "unit": "Mrays/s", "cores": threads, "kind": "port",
+            "sample": f"{cw}x{ch}, 1 spp, depth 16, every material Lambertian ({rays} rays in {sec:.1f} s; "
+                      f"BVH build of {flat.triangle_count} flattened triangles {build_s:.0f} s, untimed)",
+            "equal_rmse_seconds_estimate": round(plain.rays / (cpu * 1e6), 1),
+            "note": "the reference's path tracer has no dielectrics; its time to the plain GPU tracer's RMSE "
+                    "is estimated as the rays the plain GPU tracer traced / the CPU's Mrays/s"}
+        line["time_ratio_cache_over_cpu"] = round(cached.seconds / line["cpu_baseline"]["equal_rmse_seconds_estimate"],
+                                                  5) if cached.reached else None
+    except (ImportError, MemoryError) as e:
+        line["cpu_baseline"] = {"value": None, "sample": f"unavailable: {e}"}
     print(json.dumps(line))
     return 0
 

@@ -418,6 +418,33 @@ def _random_rotations(rng, count):
     return R
 
 
+def _enclosing_box(panel, panel_radiance):
+    """The closed box around the heightfield scenes (x -14..14, y -1..8, z
+    -8..14, inward-facing walls of albedo 0.75) and an emissive panel
+    (width x depth, centred) facing down just under the ceiling: triangles
+    (12 + 2, float32-exact) with material indices 0 (walls) and 1 (panel),
+    and those two materials."""
+    x0, x1, y0, y1, z0, z1 = -14.0, 14.0, -1.0, 8.0, -8.0, 14.0
+    # (p0, u, v) with u x v pointing into the box, as room_scene's walls
+    dx, dy, dz = x1 - x0, y1 - y0, z1 - z0
+    walls = np.concatenate([
+        _quad((x0, y0, z0), (0, 0, dz), (dx, 0, 0)),   # floor, +y
+        _quad((x0, y1, z0), (dx, 0, 0), (0, 0, dz)),   # ceiling, -y
+        _quad((x0, y0, z0), (dx, 0, 0), (0, dy, 0)),   # back, +z
+        _quad((x0, y0, z1), (0, dy, 0), (dx, 0, 0)),   # front (behind the camera), -z
+        _quad((x0, y0, z0), (0, dy, 0), (0, 0, dz)),   # left, +x
+        _quad((x1, y0, z0), (0, 0, dz), (0, dy, 0)),   # right, -x
+    ])
+    pw, pd = float(panel[0]), float(panel[1])
+    quad = np.array(_quad((-0.5 * pw, y1 - 0.01, -0.5 * pd), (pw, 0, 0), (0, 0, pd)))  # facing down, -y
+    le = float(panel_radiance)
+    mats = [Material(diffuse=(0.75, 0.75, 0.75)),
+            Material(diffuse=(0.0, 0.0, 0.0), emittance=(le, le, le), is_emissive=True)]
+    verts = np.concatenate([_f32(walls), _f32(quad)])
+    midx = np.concatenate([np.zeros(walls.shape[0], np.uint32), np.ones(quad.shape[0], np.uint32)])
+    return (verts, midx), mats
+
+
 def heightfield_blobs_scene(instances: int = 200, blob_level: int = 5, seed: int = 4, hf_nx: int = 1024,
                             hf_nz: int = 512, width: int = 1920, height: int = 1080,
                             sky=(1.0, 1.0, 1.0), enclosed: bool = False, panel=(20.0, 11.0),
@@ -455,26 +482,11 @@ def heightfield_blobs_scene(instances: int = 200, blob_level: int = 5, seed: int
     verts = np.concatenate([hf.vertices, bv])
     name = f"heightfield + {instances} blobs x {blob.shape[0]} tris"
     if enclosed:
-        x0, x1, y0, y1, z0, z1 = -14.0, 14.0, -1.0, 8.0, -8.0, 14.0
-        # (p0, u, v) with u x v pointing into the box, as room_scene's walls
-        dx, dy, dz = x1 - x0, y1 - y0, z1 - z0
-        walls = np.concatenate([
-            _quad((x0, y0, z0), (0, 0, dz), (dx, 0, 0)),   # floor, +y
-            _quad((x0, y1, z0), (dx, 0, 0), (0, 0, dz)),   # ceiling, -y
-            _quad((x0, y0, z0), (dx, 0, 0), (0, dy, 0)),   # back, +z
-            _quad((x0, y0, z1), (0, dy, 0), (dx, 0, 0)),   # front (behind the camera), -z
-            _quad((x0, y0, z0), (0, dy, 0), (0, 0, dz)),   # left, +x
-            _quad((x1, y0, z0), (0, 0, dz), (0, dy, 0)),   # right, -x
-        ])
-        pw, pd = float(panel[0]), float(panel[1])
-        panel = np.array(_quad((-0.5 * pw, y1 - 0.01, -0.5 * pd), (pw, 0, 0), (0, 0, pd)))  # facing down, -y
-        le = float(panel_radiance)
-        mats = mats + [Material(diffuse=(0.75, 0.75, 0.75)),
-                       Material(diffuse=(0.0, 0.0, 0.0), emittance=(le, le, le), is_emissive=True)]
-        wall_id, light_id = len(mats) - 2, len(mats) - 1
-        verts = np.concatenate([verts, _f32(walls), _f32(panel)])
-        midx = np.concatenate([midx, np.full(walls.shape[0], wall_id, np.uint32),
-                               np.full(panel.shape[0], light_id, np.uint32)])
+        (bv, bm), box_mats = _enclosing_box(panel, panel_radiance)
+        first = len(mats)
+        mats = mats + box_mats
+        verts = np.concatenate([verts, bv])
+        midx = np.concatenate([midx, bm + np.uint32(first)])
         name += ", enclosed, emissive panel"
     return SceneDesc(
         name=name,
@@ -570,12 +582,16 @@ def instance_matrix(mesh_vertices: np.ndarray, inst: InstanceDesc) -> np.ndarray
 
 def heightfield_blobs_instanced(instances: int = 200, blob_level: int = 5, seed: int = 4, hf_nx: int = 1024,
                                 hf_nz: int = 512, width: int = 1920, height: int = 1080, sky=(1.0, 1.0, 1.0),
-                                dielectric_fraction: float = 0.0, hf_seed: int = 2) -> InstancedScene:
+                                dielectric_fraction: float = 0.0, hf_seed: int = 2,
+                                enclosed: bool = False, panel=(20.0, 11.0),
+                                panel_radiance: float = 3.0) -> InstancedScene:
     """The heightfield (an identity instance of its own mesh) plus `instances`
     placed copies of one random blob: uniform positions over the terrain,
     Euler rotations U(0, 360)^3, uniform scale U(0.25, 0.6), each copy its
     own material (albedo U(0.1, 0.9)^3; a fraction of them dielectric with
-    IOR U(1.3, 1.7))."""
+    IOR U(1.3, 1.7)). Lit by a uniform sky, or (enclosed=True) by
+    heightfield_blobs_scene's closed box and emissive ceiling panel, a third
+    mesh with an identity instance."""
     hf = heightfield_scene(seed=hf_seed, nx=hf_nx, nz=hf_nz, width=width, height=height)
     blob = blob_mesh(seed=seed, level=blob_level)
     rng = np.random.Generator(np.random.PCG64(seed))
@@ -600,10 +616,17 @@ def heightfield_blobs_instanced(instances: int = 200, blob_level: int = 5, seed:
         insts.append(InstanceDesc(mesh=1, material=k + 1, scale=(float(scale[k]),) * 3,
                                   rotate=tuple(float(x) for x in rot[k]),
                                   translate=(float(px[k] - c[0]), float(py[k] - c[1]), float(pz[k] - c[2]))))
+    meshes = [(hf.vertices, hf.material_index), (blob, np.zeros(blob.shape[0], np.uint32))]
+    name = f"heightfield + {instances} blob instances"
+    if enclosed:
+        box, box_mats = _enclosing_box(panel, panel_radiance)
+        first = len(mats)
+        mats = mats + box_mats
+        meshes.append((box[0], box[1] + np.uint32(first)))
+        insts.append(InstanceDesc(mesh=2))
+        name += ", enclosed, emissive panel"
     return InstancedScene(
-        name=f"heightfield + {instances} blob instances",
-        meshes=[(hf.vertices, hf.material_index), (blob, np.zeros(blob.shape[0], np.uint32))],
-        instances=insts, materials=mats, camera=hf.camera, width=width, height=height,
+        name=name, meshes=meshes, instances=insts, materials=mats, camera=hf.camera, width=width, height=height,
         light_direction=None, max_leaf_size=4,
         settings=dict(tracer="path", max_path_length=12, multi_sample_count_sqrt=1, path_sample_count=1,
-                      sampler="cmj", miss_radiance=tuple(sky)))
+                      sampler="cmj", miss_radiance=None if enclosed else tuple(sky)))
