@@ -47,3 +47,27 @@ def test_heightfield_layout():
     assert 0.0 <= y.min() and y.max() <= 1.5 * (1 + 0.5 + 0.25 + 0.125 + 0.0625 + 0.03125)
     ld = np.array(s.light_direction)
     assert np.allclose(-ld, np.array([0.3, 1.0, 0.2]) / np.linalg.norm([0.3, 1.0, 0.2]))
+
+
+def test_enclosed_box_in_both_scene_forms():
+    """The closed box and its ceiling panel: 12 wall triangles facing inward
+    and 2 emissive panel triangles facing down, the same in the flat
+    radiance-cache scene and as the identity-instanced third mesh of the
+    combined-run scene."""
+    import numpy as np
+
+    from raycer_gb300 import scenes
+
+    flat = scenes.heightfield_blobs_scene(instances=2, blob_level=1, hf_nx=8, hf_nz=4, enclosed=True)
+    inst = scenes.heightfield_blobs_instanced(instances=2, blob_level=1, hf_nx=8, hf_nz=4, enclosed=True)
+    for sc in (flat, inst.flatten()):
+        v = sc.vertices[-14:].reshape(-1, 3, 3)
+        mats = [sc.materials[i] for i in sc.material_index[-14:]]
+        assert [m.is_emissive for m in mats] == [False] * 12 + [True] * 2
+        n = np.cross(v[:, 1] - v[:, 0], v[:, 2] - v[:, 0])
+        centre = v.mean(axis=1)
+        inward = np.einsum("ij,ij->i", n[:12], np.array([0.0, 3.5, 3.0]) - centre[:12])
+        assert (inward > 0).all()
+        assert (n[12:, 1] < 0).all()          # the panel faces the floor
+        assert sc.settings["miss_radiance"] is None
+    assert inst.instances[-1].mesh == 2 and inst.instances[-1].material == -1
