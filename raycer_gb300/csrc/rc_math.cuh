@@ -115,6 +115,38 @@ __device__ __forceinline__ bool slab_finite(const RayF& r, float lox, float hix,
     return !(tmax < entry);
 }
 
+// The same test for a ray whose inverse direction is finite with the signs
+// of octant OCT (bit k set: component k negative). (lo - o) and (hi - o)
+// are ordered like lo and hi (rounding is monotone), and multiplying by a
+// positive inverse keeps that order and by a negative one reverses it, so
+// the near and far plane distances of each axis are known without a
+// min/max: the values slab_finite's min/max pick, up to the sign of a zero
+// (which no comparison sees). Six FMNMX fewer per box.
+template <int OCT>
+__device__ __forceinline__ bool slab_oct(const RayF& r, float lox, float hix, float loy, float hiy, float loz,
+                                         float hiz, float& entry)
+{
+    const float nx = __fmul_rn(__fsub_rn((OCT & 1) ? hix : lox, r.o.x), r.inv.x);
+    const float fx = __fmul_rn(__fsub_rn((OCT & 1) ? lox : hix, r.o.x), r.inv.x);
+    const float ny = __fmul_rn(__fsub_rn((OCT & 2) ? hiy : loy, r.o.y), r.inv.y);
+    const float fy = __fmul_rn(__fsub_rn((OCT & 2) ? loy : hiy, r.o.y), r.inv.y);
+    const float nz = __fmul_rn(__fsub_rn((OCT & 4) ? hiz : loz, r.o.z), r.inv.z);
+    const float fz = __fmul_rn(__fsub_rn((OCT & 4) ? loz : hiz, r.o.z), r.inv.z);
+    const float tmin = fmaxf(fmaxf(nx, ny), nz);
+    const float tmax = fminf(fminf(fx, fy), fz);
+    entry = fmaxf(tmin, 0.0f);
+    return !(tmax < entry);
+}
+
+// Sign octant of a ray's inverse direction (slab_oct's OCT), or -1 when a
+// component is not finite (slab_oct does not apply).
+__device__ __forceinline__ int ray_octant(const RayF& r)
+{
+    if (!r.finite)
+        return -1;
+    return (r.inv.x < 0.0f ? 1 : 0) | (r.inv.y < 0.0f ? 2 : 0) | (r.inv.z < 0.0f ? 4 : 0);
+}
+
 // Möller–Trumbore of intersectTriangle (intersections.cl:27-69 /
 // Triangle.cpp:51-93) up to the distance window; the caller applies the
 // closest-hit comparison. Returns true with t, u, v on a hit.

@@ -11,6 +11,7 @@
 // carry no missed pixels.
 
 #include <cfloat>
+#include <cmath>
 
 #include "kernels.h"
 #include <cstdlib>
@@ -135,7 +136,10 @@ __device__ __forceinline__ RayF primary_ray(const DevCamera& cam, const rc_ray* 
 // arithmetic of stage 2 below (origin = o + t d, then + L * rayStartOffset;
 // the hit's own triangle, of its instance, skipped). Completes the record:
 // occluder and flags.
-template <bool INST, bool SL>
+// SOCT >= 0: the light's direction has the signs of octant SOCT (the host
+// checked that its inverse is finite), and the walk's box tests use them
+// (slab_oct: the same decisions, six FMNMX fewer per box).
+template <bool INST, bool SL, int SOCT = -1>
 __device__ __forceinline__ void shadow_of(const DevScene& sc, const RayF& ray, const HitF& h, float3 L,
                                           float rayStartOffset, int4& o, TravCount& cnt, int& err)
 {
@@ -148,7 +152,7 @@ __device__ __forceinline__ void shadow_of(const DevScene& sc, const RayF& ray, c
     else if (SL)
         occ = traverse_stackless<true>(sc, sr, s, h.slot);
     else
-        occ = traverse<true, ORDER_REF, false>(sc, sr, s, cnt, err, h.slot);
+        occ = traverse<true, ORDER_REF, false, SOCT>(sc, sr, s, cnt, err, h.slot);
     o.z = occ ? caller_index(sc, s.slot) + (INST ? __ldg(&sc.instances[s.inst].primBase) : 0) : -1;
     o.w = 1 | 2 | (occ ? 4 : 0);
 }
@@ -170,7 +174,7 @@ __device__ __forceinline__ void shadow_of(const DevScene& sc, const RayF& ray, c
 // pixels all hit (or all miss) keep the warp full (or cost nothing); only
 // tiles on a silhouette leave lanes idle. With the caller's rays in host
 // memory the shadow work then overlaps the ray reads over the host link.
-template <int ORDER, bool COUNT, bool PACKET, bool INST, bool FUSED = false, bool SL = false>
+template <int ORDER, bool COUNT, bool PACKET, bool INST, bool FUSED = false, bool SL = false, int SOCT = -1>
 __global__ void __launch_bounds__(kBlock, FUSED ? RC_FUSED_MIN_BLOCKS : RC_TRACE_MIN_BLOCKS) k_raycast_primary(DevScene sc, DevCamera cam, const rc_ray* __restrict__ rays,
                                                             uint64_t pixelStart, int64_t count, int64_t width,
                                                             int64_t height, int64_t tilesX, int castShadow,
@@ -226,7 +230,7 @@ __global__ void __launch_bounds__(kBlock, FUSED ? RC_FUSED_MIN_BLOCKS : RC_TRACE
                 o.z = -1;
                 o.w = found ? 1 : 0;
                 if (valid && found)
-                    shadow_of<false, SL>(sc, ray, h, L, rayStartOffset, o, cnt1, err);
+                    shadow_of<false, SL, SOCT>(sc, ray, h, L, rayStartOffset, o, cnt1, err);
                 if (valid)
                 {
                     reinterpret_cast<int4*>(out)[i] = o;
@@ -272,7 +276,7 @@ __global__ void __launch_bounds__(kBlock, FUSED ? RC_FUSED_MIN_BLOCKS : RC_TRACE
             {
                 if (found)
                 {
-                    shadow_of<INST, SL>(sc, ray, h, L, rayStartOffset, o, cnt1, err);
+                    shadow_of<INST, SL, INST ? -1 : SOCT>(sc, ray, h, L, rayStartOffset, o, cnt1, err);
                     done1++;
                 }
             }
@@ -414,6 +418,40 @@ bool whole_frame(uint64_t pixelStart, int64_t count, int64_t width)
 }
 
 
+// Sign octant of the shadow rays' direction L for slab_oct (bit k: component
+// k negative), or -1 where a component is zero, not finite or too small for
+// its reciprocal to be finite (the general box test then applies).
+int light_octant(float3 L)
+{
+    const float c[3] = { L.x, L.y, L.z };
+    int oct = 0;
+    for (int k = 0; k < 3; ++k)
+    {
+        if (!std::isfinite(c[k]) || !(std::fabs(c[k]) > 1e-30f))
+            return -1;
+        if (c[k] < 0.0f)
+            oct |= 1 << k;
+    }
+    return oct;
+}
+
+#define RC_FUSED_ARGS li, sc, cam, rays, pixelStart, count, width, height, tilesX, castShadow, L, off, out, queue, ctl
+
+// The one-kernel RAY frame, its shadow walk specialised to the light's
+// octant SOCT (or general, -1).
+template <int ORDER, bool PACKET, bool INST, bool SL, int SOCT>
+cudaError_t launch_fused(const LaunchInfo& li, const DevScene& sc, const DevCamera& cam, const rc_ray* rays,
+                         uint64_t pixelStart, int64_t count, int64_t width, int64_t height, int64_t tilesX,
+                         int castShadow, float3 L, float off, rc_cast_pixel* out, int* queue, DevControl* ctl)
+{
+    auto kf = k_raycast_primary<ORDER, false, PACKET, INST, true, SL, SOCT>;
+    static OccupancyCache occF;
+    kf<<<persistent_blocks(kf, li.numSMs, occF), kBlock, 0, li.stream>>>(sc, cam, rays, pixelStart, count, width,
+                                                                         height, tilesX, castShadow, out, queue, ctl,
+                                                                         L, off, nullptr);
+    return cudaGetLastError();
+}
+
 template <int ORDER, bool COUNT, bool PACKET, bool INST, bool SL = false, bool FUSED = false>
 cudaError_t raycast_t(const LaunchInfo& li, const DevScene& sc, const DevCamera& cam, const rc_ray* rays,
                       uint64_t pixelStart, int64_t count, int64_t width, int castShadow, float3 L, float off,
@@ -426,12 +464,23 @@ cudaError_t raycast_t(const LaunchInfo& li, const DevScene& sc, const DevCamera&
     const int64_t tilesX = whole_frame(pixelStart, count, width) ? (width + 7) / 8 : 0;
     if (FUSED && castShadow)
     {
-        auto kf = k_raycast_primary<ORDER, false, PACKET, INST, true, SL>;
-        static OccupancyCache occF;
-        kf<<<persistent_blocks(kf, li.numSMs, occF), kBlock, 0, li.stream>>>(sc, cam, rays, pixelStart, count, width, height, tilesX, castShadow, out,
-                                         queue, ctl, L, off, nullptr);
         kernels = 1;
-        return cudaGetLastError();
+        if constexpr (!INST && !SL)
+        {
+            switch (light_octant(L))
+            {
+            case 0: return launch_fused<ORDER, PACKET, INST, SL, 0>(RC_FUSED_ARGS);
+            case 1: return launch_fused<ORDER, PACKET, INST, SL, 1>(RC_FUSED_ARGS);
+            case 2: return launch_fused<ORDER, PACKET, INST, SL, 2>(RC_FUSED_ARGS);
+            case 3: return launch_fused<ORDER, PACKET, INST, SL, 3>(RC_FUSED_ARGS);
+            case 4: return launch_fused<ORDER, PACKET, INST, SL, 4>(RC_FUSED_ARGS);
+            case 5: return launch_fused<ORDER, PACKET, INST, SL, 5>(RC_FUSED_ARGS);
+            case 6: return launch_fused<ORDER, PACKET, INST, SL, 6>(RC_FUSED_ARGS);
+            case 7: return launch_fused<ORDER, PACKET, INST, SL, 7>(RC_FUSED_ARGS);
+            default: break;
+            }
+        }
+        return launch_fused<ORDER, PACKET, INST, SL, -1>(RC_FUSED_ARGS);
     }
     auto kp = k_raycast_primary<ORDER, COUNT, PACKET, INST>;
     auto ks = k_raycast_shadow<COUNT, INST, SL>;

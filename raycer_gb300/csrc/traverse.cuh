@@ -71,7 +71,9 @@ __device__ __forceinline__ void load_node(const DevNode* __restrict__ nodes, int
 // Returns true if any triangle was accepted. `hit` must be initialised by
 // the caller (slot -1, t = FLT_MAX for a fresh query). `err` is set to 1 on
 // a stack overflow (the ray is then abandoned; the host reports it).
-template <bool ANY_HIT, int ORDER, bool COUNT>
+// OCT >= 0: the caller guarantees that the ray's inverse direction is finite
+// with those signs (ray_octant), and the box tests take slab_oct<OCT>.
+template <bool ANY_HIT, int ORDER, bool COUNT, int OCT = -1>
 __device__ __forceinline__ bool traverse(const DevScene& sc, const RayF& ray, HitF& hit, TravCount& cnt, int& err,
                                          int skip = -1)
 {
@@ -92,10 +94,15 @@ __device__ __forceinline__ bool traverse(const DevScene& sc, const RayF& ray, Hi
                 cnt.nodes++;
             float e0, e1;
             bool h0, h1;
+            if (OCT >= 0)
+            {
+                h0 = slab_oct<OCT < 0 ? 0 : OCT>(ray, a.x, a.y, a.z, a.w, c.x, c.y, e0);
+                h1 = slab_oct<OCT < 0 ? 0 : OCT>(ray, b.x, b.y, b.z, b.w, c.z, c.w, e1);
+            }
 #ifndef RC_EXACT_SLAB_ONLY
-            if (ray.finite)
+            else if (ray.finite)
 #else
-            if (false)
+            else if (false)
 #endif
             {
                 h0 = slab_finite(ray, a.x, a.y, a.z, a.w, c.x, c.y, e0);

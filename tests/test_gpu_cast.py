@@ -221,3 +221,27 @@ def test_cast_with_shadow_ray_lists():
         out = t.cast_with_shadow(np.ascontiguousarray(rays[perm]))
         assert np.array_equal(out, frame[perm])
     assert (frame["prim"] >= 0).any() and (frame["occluder"] >= 0).any()
+
+
+@pytest.mark.parametrize("light", [(sx * 0.4, sy * 1.0, sz * 0.3) for sx in (1, -1) for sy in (1, -1) for sz in (1, -1)]
+                         + [(0.0, -1.0, 0.3), (-0.5, 0.0, -0.2)])
+def test_raycast_frame_light_octants(light):
+    """The one-kernel frame's shadow walk is compiled per sign octant of the
+    light's direction (box tests with the near and far planes known); every
+    octant, and lights with a zero component (the general walk), give the
+    oracle's records bit for bit, in both orders."""
+    sc = small_heightfield(width=160, height=90)
+    sc.settings["tracer"] = "ray"
+    sc.light_direction = light
+    L = -np.array(sc.light_direction, np.float32)
+    cam = camera_floats(camera_record(sc))
+    with CudaTracer(0) as t:
+        t.initializeBuffers(sc)
+        t.initializeImageBuffers(sc.width, sc.height)
+        orc = oracle.Oracle(sc, prebuilt=t.get_bvh())
+        for order in (N.RC_ORDER_NEAREST, N.RC_ORDER_REFERENCE):
+            t.set_traversal_order(order)
+            t.run(TracerState(scene=sc, filmWidth=sc.width, filmHeight=sc.height, pixelCount=sc.width * sc.height))
+            gpu = t.read_cast().view(np.int32).reshape(-1, 4)
+            ref, _ = orc.raycast32(cam, sc.width, sc.width * sc.height, L, order=order)
+            assert np.array_equal(gpu, ref), f"{(gpu != ref).any(axis=1).sum()} pixels differ"
