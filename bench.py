@@ -619,7 +619,7 @@ def path_record(sc, workload, steps, warmup, device):
             c_sec += sec
         cpu = c_rays / c_sec / 1e6
         out["cpu_baseline"] = {"value": round(cpu, 3), "unit": METRIC, "cores": threads, "kind": "port",
-                               "sample": "full 1920x1080 frame, 1 warm-up + 2 timed frames",
+                               "sample": f"full {sc.width}x{sc.height} frame, 1 warm-up + 2 timed frames",
                                "bvh_build_s": round(build_s, 2)}
         out["device_over_cpu"] = round(dev_mrays / cpu, 1)
         out["e2e_over_cpu"] = round(out["e2e"]["value"] / cpu, 1)

@@ -206,3 +206,34 @@ def test_tensor_core_wait_gives_up_and_the_handle_recovers():
         ref = ref_cache.infer(q).astype(np.float64)
     rel = np.abs(got - ref) / np.abs(ref)
     assert np.quantile(rel, 0.99) < 1e-3 and rel.max() < 2e-2
+
+
+def test_stopped_cache_render_leaves_the_cache_untouched():
+    """A radiance-cache render whose budget runs out at once: the pass's later
+    kernels (lookups, training targets, the optimizer) find the stop bit and
+    do nothing, so the weights are those before the call, bit for bit, and
+    the film is empty; the next render trains as usual."""
+    sc = scenes.heightfield_blobs_scene(instances=12, blob_level=3, hf_nx=96, hf_nz=48, width=128, height=72,
+                                        enclosed=True)
+    n = sc.width * sc.height
+    with CudaTracer(0) as t:
+        t.initializeBuffers(sc, seed=2)
+        t.initializeImageBuffers(sc.width, sc.height)
+        st = TracerState(scene=sc, filmWidth=sc.width, filmHeight=sc.height, pixelCount=n)
+        cache = RadianceCache(t, seed=5)
+        for _ in range(3):
+            t.run(st)
+        before = cache.params.copy()
+        t.clear()
+        t.set_time_budget(0.0)
+        try:
+            with pytest.raises(RaycerError) as e:
+                t.run(st)
+        finally:
+            t.set_time_budget(None)
+        assert e.value.status == N.RC_TIMEOUT
+        assert np.array_equal(cache.params, before)
+        assert (t.read_film()[:, 3] == 0).all()
+        t.run(st)
+        assert not np.array_equal(cache.params, before)
+        assert (t.read_film()[:, 3] > 0).all()
