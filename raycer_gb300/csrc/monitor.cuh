@@ -93,8 +93,8 @@ static __device__ __noinline__ int poll_render(RenderMonitor* mon, unsigned long
 // The watch warp of a monitored persistent kernel (the last warp of block
 // 0): it takes no work; its lane 0 polls the cancel word and the time budget
 // and publishes progress, sleeping ~2 us between polls, until the queue head
-// reaches `items` (every item taken), a stop, or kWatchPolls polls (then it
-// just stops watching). The other warps' work loop carries no poll at all.
+// had reached `items` at a poll (every item taken), a stop, or kWatchPolls
+// polls (then it just stops watching). The other warps' work loop carries no poll at all.
 // publish: kPublishNone, kPublishProgress, or kPublishEstimate (the pixels of
 // the items taken before those the other warps may hold, at most `pixels`).
 constexpr unsigned kWatchPolls = 1u << 24;
@@ -109,8 +109,6 @@ static __device__ __forceinline__ void watch_queue(RenderMonitor* mon, unsigned 
     for (unsigned i = 0; i < kWatchPolls; ++i)
     {
         const unsigned long long h = *reinterpret_cast<const volatile unsigned*>(head);
-        if (h >= items)
-            return;
         unsigned long long pub = publish;
         if (publish == kPublishEstimate)
         {
@@ -118,7 +116,9 @@ static __device__ __forceinline__ void watch_queue(RenderMonitor* mon, unsigned 
             pub = item > workers ? (item - workers) * 32ull : 0ull;
             pub = pub < pixels ? pub : pixels;
         }
-        if (poll_render(mon, budgetNs, ctl, head, true, pub))
+        // polled once before the head is looked at: a kernel whose items
+        // were all taken at once is still checked (a budget of 0 stops it)
+        if (poll_render(mon, budgetNs, ctl, head, true, pub) || h >= items)
             return;
         __nanosleep(2000);
     }
