@@ -39,7 +39,8 @@ At N = 1 the line also carries the rest of the headline (unless
   nrc_sky   the same under a uniform sky instead of the box
   batch     64 rooms of uneven size in one CUDA-graph launch per frame
             (1 warm-up + 2 timed frames): aggregate Mrays/s, per-scene
-            latency p50 / p99
+            latency p50 / p99, and the float64 port's rate on every 8th
+            scene of the batch (one after another, as the reference renders)
 
 `--impl reference` times the reference's CPU ray casting on this host's cores
 (the reference's own code where it was compiled, else the float64 port) on
@@ -656,11 +657,13 @@ def nrc_record(gt_spp, device, enclosed=False, max_seconds=60.0):
             "cache_stats": {k: (round(v, 4) if isinstance(v, float) else v) for k, v in res.cache_stats.items()}}
 
 
-def batch_record(steps, warmup, device=0):
+def batch_record(steps, warmup, device=0, cpu=True):
     """64 independent rooms (extra triangles log-uniform in [1e3, 2e6], film
     256..1024 square, 1..64 spp, depth 8 with Russian roulette from segment 3)
     rendered as one CUDA-graph launch per frame after autotuning; device time
-    of the graph launch (CUDA events)."""
+    of the graph launch (CUDA events). With `cpu`, the port's rate on a
+    sample of the scenes (batch_cpu_baseline) and the frame's estimated time
+    on the host cores at that rate."""
     from raycer_gb300 import scenes
     from raycer_gb300.batch import Batch
 
@@ -694,7 +697,58 @@ def batch_record(steps, warmup, device=0):
         "tuning": {k: tuning[k] for k in ("slots", "extend_block", "measured_paths_per_ms")},
     }
     b.close()
+    if cpu:
+        try:
+            res = batch_cpu_baseline(scs)
+            res["frame_seconds_estimate"] = round(out["rays_per_frame"] / (res["value"] * 1e6), 1)
+            out["cpu_baseline"] = res
+            out["device_over_cpu"] = round(out["mrays_per_s"] / res["value"], 1)
+        except ImportError as e:
+            out["cpu_baseline"] = {"value": None, "sample": f"unavailable: {e}"}
     return out
+
+
+def batch_cpu_baseline(scs, stride=8, pixels_per_scene=1 << 14):
+    """The batch on the host cores: the float64 port of the reference's path
+    tracer, one scene after another (as the reference renders them), on one
+    scene from each `stride`-scene band of the batch sorted by triangle count
+    (the middle one of the band: a sample with the batch's spread of sizes),
+    each from its own BVH (the port's restatement of FlatBVH::build, outside
+    the timing), over a band of
+    `pixels_per_scene` pixels (at least one of the port's 1000-pixel chunks
+    per thread: the reference's schedule(dynamic, 1000)) across the film's
+    middle rows, one sample per pixel, with the scene's maximum path length.
+    The rate is rays per second, which the samples per pixel do not change;
+    the reference's path tracer has no Russian roulette, so its paths run to
+    the maximum length."""
+    import oracle
+
+    threads = cpu_threads()
+    rays = sec = build_s = 0.0
+    pixels = 0
+    picked = sorted(scs, key=lambda sc: sc.triangle_count)[stride // 2::stride]
+    for i, sc in enumerate(picked):
+        depth = int(sc.settings.get("max_path_length", 8))
+        n = sc.width * sc.height
+        count = max(1, min(n, max(1000 * threads, pixels_per_scene)))
+        start = max(0, min(n - count, (sc.height // 2) * sc.width - count // 2))
+        t0 = time.perf_counter()
+        orc = oracle.Oracle(sc)
+        build_s += time.perf_counter() - t0
+        try:
+            _, r, s = orc.render_path64(oracle.camera64_of(sc), sc.width, count, depth, 1, 1, seed=7 + i,
+                                        threads=threads, pixel_start=start)
+        finally:
+            orc.close()
+        rays += r
+        sec += s
+        pixels += count
+    return {"value": round(rays / sec / 1e6, 3), "unit": METRIC, "cores": threads, "kind": "port",
+            "sample": f"{len(picked)} of the {len(scs)} scenes (the middle one of every {stride} by triangle count: "
+                      f"{', '.join(str(sc.triangle_count) for sc in picked)} tris), one after another, a band of "
+                      f"{pixels // len(picked)} pixels across each film's middle rows at 1 sample per pixel; "
+                      f"no Russian roulette", "rays": int(rays), "seconds": round(sec, 2),
+            "bvh_build_s": round(build_s, 1)}
 
 
 def run_batch(args, rank, world):
@@ -708,6 +762,8 @@ def run_batch(args, rank, world):
             "config": {k: r[k] for k in ("workload", "triangles", "paths_per_frame", "rays_per_frame", "passes",
                                          "graph_nodes", "setup_s")},
             "per_scene_latency_ms": r["per_scene_latency_ms"], "tuning": r["tuning"]}
+    if "cpu_baseline" in r:
+        line["cpu_baseline"] = r["cpu_baseline"]
     print(json.dumps(line))
     return 0
 

@@ -74,7 +74,7 @@ extern "C" rc_status rc_cast_with_shadow_device_noalloc(rc_tracer* h, const rc_r
     if (h->nInstances > 0)
         return fail(h, RC_UNSUPPORTED, "cast_with_shadow_device_noalloc: instanced scenes are traced by rc_cast "
                                        "and PATH renders only");
-    if (n <= 0 || !d_rays || !d_out)
+    if (n < 0 || (n > 0 && (!d_rays || !d_out)))
         return fail(h, RC_INVALID_ARG, "cast_with_shadow_device_noalloc: bad ray count or null buffer");
     if (n > kNoAllocMaxRays)
         return fail(h, RC_INVALID_ARG,
@@ -84,6 +84,8 @@ extern "C" rc_status rc_cast_with_shadow_device_noalloc(rc_tracer* h, const rc_r
         return fail(h, RC_INVALID_ARG, "cast_with_shadow_device_noalloc: buffers must be 16-byte aligned");
     if (order != RC_ORDER_REFERENCE && order != RC_ORDER_NEAREST)
         return fail(h, RC_INVALID_ARG, "cast_with_shadow_device_noalloc: invalid traversal order");
+    if (n == 0)
+        return RC_OK;  // an empty batch, as in rc_cast
 
     cudaError_t e = cudaSetDevice(h->device);
     void* scratch = nullptr;

@@ -1122,10 +1122,12 @@ rc_status rc_cast_with_shadow(rc_tracer* h, const rc_ray* rays, int64_t n, int32
         return RC_INVALID_ARG;
     if (!h->sceneReady)
         return fail(h, RC_NOT_READY, "cast_with_shadow: no scene uploaded");
-    if (n <= 0 || n > (int64_t(1) << 31) - 64 || !rays || !out)
+    if (n < 0 || n > (int64_t(1) << 31) - 64 || (n > 0 && (!rays || !out)))
         return fail(h, RC_INVALID_ARG, "cast_with_shadow: bad ray count or null buffer");
     if (order != RC_ORDER_REFERENCE && order != RC_ORDER_NEAREST)
         return fail(h, RC_INVALID_ARG, "cast_with_shadow: invalid traversal order");
+    if (n == 0)
+        return RC_OK;  // an empty batch, as in rc_cast
     cudaSetDevice(h->device);
     rc_status s = stackless_walk() ? ensure_ropes(h) : RC_OK;
     if (s != RC_OK)

@@ -31,3 +31,24 @@ def test_cpu_arm_never_loads_the_product_library():
     res = subprocess.run([sys.executable, "-c", PROBE.format(root=str(ROOT))], capture_output=True, text=True,
                          timeout=300)
     assert res.returncode == 0 and res.stdout.startswith("ok"), res.stdout + res.stderr
+
+
+BATCH_PROBE = r"""
+import sys
+sys.path.insert(0, {root!r})
+import bench
+from raycer_gb300 import _native, scenes
+scs = scenes.batch_scenes(seed=3, count=4, n_max=2e3, resolutions=(64,), spps=(1, 4))
+res = bench.batch_cpu_baseline(scs, stride=2, pixels_per_scene=256)
+assert res["kind"] == "port" and res["value"] > 0 and res["rays"] >= 2 * 256, res
+sizes = sorted(sc.triangle_count for sc in scs)
+assert "%d, %d tris" % (sizes[1], sizes[3]) in res["sample"], res["sample"]
+assert _native._lib is None, "the product library was loaded"
+print("ok", res["value"])
+"""
+
+
+def test_batch_cpu_baseline_samples_the_batch_by_size_with_the_port():
+    res = subprocess.run([sys.executable, "-c", BATCH_PROBE.format(root=str(ROOT))], capture_output=True, text=True,
+                         timeout=300)
+    assert res.returncode == 0 and res.stdout.startswith("ok"), res.stdout + res.stderr
