@@ -212,7 +212,9 @@ typedef struct rc_stats
      * that traces both and 1 = 0.0. (The in-place rc_cast_with_shadow
      * leaves both times 0.0.) PATH render: 0 = the extend (closest-hit)
      * kernels of all segments, 1 = everything else (generate, shade,
-     * accumulate). cast: 0 = the cast kernel. */
+     * accumulate); where a segment's extend and shade run as one kernel
+     * (plain passes over the 4-wide tree), 0 includes the shading. cast:
+     * 0 = the cast kernel. */
     uint64_t stage_rays[2];
     uint64_t stage_nodes[2];   /* when counting is on */
     uint64_t stage_tris[2];    /* when counting is on */
@@ -368,7 +370,8 @@ rc_status rc_read_cast(rc_tracer* h, rc_cast_pixel* out);
  * PathTracer::traceRecursive (PathTracer.cpp:36-40) and
  * Raytracer::calculateShadowAmount (Raytracer.cpp:497-522), batched.
  * any_hit != 0: shadow-ray semantics (isShadowRay + fastOcclusion:
- * nonShadowing triangles skipped, first hit found is reported).           */
+ * nonShadowing triangles skipped, first hit found is reported).
+ * n = 0 is an empty batch in every form: RC_OK, nothing read or written.  */
 
 /* Host buffers: rays -> hits, copies included. */
 rc_status rc_cast(rc_tracer* h, const rc_ray* rays, int64_t n, int32_t any_hit, int32_t order, rc_hit* hits);

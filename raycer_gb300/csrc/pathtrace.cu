@@ -486,6 +486,183 @@ __device__ __forceinline__ void nrc_end(const NrcPass& n, uint32_t g, float r, f
 // NRC: training paths record every vertex (query + bounce factor) and their
 // terminal radiance; other paths end at the hit of segment termSegment with
 // a cache lookup (res gets thr * cache after the last segment).
+// The shade stage for one queued slot whose extend found hit h (slot, t as
+// bits, u, v; x < 0: a miss): the miss, emitter, cache-lookup, bounce and
+// depth-limit cases above. Returns whether the path goes on (the slot joins
+// the next segment's queue); a cache lookup sets `lookup` and `lrec`. With
+// OD the caller passes the slot's ray (o, d) it already holds, else they are
+// read from the path state.
+template <bool NRC, bool OD>
+__device__ __forceinline__ bool shade_slot(const PassParams& p, int segment, int s, int4 h, float4 o, float4 d,
+                                           bool& lookup, NrcRecord& lrec)
+{
+    bool cont = false;
+    const PathChunk& ch = p.chunks[p.chunkOf[s]];
+    const PathScene& scn = p.scenes[ch.scene];
+    const bool train = NRC && nrc_training(p.nrc, uint32_t(s));
+    const uint32_t g = NRC ? uint32_t(s) / uint32_t(max(p.nrc.trainStride, 1)) : 0u;
+    if (h.x < 0)
+    {
+        if (scn.skyOn)
+        {
+            // GPU extension: misses see a constant sky radiance.
+            float4 thr = p.thr[s];
+            float4 r = p.res[s];
+            r.x = __fmul_rn(thr.x, scn.sky[0]);
+            r.y = __fmul_rn(thr.y, scn.sky[1]);
+            r.z = __fmul_rn(thr.z, scn.sky[2]);
+            p.res[s] = r;
+        }
+        if (train)
+        {
+            const float on = scn.skyOn ? 1.0f : 0.0f;
+            nrc_end(p.nrc, g, on * scn.sky[0], on * scn.sky[1], on * scn.sky[2], uint32_t(segment));
+        }
+    }
+    else
+    {
+        const DevScene sc = scn.sc;
+        const float4* tp = reinterpret_cast<const float4*>(sc.tris + h.x);
+        float4 tc = __ldg(tp + 2);
+        uint32_t mi = __float_as_uint(tc.y) & kMetaMaterialMask;
+        const int inst = sc.numInstances > 0 ? h.w : -1;
+        DevInstance in{};
+        if (inst >= 0)
+        {
+            in = load_instance(sc.instances, inst);
+            if (in.material >= 0)
+                mi = uint32_t(in.material);  // Instance::changePrimitive (Instance.cpp:93)
+        }
+        float4 md = __ldg(&sc.mats[mi].diffuse);
+        float4 me = __ldg(&sc.mats[mi].emittance);
+        uint32_t mflags = __float_as_uint(me.w);
+        const bool dielectric = (mflags & kMatDielectric) != 0;
+        float4 thr = p.thr[s];
+        if (mflags & kMatEmissive)
+        {
+            // sampleColor *= emittance (pathtrace.cl:44-51)
+            float4 r = p.res[s];
+            r.x = __fmul_rn(thr.x, me.x);
+            r.y = __fmul_rn(thr.y, me.y);
+            r.z = __fmul_rn(thr.z, me.z);
+            p.res[s] = r;
+            if (train)
+                nrc_end(p.nrc, g, me.x, me.y, me.z, uint32_t(segment));
+        }
+        else if (NRC && !train && !dielectric && segment >= p.nrc.termSegment)
+        {
+            const ShadeFrame fr = shade_frame(sc, h.x, inst >= 0 ? &in : nullptr, mflags);
+            o = OD ? o : p.o[s];
+            d = OD ? d : p.d[s];
+            V3 ip = vfma(v3(d.x, d.y, d.z), __int_as_float(h.y), v3(o.x, o.y, o.z));
+            lrec = nrc_record(ip, d, fr.n, md, 0.0f, 0.0f, 0.0f, __int_as_float(s));
+            lookup = true;
+        }
+        else if (segment + 1 < scn.maxPathLength)
+        {
+            SlotInfo si = slot_info(ch, scn, uint32_t(s));
+            uint32_t key = stream_key(scn.seed, scn.frame, si.pixelGlobal, si.sample);
+            bool alive = true;
+            float qs = 1.0f;
+            if (scn.rrDepth > 0 && segment + 1 >= scn.rrDepth)
+            {
+                float m = fmaxf(thr.x, fmaxf(thr.y, thr.z));
+                qs = fminf(m, 1.0f);
+                float xi = stream_float(key, kCounterRoulette + uint32_t(segment));
+                if (!(xi < qs))
+                    alive = false;
+                else
+                {
+                    thr.x = __fdiv_rn(thr.x, qs);
+                    thr.y = __fdiv_rn(thr.y, qs);
+                    thr.z = __fdiv_rn(thr.z, qs);
+                }
+            }
+            const ShadeFrame frm = shade_frame(sc, h.x, inst >= 0 ? &in : nullptr, mflags);
+            const V3 nrm = frm.n;
+            o = OD ? o : p.o[s];
+            d = OD ? d : p.d[s];
+            float t = __int_as_float(h.y);
+            V3 ip = vfma(v3(d.x, d.y, d.z), t, v3(o.x, o.y, o.z));
+            if (alive)
+            {
+                float xr = stream_float(key, kCounterBounce + 2u * uint32_t(segment));
+                float yr = stream_float(key, kCounterBounce + 2u * uint32_t(segment) + 1u);
+                V3 dir;
+                float fr, fg, fb;
+                if (dielectric)
+                {
+                    dir = dielectric_bounce(v3(d.x, d.y, d.z), nrm, md.w, xr);
+                    fr = fg = fb = 1.0f;
+                }
+                else
+                {
+                    dir = hemisphere_cosine(frm.t, frm.b, nrm, xr, yr);
+                    float alpha = fabsf(vdot(dir, nrm));
+                    // brdf = 2 * reflectance * alpha (PathTracer.cpp:70-71)
+                    fr = __fmul_rn(__fmul_rn(2.0f, md.x), alpha);
+                    fg = __fmul_rn(__fmul_rn(2.0f, md.y), alpha);
+                    fb = __fmul_rn(__fmul_rn(2.0f, md.z), alpha);
+                    thr.x = __fmul_rn(thr.x, fr);
+                    thr.y = __fmul_rn(thr.y, fg);
+                    thr.z = __fmul_rn(thr.z, fb);
+                }
+                V3 no = vfma(dir, scn.rayStartOffset, ip);
+                p.o[s] = make_float4(no.x, no.y, no.z, __int_as_float(h.x));
+                p.d[s] = make_float4(dir.x, dir.y, dir.z, __int_as_float(inst));
+                p.thr[s] = thr;
+                cont = true;
+                if (train)
+                {
+                    // specular vertices pass radiance on but are not training samples
+                    NrcRecord rec = nrc_record(ip, d, nrm, md, fr / qs, fg / qs, fb / qs, 0.0f);
+                    if (dielectric)
+                        rec.c.y = -1.0f;
+                    p.nrc.vtx[size_t(segment) * size_t(p.nrc.groups) + g] = rec;
+                }
+            }
+            else if (train)
+            {
+                NrcRecord rec = nrc_record(ip, d, nrm, md, 0.0f, 0.0f, 0.0f, 0.0f);
+                if (dielectric)
+                    rec.c.y = -1.0f;
+                p.nrc.vtx[size_t(segment) * size_t(p.nrc.groups) + g] = rec;
+                nrc_end(p.nrc, g, 0.0f, 0.0f, 0.0f, uint32_t(segment + 1));
+            }
+        }
+        else if (train)
+        {
+            // The depth limit cuts the path: its radiance from here on is 0.
+            const ShadeFrame fr = shade_frame(sc, h.x, inst >= 0 ? &in : nullptr, mflags);
+            o = OD ? o : p.o[s];
+            d = OD ? d : p.d[s];
+            V3 ip = vfma(v3(d.x, d.y, d.z), __int_as_float(h.y), v3(o.x, o.y, o.z));
+            NrcRecord rec = nrc_record(ip, d, fr.n, md, 0.0f, 0.0f, 0.0f, 0.0f);
+            if (dielectric)
+                rec.c.y = -1.0f;
+            p.nrc.vtx[size_t(segment) * size_t(p.nrc.groups) + g] = rec;
+            nrc_end(p.nrc, g, 0.0f, 0.0f, 0.0f, uint32_t(segment + 1) | kNrcTermTruncated);
+        }
+    }
+    return cont;
+}
+
+// Appends the slots whose paths go on to the next segment's queue: one
+// atomic per warp (warp-ballot compaction).
+__device__ __forceinline__ void enqueue_continuing(bool cont, int s, unsigned* outCount, int* __restrict__ qout)
+{
+    unsigned mask = __ballot_sync(0xffffffffu, cont);
+    if (mask)
+    {
+        unsigned qbase = 0;
+        if (lane_id() == 0)
+            qbase = atomicAdd(outCount, unsigned(__popc(mask)));
+        qbase = __shfl_sync(0xffffffffu, qbase, 0);
+        if (cont)
+            qout[qbase + __popc(mask & ((1u << lane_id()) - 1u))] = s;
+    }
+}
+
 template <int BLOCK, bool NRC>
 __global__ void __launch_bounds__(BLOCK) k_shade(PassParams p, int segment)
 {
@@ -508,165 +685,10 @@ __global__ void __launch_bounds__(BLOCK) k_shade(PassParams p, int segment)
         if (q < total)
         {
             s = qin[q];
-            int4 h = p.hit[s];
-            const PathChunk& ch = p.chunks[p.chunkOf[s]];
-            const PathScene& scn = p.scenes[ch.scene];
-            const bool train = NRC && nrc_training(p.nrc, uint32_t(s));
-            const uint32_t g = NRC ? uint32_t(s) / uint32_t(max(p.nrc.trainStride, 1)) : 0u;
-            if (h.x < 0)
-            {
-                if (scn.skyOn)
-                {
-                    // GPU extension: misses see a constant sky radiance.
-                    float4 thr = p.thr[s];
-                    float4 r = p.res[s];
-                    r.x = __fmul_rn(thr.x, scn.sky[0]);
-                    r.y = __fmul_rn(thr.y, scn.sky[1]);
-                    r.z = __fmul_rn(thr.z, scn.sky[2]);
-                    p.res[s] = r;
-                }
-                if (train)
-                {
-                    const float on = scn.skyOn ? 1.0f : 0.0f;
-                    nrc_end(p.nrc, g, on * scn.sky[0], on * scn.sky[1], on * scn.sky[2], uint32_t(segment));
-                }
-            }
-            else
-            {
-                const DevScene sc = scn.sc;
-                const float4* tp = reinterpret_cast<const float4*>(sc.tris + h.x);
-                float4 tc = __ldg(tp + 2);
-                uint32_t mi = __float_as_uint(tc.y) & kMetaMaterialMask;
-                const int inst = sc.numInstances > 0 ? h.w : -1;
-                DevInstance in{};
-                if (inst >= 0)
-                {
-                    in = load_instance(sc.instances, inst);
-                    if (in.material >= 0)
-                        mi = uint32_t(in.material);  // Instance::changePrimitive (Instance.cpp:93)
-                }
-                float4 md = __ldg(&sc.mats[mi].diffuse);
-                float4 me = __ldg(&sc.mats[mi].emittance);
-                uint32_t mflags = __float_as_uint(me.w);
-                const bool dielectric = (mflags & kMatDielectric) != 0;
-                float4 thr = p.thr[s];
-                if (mflags & kMatEmissive)
-                {
-                    // sampleColor *= emittance (pathtrace.cl:44-51)
-                    float4 r = p.res[s];
-                    r.x = __fmul_rn(thr.x, me.x);
-                    r.y = __fmul_rn(thr.y, me.y);
-                    r.z = __fmul_rn(thr.z, me.z);
-                    p.res[s] = r;
-                    if (train)
-                        nrc_end(p.nrc, g, me.x, me.y, me.z, uint32_t(segment));
-                }
-                else if (NRC && !train && !dielectric && segment >= p.nrc.termSegment)
-                {
-                    const ShadeFrame fr = shade_frame(sc, h.x, inst >= 0 ? &in : nullptr, mflags);
-                    float4 o = p.o[s];
-                    float4 d = p.d[s];
-                    V3 ip = vfma(v3(d.x, d.y, d.z), __int_as_float(h.y), v3(o.x, o.y, o.z));
-                    lrec = nrc_record(ip, d, fr.n, md, 0.0f, 0.0f, 0.0f, __int_as_float(s));
-                    lookup = true;
-                }
-                else if (segment + 1 < scn.maxPathLength)
-                {
-                    SlotInfo si = slot_info(ch, scn, uint32_t(s));
-                    uint32_t key = stream_key(scn.seed, scn.frame, si.pixelGlobal, si.sample);
-                    bool alive = true;
-                    float qs = 1.0f;
-                    if (scn.rrDepth > 0 && segment + 1 >= scn.rrDepth)
-                    {
-                        float m = fmaxf(thr.x, fmaxf(thr.y, thr.z));
-                        qs = fminf(m, 1.0f);
-                        float xi = stream_float(key, kCounterRoulette + uint32_t(segment));
-                        if (!(xi < qs))
-                            alive = false;
-                        else
-                        {
-                            thr.x = __fdiv_rn(thr.x, qs);
-                            thr.y = __fdiv_rn(thr.y, qs);
-                            thr.z = __fdiv_rn(thr.z, qs);
-                        }
-                    }
-                    const ShadeFrame frm = shade_frame(sc, h.x, inst >= 0 ? &in : nullptr, mflags);
-                    const V3 nrm = frm.n;
-                    float4 o = p.o[s];
-                    float4 d = p.d[s];
-                    float t = __int_as_float(h.y);
-                    V3 ip = vfma(v3(d.x, d.y, d.z), t, v3(o.x, o.y, o.z));
-                    if (alive)
-                    {
-                        float xr = stream_float(key, kCounterBounce + 2u * uint32_t(segment));
-                        float yr = stream_float(key, kCounterBounce + 2u * uint32_t(segment) + 1u);
-                        V3 dir;
-                        float fr, fg, fb;
-                        if (dielectric)
-                        {
-                            dir = dielectric_bounce(v3(d.x, d.y, d.z), nrm, md.w, xr);
-                            fr = fg = fb = 1.0f;
-                        }
-                        else
-                        {
-                            dir = hemisphere_cosine(frm.t, frm.b, nrm, xr, yr);
-                            float alpha = fabsf(vdot(dir, nrm));
-                            // brdf = 2 * reflectance * alpha (PathTracer.cpp:70-71)
-                            fr = __fmul_rn(__fmul_rn(2.0f, md.x), alpha);
-                            fg = __fmul_rn(__fmul_rn(2.0f, md.y), alpha);
-                            fb = __fmul_rn(__fmul_rn(2.0f, md.z), alpha);
-                            thr.x = __fmul_rn(thr.x, fr);
-                            thr.y = __fmul_rn(thr.y, fg);
-                            thr.z = __fmul_rn(thr.z, fb);
-                        }
-                        V3 no = vfma(dir, scn.rayStartOffset, ip);
-                        p.o[s] = make_float4(no.x, no.y, no.z, __int_as_float(h.x));
-                        p.d[s] = make_float4(dir.x, dir.y, dir.z, __int_as_float(inst));
-                        p.thr[s] = thr;
-                        cont = true;
-                        if (train)
-                        {
-                            // specular vertices pass radiance on but are not training samples
-                            NrcRecord rec = nrc_record(ip, d, nrm, md, fr / qs, fg / qs, fb / qs, 0.0f);
-                            if (dielectric)
-                                rec.c.y = -1.0f;
-                            p.nrc.vtx[size_t(segment) * size_t(p.nrc.groups) + g] = rec;
-                        }
-                    }
-                    else if (train)
-                    {
-                        NrcRecord rec = nrc_record(ip, d, nrm, md, 0.0f, 0.0f, 0.0f, 0.0f);
-                        if (dielectric)
-                            rec.c.y = -1.0f;
-                        p.nrc.vtx[size_t(segment) * size_t(p.nrc.groups) + g] = rec;
-                        nrc_end(p.nrc, g, 0.0f, 0.0f, 0.0f, uint32_t(segment + 1));
-                    }
-                }
-                else if (train)
-                {
-                    // The depth limit cuts the path: its radiance from here on is 0.
-                    const ShadeFrame fr = shade_frame(sc, h.x, inst >= 0 ? &in : nullptr, mflags);
-                    float4 o = p.o[s];
-                    float4 d = p.d[s];
-                    V3 ip = vfma(v3(d.x, d.y, d.z), __int_as_float(h.y), v3(o.x, o.y, o.z));
-                    NrcRecord rec = nrc_record(ip, d, fr.n, md, 0.0f, 0.0f, 0.0f, 0.0f);
-                    if (dielectric)
-                        rec.c.y = -1.0f;
-                    p.nrc.vtx[size_t(segment) * size_t(p.nrc.groups) + g] = rec;
-                    nrc_end(p.nrc, g, 0.0f, 0.0f, 0.0f, uint32_t(segment + 1) | kNrcTermTruncated);
-                }
-            }
+            cont = shade_slot<NRC, false>(p, segment, s, p.hit[s], make_float4(0.0f, 0.0f, 0.0f, 0.0f),
+                                          make_float4(0.0f, 0.0f, 0.0f, 0.0f), lookup, lrec);
         }
-        unsigned mask = __ballot_sync(0xffffffffu, cont);
-        if (mask)
-        {
-            unsigned qbase = 0;
-            if (lane_id() == 0)
-                qbase = atomicAdd(outCount, unsigned(__popc(mask)));
-            qbase = __shfl_sync(0xffffffffu, qbase, 0);
-            if (cont)
-                qout[qbase + __popc(mask & ((1u << lane_id()) - 1u))] = s;
-        }
+        enqueue_continuing(cont, s, outCount, qout);
         if (NRC)
         {
             unsigned lmask = __ballot_sync(0xffffffffu, lookup);
@@ -681,6 +703,58 @@ __global__ void __launch_bounds__(BLOCK) k_shade(PassParams p, int segment)
             }
         }
     }
+}
+
+// Extend and shade in one kernel (plain PATH passes over the 4-wide BVH of a
+// single-level scene): each lane walks its slot's ray as k_extend does, then
+// shades the slot at once with the ray still in registers (shade_slot), and
+// the warp appends the slots that go on to the next queue. The hit record
+// never goes through memory and a segment is one launch instead of two; the
+// arithmetic, and so the film, is that of k_extend + k_shade.
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK, (RC_EXTEND_WIDE_MIN_BLOCKS * 128) / BLOCK)
+    k_extend_shade(PassParams p, int segment)
+{
+    const unsigned total = *reinterpret_cast<volatile unsigned*>(&p.counts[segment * 4 + 0]);
+    const int* __restrict__ queue = (segment & 1) ? p.qb : p.qa;
+    int* __restrict__ qout = (segment & 1) ? p.qa : p.qb;
+    unsigned* outCount = &p.counts[(segment + 1) * 4 + 0];
+    int err = 0;
+    unsigned long long done = 0;
+    if (pass_stopped(p))
+        return;
+    if (is_watch_warp(p.monitor, p.budgetNs))
+    {
+        watch_queue(p.monitor, p.budgetNs, p.ctl, &p.counts[segment * 4 + 1], total, kPublishProgress, 0);
+        return;
+    }
+    while (true)
+    {
+        unsigned base = warp_fetch(&p.counts[segment * 4 + 1], 32u);
+        if (base >= total)
+            break;
+        unsigned q = base + lane_id();
+        bool cont = false;
+        int s = -1;
+        if (q < total)
+        {
+            s = queue[q];
+            const DevScene sc = scene_of_slot(p, s);
+            const float4 o = p.o[s];
+            const float4 d = p.d[s];
+            RayF ray = make_ray(v3(o.x, o.y, o.z), v3(d.x, d.y, d.z), 0.0f, FLT_MAX);
+            HitF h{ -1, FLT_MAX, 0.0f, 0.0f, -1 };
+            const bool found = traverse_wide(sc, ray, h, err, __float_as_int(o.w));
+            done++;
+            bool lookup = false;
+            NrcRecord lrec;
+            cont = shade_slot<false, true>(p, segment, s,
+                                           make_int4(found ? h.slot : -1, __float_as_int(h.t), 0, -1), o, d,
+                                           lookup, lrec);
+        }
+        enqueue_continuing(cont, s, outCount, qout);
+    }
+    flush_extend_counts(p, done, TravCount{ 0, 0 }, err);
 }
 
 __global__ void __launch_bounds__(256) k_accumulate(PassParams p)
@@ -776,6 +850,35 @@ cudaError_t extend_t(const PassParams& p, int segment, int block, cudaStream_t s
     return extend_b<ORDER, COUNT, 128>(p, segment, stream, numSMs);
 }
 
+// RC_EXTEND_SHADE=0 in the environment (read once) keeps extend and shade
+// as two kernels per segment in plain passes too.
+bool extend_shade_fused()
+{
+    static const bool on = [] {
+        const char* v = std::getenv("RC_EXTEND_SHADE");
+        return !(v && v[0] == '0');
+    }();
+    return on;
+}
+
+template <int BLOCK>
+cudaError_t extend_shade_b(const PassParams& p, int segment, cudaStream_t stream, int numSMs)
+{
+    auto k = k_extend_shade<BLOCK>;
+    static OccupancyCache occ;
+    k<<<persistent_blocks(k, BLOCK, numSMs, occ), BLOCK, 0, stream>>>(p, segment);
+    return cudaGetLastError();
+}
+
+cudaError_t extend_shade_t(const PassParams& p, int segment, int block, cudaStream_t stream, int numSMs)
+{
+    if (block == 64)
+        return extend_shade_b<64>(p, segment, stream, numSMs);
+    if (block == 256)
+        return extend_shade_b<256>(p, segment, stream, numSMs);
+    return extend_shade_b<128>(p, segment, stream, numSMs);
+}
+
 template <bool COUNT>
 cudaError_t extend_inst(const PassParams& p, int segment, cudaStream_t stream, int numSMs)
 {
@@ -859,10 +962,21 @@ cudaError_t launch_path_segments(const PassParams& p, int order, int counting, c
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess)
         return e;
+    // plain passes over a 4-wide tree: one kernel per segment
+    const bool fused = !p.instanced && order == ORDER_NEAREST && !counting && p.wide && !p.nrc.query &&
+                       !extend_refill() && extend_shade_fused();
     for (int seg = 0; seg < p.segments; ++seg)
     {
         if (extendEvents && (e = cudaEventRecord(extendEvents[2 * seg], stream)) != cudaSuccess)
             return e;
+        if (fused)
+        {
+            if ((e = extend_shade_t(p, seg, shape.extendBlock, stream, numSMs)) != cudaSuccess)
+                return e;
+            if (extendEvents && (e = cudaEventRecord(extendEvents[2 * seg + 1], stream)) != cudaSuccess)
+                return e;
+            continue;
+        }
         if (p.instanced)
             e = counting ? extend_inst<true>(p, seg, stream, numSMs) : extend_inst<false>(p, seg, stream, numSMs);
         else if (order == ORDER_NEAREST)
