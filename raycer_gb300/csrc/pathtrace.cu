@@ -22,6 +22,9 @@
 //   accumulate per pixel, in sample order: c_j = (sum_k L_jk) / P,
 //              film.rgb += w_j * c_j, film.w += w_j (Film::addSample,
 //              Film.cpp:54-59). One thread owns one pixel: deterministic.
+// Uncounted nearest-first passes over the 4-wide BVH run extend and shade of
+// a segment as one kernel (k_extend_shade); the hit record is then never
+// written.
 // Queue counts live on the device, so a pass is a fixed launch sequence the
 // host never waits on (and can be captured in a CUDA graph).
 
@@ -647,6 +650,22 @@ __device__ __forceinline__ bool shade_slot(const PassParams& p, int segment, int
     return cont;
 }
 
+// Appends the cache lookups of the warp's slots to the lookup queue (one
+// atomic per warp).
+__device__ __forceinline__ void enqueue_lookup(bool lookup, const NrcRecord& lrec, const PassParams& p)
+{
+    unsigned lmask = __ballot_sync(0xffffffffu, lookup);
+    if (lmask)
+    {
+        unsigned lbase = 0;
+        if (lane_id() == 0)
+            lbase = atomicAdd(&p.nrc.counters[0], unsigned(__popc(lmask)));
+        lbase = __shfl_sync(0xffffffffu, lbase, 0);
+        if (lookup)
+            p.nrc.query[lbase + __popc(lmask & ((1u << lane_id()) - 1u))] = lrec;
+    }
+}
+
 // Appends the slots whose paths go on to the next segment's queue: one
 // atomic per warp (warp-ballot compaction).
 __device__ __forceinline__ void enqueue_continuing(bool cont, int s, unsigned* outCount, int* __restrict__ qout)
@@ -690,28 +709,20 @@ __global__ void __launch_bounds__(BLOCK) k_shade(PassParams p, int segment)
         }
         enqueue_continuing(cont, s, outCount, qout);
         if (NRC)
-        {
-            unsigned lmask = __ballot_sync(0xffffffffu, lookup);
-            if (lmask)
-            {
-                unsigned lbase = 0;
-                if (lane_id() == 0)
-                    lbase = atomicAdd(&p.nrc.counters[0], unsigned(__popc(lmask)));
-                lbase = __shfl_sync(0xffffffffu, lbase, 0);
-                if (lookup)
-                    p.nrc.query[lbase + __popc(lmask & ((1u << lane_id()) - 1u))] = lrec;
-            }
-        }
+            enqueue_lookup(lookup, lrec, p);
     }
 }
 
-// Extend and shade in one kernel (plain PATH passes over the 4-wide BVH of a
-// single-level scene): each lane walks its slot's ray as k_extend does, then
-// shades the slot at once with the ray still in registers (shade_slot), and
-// the warp appends the slots that go on to the next queue. The hit record
-// never goes through memory and a segment is one launch instead of two; the
-// arithmetic, and so the film, is that of k_extend + k_shade.
-template <int BLOCK>
+// Extend and shade in one kernel (uncounted nearest-first passes over the
+// 4-wide BVH of a single-level scene, plain or with the radiance cache):
+// each lane walks its slot's ray as k_extend does, then shades the slot at
+// once with the ray still in registers (shade_slot), and the warp appends
+// the slots that go on to the next queue (and the cache lookups to the
+// lookup queue). The hit record never goes through memory and a segment is
+// one launch instead of two; the arithmetic, and so the film, is that of the
+// two kernels. (Two-level scenes keep the two kernels: the fused form of
+// their walk spilled and measured no faster.)
+template <int BLOCK, bool NRC>
 __global__ void __launch_bounds__(BLOCK, (RC_EXTEND_WIDE_MIN_BLOCKS * 128) / BLOCK)
     k_extend_shade(PassParams p, int segment)
 {
@@ -735,7 +746,9 @@ __global__ void __launch_bounds__(BLOCK, (RC_EXTEND_WIDE_MIN_BLOCKS * 128) / BLO
             break;
         unsigned q = base + lane_id();
         bool cont = false;
+        bool lookup = false;
         int s = -1;
+        NrcRecord lrec;
         if (q < total)
         {
             s = queue[q];
@@ -746,13 +759,12 @@ __global__ void __launch_bounds__(BLOCK, (RC_EXTEND_WIDE_MIN_BLOCKS * 128) / BLO
             HitF h{ -1, FLT_MAX, 0.0f, 0.0f, -1 };
             const bool found = traverse_wide(sc, ray, h, err, __float_as_int(o.w));
             done++;
-            bool lookup = false;
-            NrcRecord lrec;
-            cont = shade_slot<false, true>(p, segment, s,
-                                           make_int4(found ? h.slot : -1, __float_as_int(h.t), 0, -1), o, d,
-                                           lookup, lrec);
+            cont = shade_slot<NRC, true>(p, segment, s, make_int4(found ? h.slot : -1, __float_as_int(h.t), 0, -1),
+                                         o, d, lookup, lrec);
         }
         enqueue_continuing(cont, s, outCount, qout);
+        if (NRC)
+            enqueue_lookup(lookup, lrec, p);
     }
     flush_extend_counts(p, done, TravCount{ 0, 0 }, err);
 }
@@ -851,7 +863,7 @@ cudaError_t extend_t(const PassParams& p, int segment, int block, cudaStream_t s
 }
 
 // RC_EXTEND_SHADE=0 in the environment (read once) keeps extend and shade
-// as two kernels per segment in plain passes too.
+// as two kernels per segment.
 bool extend_shade_fused()
 {
     static const bool on = [] {
@@ -861,22 +873,26 @@ bool extend_shade_fused()
     return on;
 }
 
-template <int BLOCK>
+template <int BLOCK, bool NRC>
 cudaError_t extend_shade_b(const PassParams& p, int segment, cudaStream_t stream, int numSMs)
 {
-    auto k = k_extend_shade<BLOCK>;
+    auto k = k_extend_shade<BLOCK, NRC>;
     static OccupancyCache occ;
     k<<<persistent_blocks(k, BLOCK, numSMs, occ), BLOCK, 0, stream>>>(p, segment);
     return cudaGetLastError();
 }
 
+// The block sizes of the kernels it replaces: the autotuned extend block for
+// plain passes, 128 threads for cache passes.
 cudaError_t extend_shade_t(const PassParams& p, int segment, int block, cudaStream_t stream, int numSMs)
 {
+    if (p.nrc.query)
+        return extend_shade_b<128, true>(p, segment, stream, numSMs);
     if (block == 64)
-        return extend_shade_b<64>(p, segment, stream, numSMs);
+        return extend_shade_b<64, false>(p, segment, stream, numSMs);
     if (block == 256)
-        return extend_shade_b<256>(p, segment, stream, numSMs);
-    return extend_shade_b<128>(p, segment, stream, numSMs);
+        return extend_shade_b<256, false>(p, segment, stream, numSMs);
+    return extend_shade_b<128, false>(p, segment, stream, numSMs);
 }
 
 template <bool COUNT>
@@ -962,9 +978,9 @@ cudaError_t launch_path_segments(const PassParams& p, int order, int counting, c
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess)
         return e;
-    // plain passes over a 4-wide tree: one kernel per segment
-    const bool fused = !p.instanced && order == ORDER_NEAREST && !counting && p.wide && !p.nrc.query &&
-                       !extend_refill() && extend_shade_fused();
+    // uncounted nearest-first passes over a 4-wide tree: one kernel per segment
+    const bool fused = !p.instanced && order == ORDER_NEAREST && !counting && p.wide && !extend_refill() &&
+                       extend_shade_fused();
     for (int seg = 0; seg < p.segments; ++seg)
     {
         if (extendEvents && (e = cudaEventRecord(extendEvents[2 * seg], stream)) != cudaSuccess)

@@ -1,9 +1,11 @@
-"""Plain PATH passes over the 4-wide BVH run extend and shade as one kernel
-per segment (k_extend_shade); RC_EXTEND_SHADE=0 keeps the two kernels. Both
-give the same films bit for bit, and the float32 oracle's where it models
-the frame: Russian roulette, the sky extension and dielectric materials
-included. The switch is read once per process, so the two-kernel films are
-rendered in a child process."""
+"""Uncounted nearest-first PATH passes over the 4-wide BVH of a single-level
+scene run extend and shade as one kernel per segment (k_extend_shade, plain
+and radiance-cache passes); RC_EXTEND_SHADE=0 keeps the two kernels. Both give
+the same films bit for bit, and the float32 oracle's where it models the
+frame: Russian roulette, the sky extension, dielectric materials and cache
+lookups included (a two-level frame rides along: it takes the two kernels
+in both processes). The switch is read once per process, so the two-kernel
+films are rendered in a child process."""
 
 from __future__ import annotations
 
@@ -25,10 +27,14 @@ pytestmark = pytest.mark.gpu
 
 TESTS = Path(__file__).resolve().parent
 
-# The frames both processes render: (name, scene builder, seed).
+# The frames both processes render: (name, kind, scene, seed). "flat":
+# a single-level scene; "instanced": the two-level form of a scene; "cache":
+# the first frame of a fresh radiance cache (its lookups use the initial
+# weights, so the film does not depend on the order of training samples).
 _FRAMES = """
 import numpy as np
 from raycer_gb300 import scenes
+from raycer_gb300.nrc import RadianceCache
 from raycer_gb300.tracer import CudaTracer, TracerState
 from helpers import small_room
 
@@ -39,17 +45,27 @@ def frames():
                          russian_roulette_depth=3)
     sky = scenes.heightfield_blobs_scene(instances=6, blob_level=2, hf_nx=64, hf_nz=32, width=64, height=36)
     sky.settings.update(max_path_length=6)
-    glass = scenes.heightfield_blobs_instanced(instances=6, blob_level=2, hf_nx=64, hf_nz=32, width=64, height=36,
-                                               dielectric_fraction=0.5).flatten()
-    glass.settings.update(max_path_length=8)
-    return [("room_rr", room, 3), ("sky", sky, 4), ("glass", glass, 5)]
+    two_level = scenes.heightfield_blobs_instanced(instances=6, blob_level=2, hf_nx=64, hf_nz=32, width=64,
+                                                   height=36, dielectric_fraction=0.5)
+    two_level.settings.update(max_path_length=8)
+    glass = two_level.flatten()
+    box = scenes.heightfield_blobs_scene(instances=6, blob_level=2, hf_nx=64, hf_nz=32, width=96, height=54,
+                                         enclosed=True)
+    return [("room_rr", "flat", room, 3), ("sky", "flat", sky, 4), ("glass", "flat", glass, 5),
+            ("glass_two_level", "instanced", two_level, 6), ("cache_box", "cache", box, 7)]
 
 
-def render(sc, seed):
+def render(kind, sc, seed):
     with CudaTracer(0) as t:
-        t.initializeBuffers(sc, seed=seed)
+        if kind == "instanced":
+            t.initializeInstanced(sc, seed=seed)
+        else:
+            t.initializeBuffers(sc, seed=seed)
         t.initializeImageBuffers(sc.width, sc.height)
+        cache = RadianceCache(t) if kind == "cache" else None
         t.run(TracerState(scene=sc, filmWidth=sc.width, filmHeight=sc.height, pixelCount=sc.width * sc.height))
+        if cache is not None:
+            assert cache.stats()["lookups"] > 0
         return t.read_film().copy()
 """
 
@@ -59,7 +75,7 @@ sys.path.insert(0, {root!r})
 sys.path.insert(0, {tests!r})
 import numpy as np
 exec(compile({frames!r}, "frames", "exec"))
-out = {{name: render(sc, seed) for name, sc, seed in frames()}}
+out = {{name: render(kind, sc, seed) for name, kind, sc, seed in frames()}}
 np.savez({path!r}, **out)
 print("two-kernel films written")
 """
@@ -80,8 +96,8 @@ def test_one_kernel_and_two_kernel_films_are_identical(tmp_path):
     assert res.returncode == 0, res.stdout[-2000:] + res.stderr[-4000:]
     two = np.load(path)
     ns = _frames_module()
-    for name, sc, seed in ns["frames"]():
-        one = ns["render"](sc, seed)
+    for name, kind, sc, seed in ns["frames"]():
+        one = ns["render"](kind, sc, seed)
         assert np.array_equal(one, two[name]), f"{name}: {(one != two[name]).any(axis=1).sum()} pixels differ"
         assert one[:, :3].max() > 0.0, name
 
