@@ -205,6 +205,12 @@ struct RenderWatch
     uint64_t* pixels = nullptr;
     uint64_t seen = 0;
 };
+// The device address through which kernels on h's GPU can read or write
+// the host buffer [p, p + bytes) in place (page-locked memory, or pageable
+// memory whose pages are resident where the device uses the host page
+// tables), or null where they should not.
+void* device_view(rc_tracer* h, const void* p, size_t bytes);
+
 // Blocks until `done` has completed; while it waits, raises the device's
 // cancel word once the caller's flag is set and stores every larger
 // progress value it reads into the caller's counter (relaxed atomic stores).

@@ -6,6 +6,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -397,9 +398,30 @@ rc_status rc_resolve(rc_tracer* h, float* out_rgba)
     rc_status s = grow(h, &h->dTone, &h->capTone, tone_partials_bytes(h->filmPixels), "allocate tone scratch");
     if (s != RC_OK)
         return s;
+    const rc_tonemapper& t = h->tonemapper;
+    // Where the device reaches the caller's buffer (page-locked memory, or
+    // resident pageable memory on a Grace host) and it is 16-byte aligned,
+    // the mapping kernel writes the image there over the host link; else it
+    // writes a device image that one copy brings back (RC_RESOLVE_COPY=1 in
+    // the environment forces the copy).
+    static const bool forceCopy = [] {
+        const char* v = std::getenv("RC_RESOLVE_COPY");
+        return v && v[0] == '1';
+    }();
+    float4* direct = nullptr;
+    if (!forceCopy && (reinterpret_cast<uintptr_t>(out_rgba) & 15u) == 0)
+        direct = static_cast<float4*>(device_view(h, out_rgba, size_t(h->filmPixels) * sizeof(float4)));
+    if (direct)
+    {
+        RC_CUDA_TRY(h,
+                    launch_tonemap(h->dFilm, h->filmPixels, t.type, t.apply_gamma, t.should_clamp, t.gamma, t.key,
+                                   h->dTone, direct, h->stream, h->numSMs),
+                    "launch tone mapping");
+        RC_CUDA_TRY(h, cudaStreamSynchronize(h->stream), "resolve");
+        return RC_OK;
+    }
     if ((s = grow(h, &h->dImage, &h->capImage, size_t(h->filmPixels) * sizeof(float4), "allocate image")) != RC_OK)
         return s;
-    const rc_tonemapper& t = h->tonemapper;
     RC_CUDA_TRY(h,
                 launch_tonemap(h->dFilm, h->filmPixels, t.type, t.apply_gamma, t.should_clamp, t.gamma, t.key,
                                h->dTone, static_cast<float4*>(h->dImage), h->stream, h->numSMs),

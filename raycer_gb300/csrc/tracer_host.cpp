@@ -4,6 +4,8 @@
 // (src/OpenCL/CLTracer.cpp, src/OpenCL/CLScene.cpp) with CUDA underneath.
 
 #include <cuda_runtime.h>
+#include <sys/mman.h>
+#include <unistd.h>
 
 #include <algorithm>
 #include <cstdlib>
@@ -1090,32 +1092,6 @@ rc_status rc_cast(rc_tracer* h, const rc_ray* rays, int64_t n, int32_t any_hit, 
     return RC_OK;
 }
 
-// Device address of a caller's host buffer when kernels may access it in
-// place: page-locked memory mapped into the device's address space, or any
-// memory on a device that reads pageable memory coherently (Grace-class
-// hosts). nullptr otherwise.
-void* device_view(rc_tracer* h, const void* p)
-{
-    cudaPointerAttributes a{};
-    if (cudaPointerGetAttributes(&a, p) != cudaSuccess)
-    {
-        cudaGetLastError();
-        return nullptr;
-    }
-    if (a.type == cudaMemoryTypeHost && a.devicePointer && a.device == h->device)
-        return a.devicePointer;
-    if (a.type == cudaMemoryTypeManaged || (a.type == cudaMemoryTypeDevice && a.device == h->device))
-        return const_cast<void*>(p);
-    int pageable = 0;
-    if (a.type == cudaMemoryTypeUnregistered &&
-        cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccessUsesHostPageTables, h->device) ==
-            cudaSuccess &&
-        pageable)
-        return const_cast<void*>(p);
-    cudaGetLastError();
-    return nullptr;
-}
-
 rc_status rc_cast_with_shadow(rc_tracer* h, const rc_ray* rays, int64_t n, int32_t order, rc_cast_pixel* out)
 {
     if (!h)
@@ -1139,8 +1115,8 @@ rc_status rc_cast_with_shadow(rc_tracer* h, const rc_ray* rays, int64_t n, int32
     const char* forceCopy = std::getenv("RC_CAST_COPY");
     if (!(forceCopy && forceCopy[0] == '1'))
     {
-        void* vr = device_view(h, rays);
-        void* vo = vr ? device_view(h, out) : nullptr;
+        void* vr = device_view(h, rays, size_t(n) * sizeof(rc_ray));
+        void* vo = vr ? device_view(h, out, size_t(n) * sizeof(rc_cast_pixel)) : nullptr;
         if (vr && vo && ((reinterpret_cast<uintptr_t>(vr) | reinterpret_cast<uintptr_t>(vo)) & 15u) == 0)
         {
             // shadow queue (8 B per entry) + the shadow rays' origins (16 B, device
@@ -1302,6 +1278,57 @@ rc_status rc_sync(rc_tracer* h)
 
 namespace rcx
 {
+
+namespace
+{
+// Whether every page of [p, p + bytes) is resident (mincore). A kernel that
+// writes or reads pageable memory whose pages are not populated yet takes a
+// fault per page on the device side (milliseconds for a fresh 33 MB image);
+// such buffers go through a copy instead.
+bool host_resident(const void* p, size_t bytes)
+{
+    static const size_t page = [] {
+        const long v = sysconf(_SC_PAGESIZE);
+        return v > 0 ? size_t(v) : size_t(4096);
+    }();
+    const uintptr_t a = reinterpret_cast<uintptr_t>(p) & ~uintptr_t(page - 1);
+    const uintptr_t e = reinterpret_cast<uintptr_t>(p) + bytes;
+    const size_t pages = (e - a + page - 1) / page;
+    std::vector<unsigned char> vec(pages);
+    if (mincore(reinterpret_cast<void*>(a), pages * page, vec.data()) != 0)
+        return false;
+    for (unsigned char c : vec)
+        if (!(c & 1))
+            return false;
+    return true;
+}
+}  // namespace
+
+// Device address of a caller's host buffer of `bytes` bytes when kernels may
+// access it in place: page-locked memory mapped into the device's address
+// space, or pageable memory whose pages are all resident on a device that
+// reads pageable memory coherently (Grace-class hosts). nullptr otherwise.
+void* device_view(rc_tracer* h, const void* p, size_t bytes)
+{
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess)
+    {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type == cudaMemoryTypeHost && a.devicePointer && a.device == h->device)
+        return a.devicePointer;
+    if (a.type == cudaMemoryTypeManaged || (a.type == cudaMemoryTypeDevice && a.device == h->device))
+        return const_cast<void*>(p);
+    int pageable = 0;
+    if (a.type == cudaMemoryTypeUnregistered &&
+        cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccessUsesHostPageTables, h->device) ==
+            cudaSuccess &&
+        pageable && host_resident(p, bytes))
+        return const_cast<void*>(p);
+    cudaGetLastError();
+    return nullptr;
+}
 
 rc_status wait_render(rc_tracer* h, RenderWatch* w, cudaEvent_t done)
 {

@@ -36,3 +36,38 @@ def test_reinhard_matches_reference(key, gamma, clamp, ag):
     o64 = oracle.tonemap64(lin, key, gamma, bool(clamp), bool(ag))
     assert np.nanmax(np.abs(out - o64)) <= 4e-6 * scale
     assert np.all(out[:, 3] == 1.0)
+
+
+@pytest.mark.parametrize("pinned", [False, True])
+def test_resolve_in_place_equals_copied_image(pinned):
+    """rc_resolve maps the film straight into the caller's buffer where the
+    device reaches it (here: any memory on a Grace host, or page-locked
+    memory); the image equals rc_tonemap_film's, which copies through device
+    buffers, bit for bit. A buffer that is not 16-byte aligned takes the
+    copy and gives the same image."""
+    import ctypes as C
+
+    import torch
+
+    from raycer_gb300.tracer import TracerState
+
+    from helpers import small_room
+
+    sc = small_room(width=96, height=64)
+    n = sc.width * sc.height
+    with CudaTracer(0) as t:
+        t.initializeBuffers(sc, seed=2)
+        t.initializeImageBuffers(sc.width, sc.height)
+        t.run(TracerState(scene=sc, filmWidth=sc.width, filmHeight=sc.height, pixelCount=n))
+        ref = t.tonemap_film(t.read_film())
+        if pinned:
+            buf = torch.empty((n, 4), dtype=torch.float32, pin_memory=True)
+            assert N.lib().rc_resolve(t.handle, C.c_void_p(buf.data_ptr())) == N.RC_OK
+            img = buf.numpy()
+        else:
+            img = t.downloadImage().reshape(n, 4)
+        raw = np.zeros(n * 4 + 1, np.float32)          # one float off the 16-byte grid
+        assert N.lib().rc_resolve(t.handle, C.c_void_p(raw.ctypes.data + 4)) == N.RC_OK
+    assert np.array_equal(img, ref)
+    assert np.array_equal(raw[1:].reshape(n, 4), ref)
+    assert np.isfinite(ref).all() and ref[:, :3].max() > 0.0
