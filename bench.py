@@ -820,62 +820,30 @@ def run_nrc(args, rank, world):
 
 def run_cpu(args, rank, world):
     """CPU path-tracing throughput on this host's cores (the float64 port of
-    the reference's path tracer, all threads): the room at 320x240, 16 spp,
-    depth 4, a full frame (best of 3); and an estimate for the 64-scene
-    batch, each triangle bucket's first scene sampled on
-    16,384 pixels at depth 8 without roulette (the reference has none), its
-    Mrays/s and rays per sample applied to every scene of the bucket."""
+    the reference's path tracer, all threads, its own BVH and camera): the
+    room at 320x240, 16 spp, depth 4, a full frame (best of 3); and the
+    64-scene batch on its size-sampled eighth (batch_cpu_baseline)."""
     if rank != 0:
         return 0
     import oracle
     from raycer_gb300 import scenes
-    from raycer_gb300.tracer import camera_record
 
-    def cam64_of(sc):
-        cam = camera_record(sc)
-        return np.array(list(cam.position) + list(cam.right) + list(cam.up) + list(cam.image_plane_center) +
-                        [cam.aspect_ratio, cam.image_plane_width, cam.image_plane_height], np.float64)
-
-    threads = os.cpu_count() or 1
+    threads = cpu_threads()
     sc = scenes.room_scene()
     orc = oracle.Oracle(sc)
     best = None
     for _ in range(3):
-        _, rays, sec = orc.render_path64(cam64_of(sc), sc.width, sc.width * sc.height, 4, 1, 4, seed=1,
+        _, rays, sec = orc.render_path64(oracle.camera64_of(sc), sc.width, sc.width * sc.height, 4, 1, 4, seed=1,
                                          threads=threads)
         if best is None or sec < best[1]:
             best = (rays, sec)
-    batch = scenes.batch_scenes()
-    edges = [0, 16_000, 128_000, 1_000_000]
-
-    def bucket(n):
-        return max(i for i, e in enumerate(edges) if n >= e)
-
-    per = {}
-    for b in range(len(edges)):
-        members = [m for m in batch if bucket(m.triangle_count) == b]
-        if not members:
-            continue
-        m = members[0]
-        ms = int(m.settings["multi_sample_count_sqrt"])
-        count = min(m.width * m.height, 16384)
-        _, rays, sec = oracle.Oracle(m).render_path64(cam64_of(m), m.width, count, 8, 1, ms, seed=1, threads=threads)
-        per[b] = {"sample_scene_triangles": m.triangle_count, "scenes": len(members),
-                  "mrays_per_s": round(rays / sec / 1e6, 4), "rays_per_sample": round(rays / (count * ms * ms), 4)}
-    est_sec = est_rays = 0.0
-    for m in batch:
-        e = per[bucket(m.triangle_count)]
-        ms = int(m.settings["multi_sample_count_sqrt"])
-        r = m.width * m.height * ms * ms * e["rays_per_sample"]
-        est_rays += r
-        est_sec += r / (e["mrays_per_s"] * 1e6)
+    orc.close()
+    batch = batch_cpu_baseline(scenes.batch_scenes(seed=3))
     print(json.dumps({"metric": "Mrays/s", "workload": "cpu", "unit": "Mrays/s", "higher_is_better": True,
                       "kind": "port", "cores": threads,
                       "config0_room": {"rays": int(best[0]), "seconds": round(best[1], 4),
                                        "mrays_per_s": round(best[0] / best[1] / 1e6, 2)},
-                      "config2_batch_estimate": {"cpu_seconds": round(est_sec, 1), "cpu_rays": int(est_rays),
-                                                 "mrays_per_s": round(est_rays / est_sec / 1e6, 3),
-                                                 "buckets": per}}))
+                      "config2_batch": batch}))
     return 0
 
 
