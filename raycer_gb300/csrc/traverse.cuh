@@ -68,6 +68,44 @@ __device__ __forceinline__ void load_node(const DevNode* __restrict__ nodes, int
     l = __ldg(reinterpret_cast<const int4*>(p + 3));
 }
 
+// The test of one leaf triangle in traverse(): nonShadowing triangles are
+// skipped by any-hit rays (Triangle.cpp:55); returns true when an any-hit
+// ray has found its occluder (the walk ends), else updates the closest hit
+// (the reference order keeps the later of equal distances, nearest-first
+// the larger slot).
+template <bool ANY_HIT, int ORDER, bool COUNT>
+__device__ __forceinline__ bool leaf_test(const RayF& ray, HitF& hit, bool& found, TravCount& cnt, int slot, int skip,
+                                          const float4& ta, const float4& tb, const float4& tc)
+{
+    if (slot == skip)
+        return false;
+    if (ANY_HIT && (__float_as_uint(tc.y) & kMetaNonShadowing))
+        return false;
+    if (COUNT)
+        cnt.tris++;
+    float t, u, v;
+    if (!tri_hit(ray, v3(ta.x, ta.y, ta.z), v3(ta.w, tb.x, tb.y), v3(tb.z, tb.w, tc.x), t, u, v))
+        return false;
+    if (ANY_HIT)
+    {
+        hit.slot = slot;
+        hit.t = t;
+        hit.u = u;
+        hit.v = v;
+        return true;
+    }
+    const bool take = ORDER == ORDER_REF ? !(t > hit.t) : (t < hit.t || (t == hit.t && slot > hit.slot));
+    if (take)
+    {
+        hit.slot = slot;
+        hit.t = t;
+        hit.u = u;
+        hit.v = v;
+        found = true;
+    }
+    return false;
+}
+
 // Returns true if any triangle was accepted. `hit` must be initialised by
 // the caller (slot -1, t = FLT_MAX for a fresh query). `err` is set to 1 on
 // a stack overflow (the ray is then abandoned; the host reports it).
@@ -158,42 +196,12 @@ __device__ __forceinline__ bool traverse(const DevScene& sc, const RayF& ray, Hi
             int count = leaf & ((1 << kLeafCountBits) - 1);
             for (int i = 0; i < count; ++i)
             {
-                int slot = start + i;
-                if (slot == skip)
-                    continue;
+                const int slot = start + i;
                 const float4* tp = reinterpret_cast<const float4*>(sc.tris + slot);
-                float4 ta = __ldg(tp + 0);
-                float4 tb = __ldg(tp + 1);
-                float4 tc = __ldg(tp + 2);
-                if (ANY_HIT && (__float_as_uint(tc.y) & kMetaNonShadowing))
-                    continue;
-                if (COUNT)
-                    cnt.tris++;
-                float t, u, v;
-                if (tri_hit(ray, v3(ta.x, ta.y, ta.z), v3(ta.w, tb.x, tb.y), v3(tb.z, tb.w, tc.x), t, u, v))
-                {
-                    if (ANY_HIT)
-                    {
-                        hit.slot = slot;
-                        hit.t = t;
-                        hit.u = u;
-                        hit.v = v;
-                        return true;
-                    }
-                    bool take;
-                    if (ORDER == ORDER_REF)
-                        take = !(t > hit.t);
-                    else
-                        take = t < hit.t || (t == hit.t && slot > hit.slot);
-                    if (take)
-                    {
-                        hit.slot = slot;
-                        hit.t = t;
-                        hit.u = u;
-                        hit.v = v;
-                        found = true;
-                    }
-                }
+                if (slot != skip &&
+                    leaf_test<ANY_HIT, ORDER, COUNT>(ray, hit, found, cnt, slot, skip, __ldg(tp + 0), __ldg(tp + 1),
+                                                     __ldg(tp + 2)))
+                    return true;
             }
         }
 
@@ -328,6 +336,24 @@ struct WideWalk
     bool found;
 };
 
+// The closest-hit test of one leaf triangle in the 4-wide walk.
+__device__ __forceinline__ void wide_leaf_test(const RayF& ray, HitF& hit, WideWalk& w, int slot, int skip,
+                                               const float4& ta, const float4& tb, const float4& tc)
+{
+    if (slot == skip)
+        return;
+    float t, u, v;
+    if (tri_hit(ray, v3(ta.x, ta.y, ta.z), v3(ta.w, tb.x, tb.y), v3(tb.z, tb.w, tc.x), t, u, v) &&
+        (t < hit.t || (t == hit.t && slot > hit.slot)))
+    {
+        hit.slot = slot;
+        hit.t = t;
+        hit.u = u;
+        hit.v = v;
+        w.found = true;
+    }
+}
+
 // One step of the 4-wide walk: a node fetch (entering its nearest child hit
 // within the current closest distance, the others pushed) or a leaf's
 // triangle tests; where no child is entered, the pop of the next stack entry
@@ -395,25 +421,21 @@ __device__ __forceinline__ bool wide_step(const DevNode4* __restrict__ wide, con
         const int leaf = ~w.cur;
         const int start = leaf >> kLeafCountBits;
         const int count = leaf & ((1 << kLeafCountBits) - 1);
-        for (int i = 0; i < count; ++i)
+        // Two triangles per iteration, both fetched before either is tested
+        // (the second index clamped to the leaf: an odd leaf fetches its last
+        // triangle twice and tests it once), so a leaf's fetches overlap.
+        // The accepted hit does not depend on the order of the tests.
+        for (int i = 0; i < count; i += 2)
         {
-            const int slot = start + i;
-            if (slot == skip)
-                continue;
-            const float4* tp = reinterpret_cast<const float4*>(tris + slot);
-            const float4 ta = __ldg(tp + 0);
-            const float4 tb = __ldg(tp + 1);
-            const float4 tc = __ldg(tp + 2);
-            float t, u, v;
-            if (tri_hit(ray, v3(ta.x, ta.y, ta.z), v3(ta.w, tb.x, tb.y), v3(tb.z, tb.w, tc.x), t, u, v) &&
-                (t < hit.t || (t == hit.t && slot > hit.slot)))
-            {
-                hit.slot = slot;
-                hit.t = t;
-                hit.u = u;
-                hit.v = v;
-                w.found = true;
-            }
+            const int s0 = start + i;
+            const int s1 = start + min(i + 1, count - 1);
+            const float4* p0 = reinterpret_cast<const float4*>(tris + s0);
+            const float4* p1 = reinterpret_cast<const float4*>(tris + s1);
+            const float4 a0 = __ldg(p0 + 0), b0 = __ldg(p0 + 1), c0 = __ldg(p0 + 2);
+            const float4 a1 = __ldg(p1 + 0), b1 = __ldg(p1 + 1), c1 = __ldg(p1 + 2);
+            wide_leaf_test(ray, hit, w, s0, skip, a0, b0, c0);
+            if (i + 1 < count)
+                wide_leaf_test(ray, hit, w, s1, skip, a1, b1, c1);
         }
     }
     // pop
@@ -548,6 +570,7 @@ __device__ __forceinline__ bool traverse_packet(const DevScene& sc, const RayF& 
             const int start = leaf >> kLeafCountBits;
             const int count = leaf & ((1 << kLeafCountBits) - 1);
             const bool in = (curMask & bit) != 0;
+            TravCount none{ 0, 0 };
             for (int i = 0; i < count; ++i)
             {
                 const int slot = start + i;
@@ -555,25 +578,8 @@ __device__ __forceinline__ bool traverse_packet(const DevScene& sc, const RayF& 
                 const float4 ta = __ldg(tp + 0);
                 const float4 tb = __ldg(tp + 1);
                 const float4 tc = __ldg(tp + 2);
-                if (!in || slot == skip)
-                    continue;
-                float t, u, v;
-                if (tri_hit(ray, v3(ta.x, ta.y, ta.z), v3(ta.w, tb.x, tb.y), v3(tb.z, tb.w, tc.x), t, u, v))
-                {
-                    bool take;
-                    if (ORDER == ORDER_REF)
-                        take = !(t > hit.t);
-                    else
-                        take = t < hit.t || (t == hit.t && slot > hit.slot);
-                    if (take)
-                    {
-                        hit.slot = slot;
-                        hit.t = t;
-                        hit.u = u;
-                        hit.v = v;
-                        found = true;
-                    }
-                }
+                if (in)
+                    leaf_test<false, ORDER, false>(ray, hit, found, none, slot, skip, ta, tb, tc);
             }
         }
 
