@@ -500,7 +500,8 @@ __device__ __forceinline__ bool shade_slot(const PassParams& p, int segment, int
                                            bool& lookup, NrcRecord& lrec)
 {
     bool cont = false;
-    const PathChunk& ch = p.chunks[p.chunkOf[s]];
+    // a one-scene pass has one chunk: no dependent load of the slot's chunk
+    const PathChunk& ch = p.chunks[p.singleScene && p.numChunks == 1 ? 0 : p.chunkOf[s]];
     const PathScene& scn = p.scenes[ch.scene];
     const bool train = NRC && nrc_training(p.nrc, uint32_t(s));
     const uint32_t g = NRC ? uint32_t(s) / uint32_t(max(p.nrc.trainStride, 1)) : 0u;
