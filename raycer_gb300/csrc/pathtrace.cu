@@ -58,6 +58,12 @@ namespace
 #ifndef RC_EXTEND_WIDE_MIN_BLOCKS
 #define RC_EXTEND_WIDE_MIN_BLOCKS 9
 #endif
+// The same for the extend + shade kernel of radiance-cache passes, whose
+// shading also writes training vertices and lookups: at 9 blocks it spilled
+// 96 bytes, at 8 (64 registers) 52, and cache frames ran 1 % faster.
+#ifndef RC_EXTEND_SHADE_NRC_MIN_BLOCKS
+#define RC_EXTEND_SHADE_NRC_MIN_BLOCKS 8
+#endif
 
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
 
@@ -724,7 +730,8 @@ __global__ void __launch_bounds__(BLOCK) k_shade(PassParams p, int segment)
 // two kernels. (Two-level scenes keep the two kernels: the fused form of
 // their walk spilled and measured no faster.)
 template <int BLOCK, bool NRC>
-__global__ void __launch_bounds__(BLOCK, (RC_EXTEND_WIDE_MIN_BLOCKS * 128) / BLOCK)
+__global__ void __launch_bounds__(BLOCK,
+                                  ((NRC ? RC_EXTEND_SHADE_NRC_MIN_BLOCKS : RC_EXTEND_WIDE_MIN_BLOCKS) * 128) / BLOCK)
     k_extend_shade(PassParams p, int segment)
 {
     const unsigned total = *reinterpret_cast<volatile unsigned*>(&p.counts[segment * 4 + 0]);
