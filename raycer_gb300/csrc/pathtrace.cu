@@ -492,15 +492,18 @@ __device__ __forceinline__ void nrc_end(const NrcPass& n, uint32_t g, float r, f
     n.term[g] = make_float4(r, gg, b, __uint_as_float(flags | kNrcTermActive));
 }
 
-// NRC: training paths record every vertex (query + bounce factor) and their
-// terminal radiance; other paths end at the hit of segment termSegment with
-// a cache lookup (res gets thr * cache after the last segment).
 // The shade stage for one queued slot whose extend found hit h (slot, t as
-// bits, u, v; x < 0: a miss): the miss, emitter, cache-lookup, bounce and
-// depth-limit cases above. Returns whether the path goes on (the slot joins
-// the next segment's queue); a cache lookup sets `lookup` and `lrec`. With
-// OD the caller passes the slot's ray (o, d) it already holds, else they are
-// read from the path state.
+// bits, u, v; x < 0: a miss): a miss sees the sky (or black), an emitter
+// ends the path with thr * emittance, the scene's last segment ends it, and
+// otherwise optional Russian roulette, the cosine bounce and
+// thr *= 2 * rho * |w.n| (PathTracer.cpp:58-72). With the radiance cache,
+// training paths record every vertex (query + bounce factor) and their
+// terminal radiance, and other paths end at the hit of segment termSegment
+// with a cache lookup (res gets thr * cache after the last segment).
+// Returns whether the path goes on (the slot joins the next segment's
+// queue); a cache lookup sets `lookup` and `lrec`. With OD the caller passes
+// the slot's ray (o, d) it already holds, else they are read from the path
+// state.
 template <bool NRC, bool OD>
 __device__ __forceinline__ bool shade_slot(const PassParams& p, int segment, int s, int4 h, float4 o, float4 d,
                                            bool& lookup, NrcRecord& lrec)
@@ -689,6 +692,8 @@ __device__ __forceinline__ void enqueue_continuing(bool cont, int s, unsigned* o
     }
 }
 
+// The shade stage as its own kernel (passes that keep extend and shade
+// apart): shade_slot for each queued slot, from the extend's hit records.
 template <int BLOCK, bool NRC>
 __global__ void __launch_bounds__(BLOCK) k_shade(PassParams p, int segment)
 {
