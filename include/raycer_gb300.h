@@ -348,7 +348,12 @@ rc_status rc_set_time_budget(rc_tracer* h, double milliseconds);
 /* Film::generateToneMappedImage (Film.cpp:61-69) with the handle's tone
  * mapper (ReinhardToneMapper::apply, ReinhardToneMapper.cpp:18-86), and the
  * download of CLTracer::downloadImage (CLTracer.cpp:307): out_rgba =
- * film pixels x 4 floats on the host. */
+ * film pixels x 4 floats on the host (or in device memory). The mapping
+ * kernel writes the buffer in place when the device can reach it and it is
+ * 16-byte aligned (device memory, page-locked memory, or pageable memory
+ * whose pages are all resident on a host whose GPU uses its page tables);
+ * otherwise through one copy. Per pixel in float32 (the reference: double),
+ * within 4e-6 of the reference's image. */
 rc_status rc_resolve(rc_tracer* h, float* out_rgba);
 
 /* Linear film resolve (cumulativeColor / filterWeightSum) to the host, and
